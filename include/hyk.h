@@ -1,0 +1,237 @@
+/*
+ * hyk.h - C ABI of the GB300 batch Taylor integrator (libhyk.so).
+ *
+ * This library replaces the hot path of heyoka.py's batch-mode integrator
+ * (heyoka::taylor_adaptive_batch<double>, driven from
+ * heyoka/expose_batch_integrators.cpp) with FP64 CUDA kernels generated per
+ * ODE system and compiled with NVRTC for sm_103a.
+ *
+ * Conventions
+ *  - Plain C types only: no C++ exceptions, no torch types.  Every entry point
+ *    returns 0 on success or a negative HYK_ERR_* code; the message of the
+ *    last failure on the calling thread is returned by hyk_last_error().
+ *  - Device arrays are borrowed: the caller allocates them (e.g. as torch
+ *    tensors) and keeps them alive until the work on `stream` completes.  The
+ *    library allocates device memory only for compiled modules.
+ *  - Per-lane arrays use the reference's [var][lane] row-major layout: state
+ *    is (n_eq, n_lanes), pars (n_pars, n_lanes), Taylor coefficients
+ *    (n_eq, order + 1, n_lanes), grid output (n_grid, n_eq, n_lanes)
+ *    (heyoka/expose_batch_integrators.cpp:116-119, :378-382, :481-483).
+ *  - `stream` is a cudaStream_t / CUstream passed as void* (NULL = legacy
+ *    default stream).  All work is stream-ordered; nothing blocks except
+ *    hyk_module_create().
+ */
+#ifndef HYK_H
+#define HYK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Taylor decomposition (input to module creation and to the oracle) ---- */
+
+/* Elementary operations of the Taylor decomposition.  Mirrors the u-variable
+ * vocabulary of the reference's decomposition property
+ * (heyoka/expose_batch_integrators.cpp:231). */
+enum {
+    HYK_OP_ADD = 0,
+    HYK_OP_SUB = 1,
+    HYK_OP_MUL = 2,
+    HYK_OP_DIV = 3,
+    HYK_OP_NEG = 4,
+    HYK_OP_SQUARE = 5,
+    HYK_OP_SQRT = 6,
+    HYK_OP_POW = 7, /* exponent: b.num (b.kind == HYK_ARG_NUM) */
+    HYK_OP_EXP = 8,
+    HYK_OP_LOG = 9,
+    HYK_OP_SIN = 10, /* aux = index of the partner cosine u-variable */
+    HYK_OP_COS = 11  /* aux = index of the partner sine u-variable */
+};
+
+enum { HYK_ARG_NONE = 0, HYK_ARG_U = 1, HYK_ARG_NUM = 2, HYK_ARG_PAR = 3, HYK_ARG_TIME = 4 };
+
+typedef struct hyk_arg {
+    int32_t kind; /* HYK_ARG_* */
+    int32_t idx;  /* u-variable index (HYK_ARG_U) or parameter index (HYK_ARG_PAR) */
+    double num;   /* value (HYK_ARG_NUM) */
+} hyk_arg_t;
+
+typedef struct hyk_uop {
+    int32_t op;  /* HYK_OP_* */
+    int32_t aux; /* sin/cos partner, else -1 */
+    hyk_arg_t a;
+    hyk_arg_t b; /* kind HYK_ARG_NONE for unary operations */
+} hyk_uop_t;
+
+/* u-variables 0..n_eq-1 are the state variables, u-variable n_eq + k is
+ * defined by ops[k] (topological order), rhs[i] is the right-hand side of
+ * state variable i. */
+typedef struct hyk_decomp {
+    uint32_t n_eq;
+    uint32_t n_ops;
+    uint32_t n_pars;
+    uint32_t reserved;
+    const hyk_uop_t *ops;
+    const hyk_arg_t *rhs;
+} hyk_decomp_t;
+
+/* ---- taylor_outcome (values of heyoka/core.cpp:324-329, as printed in
+ *      doc/notebooks/Batch mode overview.ipynb) ---- */
+#define HYK_OUTCOME_SUCCESS (-4294967297LL)
+#define HYK_OUTCOME_STEP_LIMIT (-4294967298LL)
+#define HYK_OUTCOME_TIME_LIMIT (-4294967299LL)
+#define HYK_OUTCOME_ERR_NF_STATE (-4294967300LL)
+#define HYK_OUTCOME_CB_STOP (-4294967301LL)
+
+/* ---- error codes ---- */
+#define HYK_OK 0
+#define HYK_ERR_INVALID (-1)  /* invalid argument */
+#define HYK_ERR_CUDA (-2)     /* CUDA driver / runtime failure */
+#define HYK_ERR_NVRTC (-3)    /* kernel compilation failure */
+#define HYK_ERR_UNSUPPORTED (-4)
+#define HYK_ERR_TIMEOUT (-5)  /* a bounded device wait gave up */
+
+/* ---- GPU module: one decomposition compiled at one Taylor order ---- */
+
+typedef struct hyk_module hyk_module;
+
+typedef struct hyk_config {
+    uint32_t block_lanes;  /* lanes (threads) per CTA; 0 = autotune */
+    uint32_t persist_ctas; /* CTAs per SM of the persistent kernel; 0 = occupancy-derived */
+    uint32_t flags;        /* HYK_CFG_* */
+    uint32_t reserved;
+} hyk_config_t;
+
+#define HYK_CFG_PIN_ARITH 1u /* oracle "pin" arithmetic: no FMA, divide by n (slower; for cross-checks) */
+
+typedef struct hyk_module_info {
+    uint32_t n_eq, n_pars, order, n_u;
+    uint32_t block_lanes;        /* threads per CTA used by the kernels */
+    uint32_t smem_per_lane;      /* bytes of shared-memory jet storage per lane */
+    uint32_t regs_per_thread;    /* from the compiled kernel */
+    uint32_t ctas_per_sm;        /* resident CTAs per SM of the propagate kernel */
+    uint32_t n_sm;
+    uint32_t reserved;
+    double flops_per_step;       /* algorithmic FP64 flops of one Taylor step of one lane */
+    double compile_seconds;
+} hyk_module_info_t;
+
+/* Decompose-compile-load.  Replaces the construction of
+ * heyoka::taylor_adaptive_batch<double> (decomposition + order selection + JIT,
+ * heyoka/expose_batch_integrators.cpp:166-208).  `order` >= 2.  `device` is a
+ * CUDA device ordinal.  Compiled kernels are cached per process by
+ * (decomposition, order, config). */
+int hyk_module_create(const hyk_decomp_t *d, uint32_t order, const hyk_config_t *cfg, int device,
+                      hyk_module **out);
+int hyk_module_destroy(hyk_module *m);
+int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info);
+/* The generated CUDA source of the module (valid until hyk_module_destroy). */
+const char *hyk_module_source(const hyk_module *m);
+
+/* Lane data, device pointers, row stride `ld` (>= n_lanes) for 2-D arrays. */
+typedef struct hyk_lanes {
+    uint64_t n_lanes;
+    uint64_t ld;
+    double *state;         /* (n_eq, ld) in/out */
+    const double *pars;    /* (n_pars, ld) or NULL when n_pars == 0 */
+    double *time_hi;       /* (n_lanes) double-length time, in/out */
+    double *time_lo;       /* (n_lanes) */
+} hyk_lanes_t;
+
+/* One Taylor step on every lane.  Replaces taylor_adaptive_batch::step /
+ * step(max_delta_t) / step_backward (heyoka/expose_batch_integrators.cpp:233-241,
+ * reference method bodies in the heyoka C++ library).
+ *   max_delta_t: (n_lanes) signed step limits, or NULL for +inf (forward step);
+ *                pass `backward` = 1 with NULL for step_backward (-inf).
+ *   outcome:     (n_lanes) int64 taylor_outcome per lane (out)
+ *   h:           (n_lanes) step taken per lane (out)
+ *   tc:          (n_eq, order+1, n_lanes) Taylor coefficients of the step, or NULL */
+int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t, int backward,
+             int64_t *outcome, double *h, double *tc, void *stream);
+
+/* Propagation of every lane to its own final time.  Replaces
+ * taylor_adaptive_batch::propagate_until / propagate_for / propagate_grid
+ * (heyoka/expose_batch_integrators.cpp:243-392).  Each lane follows the
+ * reference's per-lane rules (double-length remaining time, step clamped to
+ * the remaining time and to max_delta_t, zero steps not counted, per-lane
+ * outcome / min |h| / max |h| / step count).
+ *
+ * The per-lane bookkeeping arrays are caller-owned device memory and are both
+ * input and output, so a propagation can be resumed (hyk_prop_init fills them
+ * from the targets; hyk_propagate advances them). */
+typedef struct hyk_prop {
+    /* targets and limits */
+    const double *tf_hi;       /* (n_lanes) final time, double-length */
+    const double *tf_lo;       /* (n_lanes) */
+    const double *max_delta_t; /* (n_lanes) >= 0, or NULL for +inf */
+    uint64_t max_steps;        /* 0 = unlimited; iterations per lane */
+    /* optional dense output over a grid: grid (n_grid, ld), out (n_grid, n_eq, ld) */
+    const double *grid;
+    uint64_t n_grid;
+    double *grid_out;
+    /* optional per-step Taylor-coefficient capture (continuous output):
+     * tc_out (tc_capacity, n_eq, order+1, ld), tc_t_hi/lo (tc_capacity, ld) =
+     * time at the END of each captured step */
+    double *tc_out;
+    double *tc_t_hi;
+    double *tc_t_lo;
+    uint64_t tc_capacity;
+    /* per-lane bookkeeping, in/out */
+    double *rem_hi;      /* remaining time (double-length) */
+    double *rem_lo;
+    int64_t *outcome;    /* last outcome */
+    double *min_h;
+    double *max_h;
+    uint64_t *n_steps;   /* accepted non-zero steps */
+    uint64_t *n_iter;    /* iterations (steps attempted, incl. zero) */
+    uint64_t *grid_idx;  /* next grid row to write */
+    double *last_h;      /* h of the last iteration */
+    double *last_tc;     /* (n_eq, order+1, ld) Taylor coefficients of the last step, or NULL */
+    uint32_t *status;    /* per-lane status bits HYK_LANE_* */
+} hyk_prop_t;
+
+#define HYK_LANE_DONE 1u     /* reached the final time */
+#define HYK_LANE_STOPPED 2u  /* stopped early: error, step limit or capacity */
+#define HYK_LANE_CAPACITY 4u /* stopped because tc_capacity was reached (resumable) */
+
+/* Initialise the bookkeeping arrays of `p` for a propagation to tf. */
+int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, void *stream);
+
+#define HYK_MODE_PLAIN 0      /* one kernel launch per step (drop-in form) */
+#define HYK_MODE_PERSISTENT 1 /* persistent kernel, per-lane loops, lane queue */
+
+/* Device workspace needed by hyk_propagate (bytes, 256-byte aligned pointer). */
+size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode);
+
+/* Advance every unfinished lane until it is done or stopped.
+ * PLAIN mode launches one step kernel per iteration and reads one word back
+ * every `check_every` launches to detect completion (synchronises `stream`).
+ * PERSISTENT mode runs one persistent launch.  `workspace` is device memory
+ * of hyk_propagate_workspace_size() bytes.  On return, `*iters` (may be NULL)
+ * holds the number of step launches made (PLAIN) or 1 (PERSISTENT). */
+int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode,
+                  void *workspace, size_t workspace_bytes, uint32_t check_every, uint64_t *iters,
+                  void *stream);
+
+/* Dense output: out[i][l] = sum_n tc[i][n][l] * dt[l]^n (Horner), the
+ * evaluator behind update_d_output / continuous output
+ * (heyoka/expose_batch_integrators.cpp:519-541,
+ *  heyoka/taylor_expose_c_output.cpp:272-408). */
+int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
+                   const double *dt, double *out, void *stream);
+
+/* Device FP64 FMA throughput microbenchmark (flop/s, 2 flops per FMA), used
+ * as the roofline denominator.  Runs for about `millis` milliseconds. */
+int hyk_fp64_peak(int device, double millis, double *flops_per_s);
+
+const char *hyk_last_error(void);
+const char *hyk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYK_H */
