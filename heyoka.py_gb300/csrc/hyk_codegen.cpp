@@ -1,0 +1,618 @@
+// Code generator: Taylor decomposition -> fused FP64 CUDA step kernel.
+//
+// The reference JIT-compiles the Taylor recurrences of each ODE system with
+// LLVM for the host CPU (inside the heyoka C++ library, reached from
+// heyoka/expose_batch_integrators.cpp:166-208).  Here the same recurrences
+// are emitted as straight-line CUDA C++, one block per Taylor order, and
+// compiled with NVRTC for sm_103a.  Every index is a compile-time constant:
+// jets that later orders read live in shared memory at fixed slots, values
+// used only within their own order stay in registers, a NEG node is folded
+// into its readers as a sign, and the order-p coefficients of the
+// intermediate u-variables are skipped (only the state's order p is used).
+//
+// Recurrences (normalised derivatives, restated from doc/tut_taylor_method.rst):
+//   add/sub  c_n = a_n +- b_n
+//   mul      c_n = sum_{j=0}^{n} a_j b_{n-j}
+//   div      c_n = (a_n - sum_{j=1}^{n} b_j c_{n-j}) / b_0
+//   square   c_n = 2 sum_{j<n-j} a_j a_{n-j} (+ a_{n/2}^2)
+//   sqrt     c_n = (a_n - 2 sum_{0<j<n-j} c_j c_{n-j} (- c_{n/2}^2)) / (2 c_0)
+//   pow      c_n = sum_{j=0}^{n-1} (n alpha - j (alpha + 1)) a_{n-j} c_j / (n a_0)
+//   exp      c_n = (1/n) sum_{j=1}^{n} (j a_j) c_{n-j}
+//   log      c_n = (a_n - (1/n) sum_{j=1}^{n-1} (j c_j) a_{n-j}) / a_0
+//   sin/cos  s_n = (1/n) sum (j a_j) c_{n-j},  c_n = -(1/n) sum (j a_j) s_{n-j}
+//   state    x_{n+1} = f_n / (n + 1)
+// Sums run over increasing j, skip identically-zero terms, start with a
+// product and accumulate with fused multiply-adds; "/ n" is a multiplication
+// by the double nearest 1/n and "/ b_0" (n >= 1) a multiplication by 1/b_0
+// computed once per step.  The CPU oracle's "gpu" mode performs the same
+// operations in the same order.  With pin arithmetic (HYK_CFG_PIN_ARITH)
+// the generator emits plain multiply + add and true divisions instead, the
+// oracle's "pin" mode.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <sstream>
+
+#include "hyk_internal.hpp"
+
+namespace hyk {
+
+bool load_dec(const hyk_decomp_t *d, Dec &out, std::string &err) {
+    if (!d || d->n_eq == 0) {
+        err = "invalid decomposition: no state variables";
+        return false;
+    }
+    if (d->n_ops > 0 && !d->ops) {
+        err = "invalid decomposition: null ops";
+        return false;
+    }
+    if (!d->rhs) {
+        err = "invalid decomposition: null right-hand sides";
+        return false;
+    }
+    out.n_eq = d->n_eq;
+    out.n_ops = d->n_ops;
+    out.n_pars = d->n_pars;
+    out.ops.assign(d->ops, d->ops + d->n_ops);
+    out.rhs.assign(d->rhs, d->rhs + d->n_eq);
+    const uint32_t nu = out.n_u();
+    auto chk = [&](const hyk_arg_t &a, uint32_t self) {
+        switch (a.kind) {
+        case HYK_ARG_NONE:
+        case HYK_ARG_TIME:
+            return true;
+        case HYK_ARG_NUM:
+            return true;
+        case HYK_ARG_U:
+            return a.idx >= 0 && (uint32_t)a.idx < self;
+        case HYK_ARG_PAR:
+            return a.idx >= 0 && (uint32_t)a.idx < out.n_pars;
+        default:
+            return false;
+        }
+    };
+    for (uint32_t k = 0; k < out.n_ops; ++k) {
+        const auto &o = out.ops[k];
+        const uint32_t self = out.n_eq + k;
+        if (o.op < HYK_OP_ADD || o.op > HYK_OP_COS || !chk(o.a, self) || o.a.kind == HYK_ARG_NONE ||
+            !chk(o.b, self)) {
+            err = "invalid u-variable definition at index " + std::to_string(self);
+            return false;
+        }
+        const bool binary = o.op == HYK_OP_ADD || o.op == HYK_OP_SUB || o.op == HYK_OP_MUL || o.op == HYK_OP_DIV;
+        if (binary && o.b.kind == HYK_ARG_NONE) {
+            err = "missing second argument at index " + std::to_string(self);
+            return false;
+        }
+        if (o.op == HYK_OP_POW && o.b.kind != HYK_ARG_NUM) {
+            err = "pow() needs a numerical exponent (index " + std::to_string(self) + ")";
+            return false;
+        }
+        if (o.op == HYK_OP_SIN || o.op == HYK_OP_COS) {
+            if (o.aux < (int)out.n_eq || (uint32_t)o.aux >= nu) {
+                err = "invalid sin/cos partner at index " + std::to_string(self);
+                return false;
+            }
+            const auto &pt = out.ops[o.aux - out.n_eq];
+            const int want = o.op == HYK_OP_SIN ? HYK_OP_COS : HYK_OP_SIN;
+            if (pt.op != want || pt.aux != (int)self || pt.a.kind != o.a.kind || pt.a.idx != o.a.idx) {
+                err = "inconsistent sin/cos pair at index " + std::to_string(self);
+                return false;
+            }
+        }
+    }
+    for (const auto &r : out.rhs)
+        if (!chk(r, nu) || r.kind == HYK_ARG_NONE) {
+            err = "invalid right-hand side";
+            return false;
+        }
+    return true;
+}
+
+namespace {
+
+std::string lit(double v) {
+    if (std::isnan(v)) return "__longlong_as_double(0x7ff8000000000000LL)";
+    if (std::isinf(v)) return v > 0 ? "hyk_inf()" : "(-hyk_inf())";
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%.17g", v);
+    std::string s(buf);
+    if (s.find_first_of(".eE") == std::string::npos) s += ".0";
+    if (v < 0 || (v == 0 && std::signbit(v))) s = "(" + s + ")";
+    return s;
+}
+
+struct Ref {
+    int kind = HYK_ARG_NONE;  // after NEG folding
+    int u = -1;
+    bool neg = false;
+    double num = 0;
+    int par = -1;
+};
+
+struct Gen {
+    const Dec &d;
+    uint32_t p, N, NU;
+    bool pin;
+    std::vector<int> base;
+    std::vector<char> negf, alias, hist, needka;
+    std::vector<int> slot, kslot;
+    uint32_t nslot = 0, par_slot = 0;
+    std::ostringstream o;
+    double flops = 0;
+
+    Gen(const Dec &dd, uint32_t order, bool pin_arith) : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith) {
+        base.resize(NU);
+        negf.assign(NU, 0);
+        alias.assign(NU, 0);
+        for (uint32_t u = 0; u < NU; ++u) base[u] = (int)u;
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const auto &op = d.ops[k];
+            const uint32_t u = N + k;
+            if (op.op == HYK_OP_NEG && op.a.kind == HYK_ARG_U) {
+                alias[u] = 1;
+                base[u] = base[op.a.idx];
+                negf[u] = !negf[op.a.idx];
+            }
+        }
+        analyse();
+    }
+
+    Ref res(const hyk_arg_t &a) const {
+        Ref r;
+        r.kind = a.kind;
+        if (a.kind == HYK_ARG_U) {
+            r.u = base[a.idx];
+            r.neg = negf[a.idx];
+        } else if (a.kind == HYK_ARG_NUM) {
+            r.num = a.num;
+        } else if (a.kind == HYK_ARG_PAR) {
+            r.par = a.idx;
+        }
+        return r;
+    }
+    static bool varying(const Ref &r) { return r.kind == HYK_ARG_U || r.kind == HYK_ARG_TIME; }
+
+    void analyse() {
+        hist.assign(NU, 0);
+        needka.assign(NU, 0);
+        for (uint32_t i = 0; i < N; ++i) hist[i] = 1;
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const uint32_t u = N + k;
+            if (alias[u]) continue;
+            const auto &op = d.ops[k];
+            const Ref A = res(op.a), B = res(op.b);
+            auto H = [&](const Ref &r) {
+                if (r.kind == HYK_ARG_U) hist[r.u] = 1;
+            };
+            auto K = [&](const Ref &r) {
+                if (r.kind == HYK_ARG_U) needka[r.u] = 1;
+            };
+            switch (op.op) {
+            case HYK_OP_MUL:
+                if (varying(B)) H(A);
+                if (varying(A)) H(B);
+                break;
+            case HYK_OP_DIV:
+                H(B);
+                if (varying(B)) hist[u] = 1;
+                break;
+            case HYK_OP_SQUARE:
+                H(A);
+                break;
+            case HYK_OP_SQRT:
+                if (varying(A)) hist[u] = 1;
+                break;
+            case HYK_OP_POW:
+                H(A);
+                if (varying(A)) hist[u] = 1;
+                break;
+            case HYK_OP_EXP:
+                K(A);
+                if (varying(A)) hist[u] = 1;
+                break;
+            case HYK_OP_LOG:
+                H(A);
+                if (varying(A)) needka[u] = 1;
+                break;
+            case HYK_OP_SIN:
+            case HYK_OP_COS:
+                K(A);
+                if (varying(A)) {
+                    hist[u] = 1;
+                    hist[op.aux] = 1;
+                }
+                break;
+            default:
+                break;
+            }
+        }
+        // Slots: state variables (orders 0..p), other histories (orders
+        // 0..p-2: order p-1 is only read within its own block and order p of
+        // intermediates is never computed), j*a_j histories (orders 1..p-2),
+        // then the parameters.
+        slot.assign(NU, -1);
+        kslot.assign(NU, -1);
+        uint32_t s = 0;
+        for (uint32_t i = 0; i < N; ++i) {
+            slot[i] = (int)s;
+            s += p + 1;
+        }
+        const uint32_t hl = p >= 2 ? p - 1 : 1, kl = p >= 3 ? p - 2 : 0;
+        for (uint32_t u = N; u < NU; ++u)
+            if (hist[u] && !alias[u]) {
+                slot[u] = (int)s;
+                s += hl;
+            }
+        for (uint32_t u = 0; u < NU; ++u)
+            if (needka[u] && !alias[u] && kl > 0) {
+                kslot[u] = (int)s;
+                s += kl;
+            }
+        par_slot = s;
+        s += d.n_pars;
+        nslot = s;
+    }
+
+    std::string vname(uint32_t u, uint32_t n) const { return "v" + std::to_string(u) + "_" + std::to_string(n); }
+    std::string kname(uint32_t u, uint32_t n) const { return "k" + std::to_string(u) + "_" + std::to_string(n); }
+    std::string smem(uint32_t s) const { return "S[" + std::to_string(s) + " * HYK_BLK]"; }
+
+    // Coefficient of order j of u-variable u (not an alias) while emitting block n.
+    std::string ucoef(uint32_t u, uint32_t j, uint32_t n) const {
+        if (j == n) return vname(u, j);
+        if (!hist[u] || slot[u] < 0) {
+            std::fprintf(stderr, "hyk codegen: missing history for u%u\n", u);
+            std::abort();
+        }
+        return smem((uint32_t)slot[u] + j);
+    }
+    // Coefficient expression, or "" when identically zero.
+    std::string cf(const Ref &r, uint32_t j, uint32_t n) const {
+        switch (r.kind) {
+        case HYK_ARG_U: {
+            const std::string s = ucoef((uint32_t)r.u, j, n);
+            return r.neg ? "(-" + s + ")" : s;
+        }
+        case HYK_ARG_NUM:
+            return j == 0 ? lit(r.num) : "";
+        case HYK_ARG_PAR:
+            return j == 0 ? "HYK_PAR(" + std::to_string(r.par) + ")" : "";
+        case HYK_ARG_TIME:
+            return j == 0 ? "t0" : (j == 1 ? "1.0" : "");
+        }
+        return "";
+    }
+    // j * a_j (j >= 1), or "" when identically zero.
+    std::string kcf(const Ref &r, uint32_t j, uint32_t n) const {
+        switch (r.kind) {
+        case HYK_ARG_U: {
+            const uint32_t u = (uint32_t)r.u;
+            std::string s;
+            if (j == n)
+                s = kname(u, j);
+            else {
+                if (kslot[u] < 0) {
+                    std::fprintf(stderr, "hyk codegen: missing j*a_j history for u%u\n", u);
+                    std::abort();
+                }
+                s = smem((uint32_t)kslot[u] + j - 1);
+            }
+            return r.neg ? "(-" + s + ")" : s;
+        }
+        case HYK_ARG_TIME:
+            return j == 1 ? "1.0" : "";
+        default:
+            return "";
+        }
+    }
+
+    std::string fma(const std::string &x, const std::string &y, const std::string &c) const {
+        if (pin) return "(" + c + " + " + x + " * " + y + ")";
+        return "__fma_rn(" + x + ", " + y + ", " + c + ")";
+    }
+
+    struct Acc {
+        std::string name;
+        bool first = true;
+    };
+    void term(Acc &a, const std::string &x, const std::string &y) {
+        if (x.empty() || y.empty()) return;
+        if (a.first) {
+            o << "    double " << a.name << " = " << x << " * " << y << ";\n";
+            a.first = false;
+            flops += 1;
+        } else {
+            o << "    " << a.name << " = " << fma(x, y, a.name) << ";\n";
+            flops += 2;
+        }
+    }
+    std::string divn(const std::string &x, uint32_t n) {
+        flops += 1;
+        if (pin) return "(" + x + " / " + lit((double)n) + ")";
+        return "(" + x + " * " + lit(1.0 / (double)n) + ")";
+    }
+    std::string inv0(uint32_t u) const { return "i" + std::to_string(u); }
+
+    void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
+
+    void store_hist(uint32_t u, uint32_t n) {
+        if (u >= N && hist[u] && n + 2 <= p) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
+        if (needka[u] && n >= 1) {
+            o << "    const double " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
+            flops += 1;
+            if (kslot[u] >= 0 && n + 2 <= p) o << "    " << smem((uint32_t)kslot[u] + n - 1) << " = " << kname(u, n) << ";\n";
+        }
+    }
+
+    void emit_op(uint32_t k, uint32_t n) {
+        const auto &op = d.ops[k];
+        const uint32_t u = N + k;
+        if (alias[u]) return;
+        const Ref A = res(op.a), B = res(op.b);
+        const std::string acc = "a" + std::to_string(u) + "_" + std::to_string(n);
+        const std::string z = "0.0";
+        switch (op.op) {
+        case HYK_OP_ADD:
+        case HYK_OP_SUB: {
+            const std::string a = cf(A, n, n), b = cf(B, n, n);
+            const bool add = op.op == HYK_OP_ADD;
+            if (!a.empty() && !b.empty()) {
+                def(u, n, "(" + a + (add ? " + " : " - ") + b + ")");
+                flops += 1;
+            } else if (!a.empty())
+                def(u, n, a);
+            else if (!b.empty())
+                def(u, n, add ? b : "(-" + b + ")");
+            else
+                def(u, n, z);
+            break;
+        }
+        case HYK_OP_NEG: {
+            const std::string a = cf(A, n, n);
+            def(u, n, a.empty() ? z : "(-" + a + ")");
+            break;
+        }
+        case HYK_OP_MUL: {
+            Acc s{acc};
+            for (uint32_t j = 0; j <= n; ++j) term(s, cf(A, j, n), cf(B, n - j, n));
+            def(u, n, s.first ? z : acc);
+            break;
+        }
+        case HYK_OP_DIV: {
+            const std::string b0 = cf(B, 0, n), an = cf(A, n, n);
+            if (n == 0) {
+                def(u, 0, "(" + an + " / " + b0 + ")");
+                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << b0 << ";\n";
+                flops += 2;
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 1; j <= n; ++j) term(s, cf(B, j, n), ucoef(u, n - j, n));
+            const std::string av = an.empty() ? z : an;
+            const std::string num = s.first ? av : "(" + av + " - " + acc + ")";
+            if (!s.first) flops += 1;
+            flops += 1;
+            def(u, n, pin ? "(" + num + " / " + b0 + ")" : "(" + num + " * " + inv0(u) + ")");
+            break;
+        }
+        case HYK_OP_SQUARE: {
+            Acc s{acc};
+            for (uint32_t j = 0; 2 * j < n; ++j) term(s, cf(A, j, n), cf(A, n - j, n));
+            if (!s.first) {
+                o << "    " << acc << " = " << acc << " + " << acc << ";\n";
+                flops += 1;
+            }
+            if (n % 2 == 0) term(s, cf(A, n / 2, n), cf(A, n / 2, n));
+            def(u, n, s.first ? z : acc);
+            break;
+        }
+        case HYK_OP_SQRT: {
+            const std::string an = cf(A, n, n);
+            if (n == 0) {
+                def(u, 0, "sqrt(" + an + ")");
+                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / (2.0 * " << vname(u, 0) << ");\n";
+                flops += 3;
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 1; 2 * j < n; ++j) term(s, ucoef(u, j, n), ucoef(u, n - j, n));
+            if (!s.first) {
+                o << "    " << acc << " = " << acc << " + " << acc << ";\n";
+                flops += 1;
+            }
+            if (n % 2 == 0) term(s, ucoef(u, n / 2, n), ucoef(u, n / 2, n));
+            const std::string av = an.empty() ? z : an;
+            const std::string num = s.first ? av : "(" + av + " - " + acc + ")";
+            flops += s.first ? 1 : 2;
+            def(u, n, pin ? "(" + num + " / (2.0 * " + ucoef(u, 0, n) + "))" : "(" + num + " * " + inv0(u) + ")");
+            break;
+        }
+        case HYK_OP_POW: {
+            const double alpha = op.b.num;
+            const std::string a0 = cf(A, 0, n);
+            if (n == 0) {
+                def(u, 0, "pow(" + a0 + ", " + lit(alpha) + ")");
+                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
+                flops += 21;
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 0; j < n; ++j) {
+                const std::string anj = cf(A, n - j, n);
+                if (anj.empty()) continue;
+                const double coef = (double)n * alpha - (double)j * (alpha + 1.0);
+                const std::string t = "t" + std::to_string(u) + "_" + std::to_string(n) + "_" + std::to_string(j);
+                o << "    const double " << t << " = " << lit(coef) << " * " << anj << ";\n";
+                flops += 1;
+                term(s, t, ucoef(u, j, n));
+            }
+            if (s.first) {
+                def(u, n, z);
+                break;
+            }
+            flops += 2;
+            if (pin)
+                def(u, n, "(" + acc + " / (" + lit((double)n) + " * " + a0 + "))");
+            else
+                def(u, n, "((" + acc + " * " + lit(1.0 / (double)n) + ") * " + inv0(u) + ")");
+            break;
+        }
+        case HYK_OP_EXP: {
+            if (n == 0) {
+                def(u, 0, "exp(" + cf(A, 0, n) + ")");
+                flops += 20;
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 1; j <= n; ++j) term(s, kcf(A, j, n), ucoef(u, n - j, n));
+            def(u, n, s.first ? z : divn(acc, n));
+            break;
+        }
+        case HYK_OP_LOG: {
+            const std::string a0 = cf(A, 0, n), an = cf(A, n, n);
+            if (n == 0) {
+                def(u, 0, "log(" + a0 + ")");
+                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
+                flops += 21;
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 1; j < n; ++j) {
+                const Ref self{HYK_ARG_U, (int)u, false, 0, -1};
+                term(s, kcf(self, j, n), cf(A, n - j, n));
+            }
+            const std::string av = an.empty() ? z : an;
+            std::string num = av;
+            if (!s.first) {
+                num = "(" + av + " - " + divn(acc, n) + ")";
+                flops += 1;
+            }
+            flops += 1;
+            def(u, n, pin ? "(" + num + " / " + a0 + ")" : "(" + num + " * " + inv0(u) + ")");
+            break;
+        }
+        case HYK_OP_SIN:
+        case HYK_OP_COS: {
+            const uint32_t partner = (uint32_t)op.aux;
+            const bool is_sin = op.op == HYK_OP_SIN;
+            if (n == 0) {
+                // The pair is evaluated together at its first member.
+                if (u < partner) {
+                    const uint32_t su = is_sin ? u : partner, cu = is_sin ? partner : u;
+                    o << "    double " << vname(su, 0) << "_m, " << vname(cu, 0) << "_m;\n";
+                    o << "    sincos(" << cf(A, 0, n) << ", &" << vname(su, 0) << "_m, &" << vname(cu, 0) << "_m);\n";
+                    o << "    const double " << vname(su, 0) << " = " << vname(su, 0) << "_m;\n";
+                    o << "    const double " << vname(cu, 0) << " = " << vname(cu, 0) << "_m;\n";
+                    flops += 40;
+                }
+                break;
+            }
+            Acc s{acc};
+            for (uint32_t j = 1; j <= n; ++j) term(s, kcf(A, j, n), ucoef(partner, n - j, n));
+            if (s.first)
+                def(u, n, z);
+            else
+                def(u, n, is_sin ? divn(acc, n) : "(-" + divn(acc, n) + ")");
+            break;
+        }
+        default:
+            break;
+        }
+    }
+
+    void emit_jets() {
+        o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
+        for (uint32_t i = 0; i < N; ++i) {
+            o << "    const double " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
+            if (needka[i]) {
+                // k_i_0 is never read (sums start at j = 1).
+            }
+        }
+        for (uint32_t n = 0; n < p; ++n) {
+            o << "    // ---- order " << n << "\n";
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                emit_op(k, n);
+                const uint32_t u = N + k;
+                if (!alias[u]) store_hist(u, n);
+            }
+            for (uint32_t i = 0; i < N; ++i) {
+                const Ref r = res(d.rhs[i]);
+                const std::string f = cf(r, n, n);
+                def(i, n + 1, f.empty() ? "0.0" : divn(f, n + 1));
+                o << "    HYK_SX(" << i << ", " << (n + 1) << ") = " << vname(i, n + 1) << ";\n";
+                if (needka[i]) {
+                    o << "    const double " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
+                      << vname(i, n + 1) << ";\n";
+                    flops += 1;
+                    if (kslot[i] >= 0 && n + 1 + 2 <= p)
+                        o << "    " << smem((uint32_t)kslot[i] + n) << " = " << kname(i, n + 1) << ";\n";
+                }
+            }
+            // Values of earlier orders are re-read from shared memory: the
+            // warp barrier keeps the compiler from carrying them in registers.
+            o << "    __syncwarp();\n";
+        }
+        o << "}\n";
+    }
+};
+
+const char *kTemplate =
+#include "kernel_template.inc"
+    ;
+
+}  // namespace
+
+uint32_t count_slots(const Dec &d, uint32_t order) {
+    Gen g(d, order, false);
+    return g.nslot;
+}
+
+bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
+              std::string &err) {
+    if (order < 2) {
+        err = "the Taylor order must be at least 2";
+        return false;
+    }
+    Gen g(d, order, pin_arith);
+    const double p = (double)order;
+    const double e1 = std::exp(1.0);
+    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+    std::ostringstream h;
+    h << "// Generated by libhyk: " << d.n_eq << " equations, " << d.n_ops << " u-operations, order " << order
+      << (pin_arith ? ", pin arithmetic" : "") << "\n";
+    h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
+      << "\n#define HYK_BLK " << blk << "\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
+      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
+      << lit(1.0 / (p - 1.0)) << "\n";
+    if (pin_arith)
+        h << "#define HYK_FMA_ACC(a, b, c) ((a) * (b) + (c))\n";
+    else
+        h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
+    h << kTemplate << "\n";
+    h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
+    g.emit_jets();
+    // The template's kernels call hyk_jets(); declare-before-use ordering is
+    // satisfied by emitting the jets function first.
+    std::string body = g.o.str();
+    std::string full = h.str();
+    // Insert the jets definition before the first kernel of the template.
+    const std::string marker = "// One Taylor step per lane";
+    const size_t pos = full.find(marker);
+    if (pos == std::string::npos) {
+        err = "internal: template marker not found";
+        return false;
+    }
+    full.insert(pos, body + "\n");
+    out.src = std::move(full);
+    out.n_slot = g.nslot;
+    out.par_slot = g.par_slot;
+    // Per-step flops: recurrences + Horner (2 per coefficient) + step size
+    // (two pow and the norm arithmetic) + double-length time update.
+    out.flops = g.flops + 2.0 * d.n_eq * order + 46.0 + 10.0;
+    return true;
+}
+
+}  // namespace hyk

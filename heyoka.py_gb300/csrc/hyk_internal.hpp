@@ -1,0 +1,37 @@
+// Internal declarations shared by the code generator and the runtime of libhyk.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "hyk.h"
+
+namespace hyk {
+
+// A validated copy of a hyk_decomp_t.
+struct Dec {
+    uint32_t n_eq = 0, n_ops = 0, n_pars = 0;
+    std::vector<hyk_uop_t> ops;
+    std::vector<hyk_arg_t> rhs;
+    uint32_t n_u() const { return n_eq + n_ops; }
+};
+
+bool load_dec(const hyk_decomp_t *d, Dec &out, std::string &err);
+
+// Result of code generation for one (decomposition, order, arithmetic, block) tuple.
+struct GenOut {
+    std::string src;          // complete NVRTC translation unit
+    uint32_t n_slot = 0;      // shared-memory doubles per lane
+    uint32_t par_slot = 0;    // first parameter slot
+    double flops = 0;         // algorithmic FP64 flops per step per lane
+};
+
+// Shared-memory slots per lane for a decomposition at a given order (the
+// block size does not change it).
+uint32_t count_slots(const Dec &d, uint32_t order);
+
+bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
+              std::string &err);
+
+}  // namespace hyk

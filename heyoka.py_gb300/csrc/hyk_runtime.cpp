@@ -1,0 +1,553 @@
+// libhyk runtime: the C ABI of include/hyk.h.
+//
+// Module creation generates the CUDA source of one ODE system (hyk_codegen.cpp),
+// compiles it with NVRTC straight to an sm_103a cubin, loads it through the
+// driver API into the device's primary context (the one torch also uses) and
+// keeps the kernel handles.  Launch functions marshal the caller's device
+// pointers into one by-value parameter block.  No function here allocates
+// device memory except module loading; all buffers are the caller's.
+
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hyk.h"
+#include "hyk_internal.hpp"
+
+// Generic kernels compiled by nvcc into this library (hyk_generic.cu).
+extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
+                                      const double *dt, double *out, void *stream);
+extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
+extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
+
+namespace {
+
+thread_local std::string g_err;
+
+// The CUDA driver is loaded at run time (dlopen), so that the library also
+// loads on machines without a GPU driver (build and symbol checks); every
+// driver entry point goes through this table.
+#define HYK_STR2(x) #x
+#define HYK_STR(x) HYK_STR2(x)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString)
+
+struct DriverApi {
+#define HYK_DECL(f) decltype(&::f) f = nullptr;
+    HYK_DRIVER_FNS(HYK_DECL)
+#undef HYK_DECL
+    bool ok = false;
+    std::string err;
+};
+
+DriverApi &drv() {
+    static DriverApi api;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *h = dlopen("libcuda.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) h = dlopen("libcuda.so", RTLD_NOW | RTLD_LOCAL);
+        if (!h) {
+            api.err = std::string("cannot load the CUDA driver (libcuda.so.1): ") + dlerror();
+            return;
+        }
+#define HYK_LOAD(f)                                                             \
+    api.f = reinterpret_cast<decltype(&::f)>(dlsym(h, HYK_STR(f)));             \
+    if (!api.f) {                                                               \
+        api.err = std::string("CUDA driver symbol missing: ") + HYK_STR(f);     \
+        return;                                                                 \
+    }
+        HYK_DRIVER_FNS(HYK_LOAD)
+#undef HYK_LOAD
+        api.ok = true;
+    });
+    return api;
+}
+
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+std::string cu_msg(CUresult r) {
+    const char *s = nullptr;
+    if (drv().ok) drv().cuGetErrorString(r, &s);
+    return s ? s : "unknown CUDA error";
+}
+
+#define HYK_CU(call)                                                                                       \
+    do {                                                                                                   \
+        CUresult hyk_r_ = (call);                                                                          \
+        if (hyk_r_ != CUDA_SUCCESS) return fail(HYK_ERR_CUDA, std::string(#call) + ": " + cu_msg(hyk_r_)); \
+    } while (0)
+
+// Host mirror of the device parameter block (kernel_template.inc).
+struct KParams {
+    uint64_t n_lanes, ld;
+    double *state;
+    const double *pars;
+    double *t_hi, *t_lo;
+    const double *step_lim;
+    double step_default_lim;
+    int64_t *step_oc;
+    double *step_h;
+    double *step_tc;
+    const double *tf_hi, *tf_lo, *maxdt;
+    uint64_t max_steps;
+    const double *grid;
+    uint64_t n_grid;
+    double *grid_out;
+    double *tc_out, *tc_thi, *tc_tlo;
+    uint64_t tc_cap;
+    double *rem_hi, *rem_lo;
+    int64_t *outcome;
+    double *min_h, *max_h;
+    uint64_t *n_steps, *n_iter, *grid_idx;
+    double *last_h, *last_tc;
+    uint32_t *status;
+    uint64_t iters_per_launch;
+    uint64_t *queue;
+    uint32_t *finished;
+    int persistent;
+};
+
+struct Device {
+    CUdevice dev = 0;
+    CUcontext ctx = nullptr;
+    int n_sm = 0;
+    int smem_optin = 0;   // max dynamic shared memory per block (opt-in)
+    int smem_per_sm = 0;  // shared memory per multiprocessor
+};
+
+std::mutex g_mtx;
+std::map<int, Device> g_devs;
+std::map<std::string, std::string> g_cubin_cache;  // key -> cubin bytes
+
+int get_device(int ordinal, Device *&out) {
+    if (!drv().ok) return fail(HYK_ERR_CUDA, drv().err);
+    std::lock_guard<std::mutex> lk(g_mtx);
+    auto it = g_devs.find(ordinal);
+    if (it == g_devs.end()) {
+        HYK_CU(drv().cuInit(0));
+        Device d;
+        HYK_CU(drv().cuDeviceGet(&d.dev, ordinal));
+        HYK_CU(drv().cuDevicePrimaryCtxRetain(&d.ctx, d.dev));
+        HYK_CU(drv().cuDeviceGetAttribute(&d.n_sm, CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT, d.dev));
+        HYK_CU(drv().cuDeviceGetAttribute(&d.smem_optin, CU_DEVICE_ATTRIBUTE_MAX_SHARED_MEMORY_PER_BLOCK_OPTIN, d.dev));
+        HYK_CU(drv().cuDeviceGetAttribute(&d.smem_per_sm, CU_DEVICE_ATTRIBUTE_MAX_SHARED_MEMORY_PER_MULTIPROCESSOR, d.dev));
+        int major = 0, minor = 0;
+        HYK_CU(drv().cuDeviceGetAttribute(&major, CU_DEVICE_ATTRIBUTE_COMPUTE_CAPABILITY_MAJOR, d.dev));
+        HYK_CU(drv().cuDeviceGetAttribute(&minor, CU_DEVICE_ATTRIBUTE_COMPUTE_CAPABILITY_MINOR, d.dev));
+        if (major != 10 || minor != 3)
+            return fail(HYK_ERR_UNSUPPORTED, "libhyk targets sm_103 (GB300); device " + std::to_string(ordinal) +
+                                                 " is sm_" + std::to_string(major) + std::to_string(minor));
+        it = g_devs.emplace(ordinal, d).first;
+    }
+    out = &it->second;
+    HYK_CU(drv().cuCtxSetCurrent(out->ctx));
+    return 0;
+}
+
+uint64_t fnv1a(const std::string &s, uint64_t h = 1469598103934665603ULL) {
+    for (unsigned char c : s) {
+        h ^= c;
+        h *= 1099511628211ULL;
+    }
+    return h;
+}
+
+std::string cache_dir() {
+    const char *e = std::getenv("HYK_CACHE_DIR");
+    if (e && *e) return e;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/hyk";
+}
+
+int compile_nvrtc(const std::string &src, const std::string &name, std::string &cubin, std::string &log) {
+    nvrtcProgram prog;
+    nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), name.c_str(), 0, nullptr, nullptr);
+    if (r != NVRTC_SUCCESS) return fail(HYK_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+    std::vector<const char *> opts = {"--gpu-architecture=sm_103a", "--fmad=false", "-std=c++17", "-lineinfo",
+                                      "--restrict"};
+    const char *pv = std::getenv("HYK_PTXAS_VERBOSE");
+    if (pv && *pv == '1') opts.push_back("--ptxas-options=-v");
+    r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+    size_t ls = 0;
+    nvrtcGetProgramLogSize(prog, &ls);
+    log.assign(ls, '\0');
+    if (ls) nvrtcGetProgramLog(prog, &log[0]);
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return fail(HYK_ERR_NVRTC, "NVRTC compilation failed: " + log);
+    }
+    size_t cs = 0;
+    nvrtcGetCUBINSize(prog, &cs);
+    cubin.assign(cs, '\0');
+    nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    return 0;
+}
+
+}  // namespace
+
+struct hyk_module {
+    hyk::Dec d;
+    uint32_t order = 0;
+    hyk_config_t cfg{};
+    int device = 0;
+    Device *dv = nullptr;
+    CUmodule mod = nullptr;
+    CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr;
+    std::string src, log;
+    uint32_t blk = 0, nslot = 0;
+    size_t smem = 0;
+    int regs = 0, local_bytes = 0, ctas_per_sm = 0;
+    double flops = 0, compile_s = 0;
+};
+
+extern "C" {
+
+const char *hyk_last_error(void) { return g_err.c_str(); }
+const char *hyk_version(void) { return "hyk 0.1 (sm_103a, FP64 Taylor, NVRTC)"; }
+
+int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t *cfg, int device, hyk_module **out) {
+    if (!out) return fail(HYK_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    std::unique_ptr<hyk_module> m(new hyk_module());
+    std::string err;
+    if (!hyk::load_dec(dd, m->d, err)) return fail(HYK_ERR_INVALID, err);
+    if (order < 2 || order > 200) return fail(HYK_ERR_INVALID, "the Taylor order must be in [2, 200]");
+    if (cfg) m->cfg = *cfg;
+    m->order = order;
+    m->device = device;
+    int rc = get_device(device, m->dv);
+    if (rc) return rc;
+    const Device &dv = *m->dv;
+
+    const uint32_t nslot = hyk::count_slots(m->d, order);
+    const size_t lane_bytes = (size_t)nslot * sizeof(double);
+    uint32_t blk = m->cfg.block_lanes;
+    if (blk == 0) {
+        // Pick the block size maximising resident lanes per SM under the
+        // shared-memory budget (1 KiB per CTA is reserved by the hardware),
+        // capped at 512 lanes per SM and 256 per CTA.
+        uint32_t best = 0, best_lanes = 0;
+        for (uint32_t b = 32; b <= 256; b += 32) {
+            const size_t per_cta = b * lane_bytes;
+            if (per_cta > (size_t)dv.smem_optin) break;
+            uint32_t ctas = (uint32_t)((size_t)dv.smem_per_sm / (per_cta + 1024));
+            uint32_t lanes = std::min<uint32_t>(ctas * b, 512);
+            if (lanes >= best_lanes) {
+                best_lanes = lanes;
+                best = b;
+            }
+        }
+        if (best == 0) {
+            if (lane_bytes * 32 > (size_t)dv.smem_optin)
+                return fail(HYK_ERR_UNSUPPORTED, "the system needs " + std::to_string(lane_bytes) +
+                                                     " bytes of Taylor coefficients per lane; at most " +
+                                                     std::to_string(dv.smem_optin / 32) + " fit the shared memory");
+            best = 32;
+        }
+        blk = best;
+    }
+    if (blk % 32 != 0 || blk > 1024) return fail(HYK_ERR_INVALID, "block_lanes must be a multiple of 32, <= 1024");
+    m->blk = blk;
+    m->nslot = nslot;
+    m->smem = (size_t)blk * lane_bytes;
+    if (m->smem > (size_t)dv.smem_optin)
+        return fail(HYK_ERR_UNSUPPORTED, "shared memory per CTA (" + std::to_string(m->smem) + ") exceeds the device limit");
+
+    hyk::GenOut g;
+    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err))
+        return fail(HYK_ERR_INVALID, err);
+    m->src = g.src;
+    m->flops = g.flops;
+
+    const auto t0 = std::chrono::steady_clock::now();
+    const std::string key = std::to_string(fnv1a(m->src)) + "_sm103a";
+    std::string cubin;
+    {
+        std::lock_guard<std::mutex> lk(g_mtx);
+        auto it = g_cubin_cache.find(key);
+        if (it != g_cubin_cache.end()) cubin = it->second;
+    }
+    const std::string dpath = cache_dir() + "/" + key + ".cubin";
+    if (cubin.empty() && !std::getenv("HYK_NO_DISK_CACHE")) {
+        std::ifstream f(dpath, std::ios::binary);
+        if (f) {
+            std::ostringstream ss;
+            ss << f.rdbuf();
+            cubin = ss.str();
+        }
+    }
+    if (cubin.empty()) {
+        rc = compile_nvrtc(m->src, "hyk_module.cu", cubin, m->log);
+        if (rc) return rc;
+        if (!std::getenv("HYK_NO_DISK_CACHE")) {
+            std::string cmd = "mkdir -p '" + cache_dir() + "'";
+            if (std::system(cmd.c_str()) == 0) {
+                std::ofstream f(dpath + ".tmp", std::ios::binary);
+                f.write(cubin.data(), (std::streamsize)cubin.size());
+                f.close();
+                std::rename((dpath + ".tmp").c_str(), dpath.c_str());
+            }
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_mtx);
+        g_cubin_cache[key] = cubin;
+    }
+    m->compile_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+    HYK_CU(drv().cuModuleLoadData(&m->mod, cubin.data()));
+    HYK_CU(drv().cuModuleGetFunction(&m->f_step, m->mod, "hyk_step_kernel"));
+    HYK_CU(drv().cuModuleGetFunction(&m->f_prop, m->mod, "hyk_prop_kernel"));
+    HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
+    for (CUfunction f : {m->f_step, m->f_prop}) {
+        HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
+        HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+    }
+    HYK_CU(drv().cuFuncGetAttribute(&m->regs, CU_FUNC_ATTRIBUTE_NUM_REGS, m->f_prop));
+    HYK_CU(drv().cuFuncGetAttribute(&m->local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, m->f_prop));
+    HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->ctas_per_sm, m->f_prop, (int)blk, m->smem));
+    if (m->ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the propagation kernel cannot be resident on an SM");
+    *out = m.release();
+    return 0;
+}
+
+int hyk_module_destroy(hyk_module *m) {
+    if (!m) return 0;
+    if (m->mod) {
+        drv().cuCtxSetCurrent(m->dv->ctx);
+        drv().cuModuleUnload(m->mod);
+    }
+    delete m;
+    return 0;
+}
+
+int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info) {
+    if (!m || !info) return fail(HYK_ERR_INVALID, "null argument");
+    std::memset(info, 0, sizeof *info);
+    info->n_eq = m->d.n_eq;
+    info->n_pars = m->d.n_pars;
+    info->order = m->order;
+    info->n_u = m->d.n_u();
+    info->block_lanes = m->blk;
+    info->smem_per_lane = m->nslot * 8;
+    info->regs_per_thread = (uint32_t)m->regs;
+    info->ctas_per_sm = (uint32_t)m->ctas_per_sm;
+    info->n_sm = (uint32_t)m->dv->n_sm;
+    info->reserved = (uint32_t)m->local_bytes;
+    info->flops_per_step = m->flops;
+    info->compile_seconds = m->compile_s;
+    return 0;
+}
+
+const char *hyk_module_source(const hyk_module *m) { return m ? m->src.c_str() : ""; }
+
+static int check_lanes(const hyk_module *m, const hyk_lanes_t *l) {
+    if (!m || !l) return fail(HYK_ERR_INVALID, "null argument");
+    if (l->n_lanes == 0) return 0;
+    if (l->ld < l->n_lanes) return fail(HYK_ERR_INVALID, "ld must be >= n_lanes");
+    if (!l->state || !l->time_hi || !l->time_lo) return fail(HYK_ERR_INVALID, "null state or time pointer");
+    if (m->d.n_pars && !l->pars) return fail(HYK_ERR_INVALID, "the system has parameters but pars is NULL");
+    return 0;
+}
+
+static void fill_lanes(KParams &k, const hyk_lanes_t *l) {
+    std::memset(&k, 0, sizeof k);
+    k.n_lanes = l->n_lanes;
+    k.ld = l->ld;
+    k.state = l->state;
+    k.pars = l->pars;
+    k.t_hi = l->time_hi;
+    k.t_lo = l->time_lo;
+}
+
+static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k, void *stream) {
+    if (grid == 0) return 0;
+    if (grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
+    void *args[] = {&k};
+    HYK_CU(drv().cuLaunchKernel(f, (unsigned)grid, 1, 1, blk, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr));
+    return 0;
+}
+
+int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t, int backward, int64_t *outcome,
+             double *h, double *tc, void *stream) {
+    int rc = check_lanes(m, lanes);
+    if (rc) return rc;
+    if (!outcome || !h) return fail(HYK_ERR_INVALID, "null outcome or h pointer");
+    if (lanes->n_lanes == 0) return 0;
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    KParams k;
+    fill_lanes(k, lanes);
+    k.step_lim = max_delta_t;
+    k.step_default_lim = backward ? -INFINITY : INFINITY;
+    k.step_oc = outcome;
+    k.step_h = h;
+    k.step_tc = tc;
+    return launch(m, m->f_step, (lanes->n_lanes + m->blk - 1) / m->blk, m->blk, m->smem, k, stream);
+}
+
+static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const hyk_prop_t *p) {
+    if (!p) return fail(HYK_ERR_INVALID, "null propagation descriptor");
+    if (!p->tf_hi || !p->rem_hi || !p->rem_lo || !p->outcome || !p->min_h || !p->max_h || !p->n_steps ||
+        !p->n_iter || !p->status || !p->last_h)
+        return fail(HYK_ERR_INVALID, "a required propagation array is NULL");
+    if (p->grid && (!p->grid_out || !p->grid_idx || p->n_grid == 0))
+        return fail(HYK_ERR_INVALID, "grid propagation needs grid_out, grid_idx and n_grid >= 1");
+    if (p->tc_out && (!p->tc_t_hi || !p->tc_t_lo))
+        return fail(HYK_ERR_INVALID, "Taylor-coefficient capture needs tc_t_hi and tc_t_lo");
+    fill_lanes(k, lanes);
+    k.tf_hi = p->tf_hi;
+    k.tf_lo = p->tf_lo;
+    k.maxdt = p->max_delta_t;
+    k.max_steps = p->max_steps;
+    k.grid = p->grid;
+    k.n_grid = p->n_grid;
+    k.grid_out = p->grid_out;
+    k.tc_out = p->tc_out;
+    k.tc_thi = p->tc_t_hi;
+    k.tc_tlo = p->tc_t_lo;
+    k.tc_cap = p->tc_capacity;
+    k.rem_hi = p->rem_hi;
+    k.rem_lo = p->rem_lo;
+    k.outcome = p->outcome;
+    k.min_h = p->min_h;
+    k.max_h = p->max_h;
+    k.n_steps = p->n_steps;
+    k.n_iter = p->n_iter;
+    k.grid_idx = p->grid_idx;
+    k.last_h = p->last_h;
+    k.last_tc = p->last_tc;
+    k.status = p->status;
+    (void)m;
+    return 0;
+}
+
+int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, void *stream) {
+    int rc = check_lanes(m, lanes);
+    if (rc) return rc;
+    if (lanes->n_lanes == 0) return 0;
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    KParams k;
+    rc = fill_prop(m, k, lanes, p);
+    if (rc) return rc;
+    return launch(m, m->f_init, (lanes->n_lanes + 127) / 128, 128, 0, k, stream);
+}
+
+size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode) {
+    (void)m;
+    (void)n_lanes;
+    (void)mode;
+    return 256;  // queue counter (8 B) + finished counter (4 B), padded
+}
+
+int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
+                  size_t workspace_bytes, uint32_t check_every, uint64_t *iters, void *stream) {
+    int rc = check_lanes(m, lanes);
+    if (rc) return rc;
+    if (iters) *iters = 0;
+    if (lanes->n_lanes == 0) return 0;
+    if (!workspace || workspace_bytes < hyk_propagate_workspace_size(m, lanes->n_lanes, mode))
+        return fail(HYK_ERR_INVALID, "workspace too small");
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return fail(HYK_ERR_INVALID, "workspace must be 256-byte aligned");
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    KParams k;
+    rc = fill_prop(m, k, lanes, p);
+    if (rc) return rc;
+    k.queue = reinterpret_cast<uint64_t *>(workspace);
+    k.finished = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(workspace) + 8);
+    const CUstream s = (CUstream)stream;
+    if (mode == HYK_MODE_PERSISTENT) {
+        HYK_CU(drv().cuMemsetD32Async((CUdeviceptr)workspace, 0, 4, s));
+        k.persistent = 1;
+        k.iters_per_launch = ~0ULL;
+        const uint64_t grid = (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm;
+        rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
+        if (rc) return rc;
+        if (iters) *iters = 1;
+        return 0;
+    }
+    if (mode != HYK_MODE_PLAIN) return fail(HYK_ERR_INVALID, "unknown propagation mode");
+    // One launch per step.  Completion is detected by counting lanes whose
+    // status is done or stopped; the count is read back every check_every
+    // launches (the only host synchronisation of the loop).
+    if (check_every == 0) check_every = 16;
+    k.persistent = 0;
+    k.iters_per_launch = 1;
+    const uint64_t grid = (lanes->n_lanes + m->blk - 1) / m->blk;
+    rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
+    if (rc) return rc;
+    uint64_t n = 0;
+    uint32_t fin = 0;
+    for (;;) {
+        HYK_CU(drv().cuMemcpyDtoHAsync(&fin, (CUdeviceptr)k.finished, sizeof fin, s));
+        HYK_CU(drv().cuStreamSynchronize(s));
+        if ((uint64_t)fin >= lanes->n_lanes) break;
+        for (uint32_t c = 0; c < check_every; ++c) {
+            rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
+            if (rc) return rc;
+            ++n;
+        }
+    }
+    if (iters) *iters = n;
+    return 0;
+}
+
+int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld, const double *dt,
+                   double *out, void *stream) {
+    if (n_lanes == 0) return 0;
+    if (!tc || !dt || !out || ld < n_lanes || n_eq == 0) return fail(HYK_ERR_INVALID, "invalid dense-output arguments");
+    const int rc = hyk_generic_dense_eval(tc, n_eq, order, n_lanes, ld, dt, out, stream);
+    if (rc) return fail(HYK_ERR_CUDA, "dense-output kernel launch failed");
+    return 0;
+}
+
+int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
+                      size_t log_len, uint32_t *n_slot, double *flops) {
+    hyk::Dec d;
+    std::string err;
+    if (!hyk::load_dec(dd, d, err)) return fail(HYK_ERR_INVALID, err);
+    if (order < 2 || order > 200) return fail(HYK_ERR_INVALID, "the Taylor order must be in [2, 200]");
+    const uint32_t blk = (cfg && cfg->block_lanes) ? cfg->block_lanes : 128;
+    const bool pin = cfg && (cfg->flags & HYK_CFG_PIN_ARITH);
+    hyk::GenOut g;
+    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err)) return fail(HYK_ERR_INVALID, err);
+    if (n_slot) *n_slot = g.n_slot;
+    if (flops) *flops = g.flops;
+    if (verbose) setenv("HYK_PTXAS_VERBOSE", "1", 1);
+    std::string cubin, lg;
+    const int rc = compile_nvrtc(g.src, "hyk_check.cu", cubin, lg);
+    if (verbose) unsetenv("HYK_PTXAS_VERBOSE");
+    if (log && log_len) {
+        std::snprintf(log, log_len, "%s", lg.c_str());
+    }
+    return rc;
+}
+
+int hyk_fp64_peak(int device, double millis, double *flops_per_s) {
+    char buf[256] = {0};
+    const int rc = hyk_generic_fp64_peak(device, millis, flops_per_s, buf, sizeof buf);
+    if (rc) return fail(HYK_ERR_CUDA, buf);
+    return 0;
+}
+
+}  // extern "C"
+
+// Compile-time check that the module source carries the same parameter block.
+static_assert(sizeof(KParams) % 8 == 0, "unexpected KParams padding");

@@ -1,4 +1,30 @@
-"""hyk - GB300-native batch Taylor integrator with heyoka.py's batch API."""
+"""hyk - GB300-native batch Taylor integrator with heyoka.py's batch API.
+
+The Python surface mirrors heyoka.py's (heyoka/__init__.py): expressions
+(``make_vars``, ``par``, ``time``, elementary functions), the ``model``
+factories, ``taylor_adaptive_batch``, ``taylor_outcome``,
+``continuous_output_batch`` and the ``ensemble_propagate_*`` functions.  The
+arithmetic runs in FP64 CUDA kernels generated per ODE system and compiled
+with NVRTC for sm_103a (libhyk.so, C ABI in include/hyk.h).
+"""
 from .expr import expression, make_vars, par, time, sin, cos, exp, log, sqrt, square, sum, prod  # noqa: F401
 from .decompose import taylor_decompose, order_from_tol  # noqa: F401
-from . import model  # noqa: F401
+from . import model, workloads  # noqa: F401
+from .integrator import taylor_adaptive_batch, taylor_outcome  # noqa: F401
+from .c_output import continuous_output_batch  # noqa: F401
+
+
+def recommended_simd_size(fp_type=float):
+    """Lanes per batch for good GPU occupancy (the reference returns the CPU SIMD width)."""
+    return 32
+
+
+def fp64_peak(device=0, millis=200.0):
+    """Measured FP64 FMA throughput of the device in flop/s (2 flops per FMA)."""
+    import ctypes
+
+    from . import _lib
+
+    v = ctypes.c_double()
+    _lib.check(_lib.load().hyk_fp64_peak(int(device), float(millis), ctypes.byref(v)), "hyk_fp64_peak")
+    return v.value

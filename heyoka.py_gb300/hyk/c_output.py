@@ -1,0 +1,154 @@
+"""``continuous_output_batch``: dense output over a whole batch propagation.
+
+Mirrors the reference's continuous_output_batch (heyoka/taylor_expose_c_output.cpp:259-523):
+``tcs`` of shape ``(n_steps, dim, order + 1, batch_size)`` (the Taylor
+coefficients of every iteration, zero steps of lanes that finished early
+included), ``times`` of shape ``(n_steps + 1, batch_size)`` (the start time,
+then the end time of every iteration), and a call operator taking a time
+batch ``(batch_size,)`` or a 2-D array of batches ``(n, batch_size)`` and
+returning ``(dim, batch_size)`` / ``(n, dim, batch_size)``.
+
+Evaluation runs on the GPU: for each lane the step containing t is found by a
+batched binary search over the lane's end times (the last step whose start
+time is <= t, clamped to the first/last step outside the range), and the
+state polynomial is evaluated by Horner at the double-length offset from the
+step start (libhyk's dense-output kernel).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .core import stream_handle
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _dsub_hi(ah, bh, bl):
+    # hi part of (ah, 0) - (bh, bl) in double-length arithmetic
+    s, e = _two_sum(ah, -bh)
+    e = e + (0.0 - bl)
+    return s + e
+
+
+class continuous_output_batch:
+    def __init__(self, tcs, t_hi, t_lo, order):
+        self._tcs = tcs.contiguous()
+        self._thi = t_hi.contiguous()
+        self._tlo = t_lo.contiguous()
+        self._order = int(order)
+        self._dev = tcs.device
+        self._B = t_hi.shape[1]
+        self._dim = tcs.shape[1]
+        self._out = None
+        n = self._tcs.shape[0]
+        if n:
+            # Search keys: start times of the steps, sign-normalised per lane
+            # so that they are non-decreasing for backward propagations too.
+            self._sgn = torch.where(self._thi[-1] < self._thi[0], -1.0, 1.0).to(torch.float64)
+            self._keys = (self._thi[:n] * self._sgn).t().contiguous()  # (B, n)
+
+    @property
+    def n_steps(self):
+        return int(self._tcs.shape[0])
+
+    @property
+    def batch_size(self):
+        return self._B
+
+    @property
+    def tcs(self):
+        a = self._tcs.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def times(self):
+        a = self._thi.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def output(self):
+        if self._out is None:
+            return None
+        a = self._out.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def bounds(self):
+        t = self._thi.cpu().numpy()
+        return (np.array(t[0]), np.array(t[-1]))
+
+    def _eval_row(self, t):
+        n = self.n_steps
+        idx = torch.searchsorted(self._keys, (t * self._sgn).view(self._B, 1).contiguous(), right=True).view(self._B)
+        idx = (idx - 1).clamp(0, n - 1)
+        lanes = torch.arange(self._B, device=self._dev)
+        tc = self._tcs[idx, :, :, lanes].permute(1, 2, 0).contiguous()  # (dim, order+1, B)
+        dt = _dsub_hi(t, self._thi[idx, lanes], self._tlo[idx, lanes]).contiguous()
+        out = torch.empty((self._dim, self._B), dtype=torch.float64, device=self._dev)
+        L = _lib.load()
+        with torch.cuda.device(self._dev):
+            _lib.check(
+                L.hyk_dense_eval(
+                    tc.data_ptr(), self._dim, self._order, self._B, self._B, dt.data_ptr(), out.data_ptr(),
+                    stream_handle(self._dev.index),
+                ),
+                "hyk_dense_eval",
+            )
+        return out
+
+    def __call__(self, tm):
+        if self.n_steps == 0:
+            raise ValueError("Cannot use a default-constructed continuous_output_batch object")
+        if isinstance(tm, torch.Tensor):
+            t = tm.to(device=self._dev, dtype=torch.float64)
+        else:
+            a = np.asarray(tm)
+            if a.dtype != np.float64:
+                a = a.astype(np.float64, casting="safe")
+            t = torch.tensor(a, dtype=torch.float64, device=self._dev)
+        if t.dim() not in (1, 2):
+            raise ValueError(
+                "Invalid time array passed to a continuous_output_batch object: the number of dimensions "
+                "must be 1 or 2, but it is {} instead".format(t.dim())
+            )
+        if t.dim() == 1:
+            if t.shape[0] != self._B:
+                raise ValueError(
+                    "Invalid time array passed to a continuous_output_batch object: the length must be {} "
+                    "but it is {} instead".format(self._B, t.shape[0])
+                )
+            self._out = self._eval_row(t)
+            return self.output
+        if t.shape[1] != self._B:
+            raise ValueError(
+                "Invalid time array passed to a continuous_output_batch object: the number of columns must be "
+                "{} but it is {} instead".format(self._B, t.shape[1])
+            )
+        rows = [self._eval_row(t[i].contiguous()) for i in range(t.shape[0])]
+        if rows:
+            self._out = rows[-1]
+        res = torch.stack(rows) if rows else torch.empty((0, self._dim, self._B), dtype=torch.float64)
+        a = res.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    def __copy__(self):
+        return continuous_output_batch(self._tcs.clone(), self._thi.clone(), self._tlo.clone(), self._order)
+
+    def __deepcopy__(self, memo):
+        return self.__copy__()
+
+    def __repr__(self):
+        return "Directions : {}\nNumber of steps: {}\nBatch size: {}\n".format(
+            "forward/backward per lane", self.n_steps, self._B
+        )

@@ -1,0 +1,90 @@
+"""GPU module cache and thin wrappers over the C ABI (device pointers in, status out)."""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+
+import torch
+
+from . import _lib
+from .decompose import Decomposition
+
+_cache_lock = threading.Lock()
+_modules: dict = {}
+
+
+class Module:
+    """A compiled (decomposition, order, config) on one device; shared by integrators."""
+
+    def __init__(self, dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False):
+        L = _lib.load()
+        self.dec, self.order, self.device = dec, int(order), int(device)
+        self._cdec, self._keep = dec.as_c()
+        cfg = _lib.hyk_config_t(int(block_lanes), 0, _lib.HYK_CFG_PIN_ARITH if pin_arith else 0, 0)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream().synchronize()
+            _lib.check(
+                L.hyk_module_create(ctypes.byref(self._cdec), self.order, ctypes.byref(cfg), self.device, ctypes.byref(h)),
+                "hyk_module_create",
+            )
+        self.handle = h
+        info = _lib.hyk_module_info_t()
+        _lib.check(L.hyk_module_get_info(h, ctypes.byref(info)))
+        self.info = info
+        self.ws = torch.zeros(64, dtype=torch.int32, device=torch.device("cuda", self.device))
+        self.ws_bytes = int(L.hyk_propagate_workspace_size(h, 0, 1))
+        if self.ws.data_ptr() % 256 != 0:  # pragma: no cover - torch allocations are 512-byte aligned
+            raise _lib.HykError("workspace misaligned")
+
+    @property
+    def source(self) -> str:
+        return _lib.load().hyk_module_source(self.handle).decode()
+
+    def info_dict(self):
+        i = self.info
+        return {
+            "n_eq": i.n_eq,
+            "n_pars": i.n_pars,
+            "order": i.order,
+            "n_u": i.n_u,
+            "block_lanes": i.block_lanes,
+            "smem_per_lane": i.smem_per_lane,
+            "regs_per_thread": i.regs_per_thread,
+            "ctas_per_sm": i.ctas_per_sm,
+            "n_sm": i.n_sm,
+            "local_bytes": i.reserved,
+            "flops_per_step": i.flops_per_step,
+            "compile_seconds": i.compile_seconds,
+        }
+
+
+def get_module(dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False) -> Module:
+    key = (dec.digest(), int(order), int(device), int(block_lanes), bool(pin_arith))
+    with _cache_lock:
+        m = _modules.get(key)
+        if m is None:
+            m = Module(dec, order, device, block_lanes, pin_arith)
+            _modules[key] = m
+        return m
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def lanes_struct(state, pars, t_hi, t_lo):
+    B = state.shape[1]
+    return _lib.hyk_lanes_t(
+        B,
+        state.stride(0) if state.dim() == 2 else B,
+        state.data_ptr(),
+        pars.data_ptr() if pars is not None and pars.numel() > 0 else None,
+        t_hi.data_ptr(),
+        t_lo.data_ptr(),
+    )
+
+
+def stream_handle(device: int):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)

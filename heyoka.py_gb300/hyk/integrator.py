@@ -1,0 +1,750 @@
+"""``taylor_adaptive_batch``: the reference's batch integrator API on the GPU.
+
+Mirrors the Python surface of heyoka.py's batch integrator
+(heyoka/expose_batch_integrators.cpp:214-729, constructor at :91-212 and
+:276-289, dispatch at heyoka/__init__.py:78-86): same constructor arguments,
+methods, properties, return tuples and error messages.  Differences that
+follow from living on a GPU:
+
+* ``state`` and ``pars`` are writable **torch CUDA tensors** (shape
+  ``(n, batch_size)``), not NumPy views; ``ta.state[:] = ...`` works as in the
+  reference.  ``time``, ``dtime``, ``tc``, ``last_h``, ``d_output`` are
+  read-only NumPy copies, as read-only as the reference's.
+* ``batch_size`` is the number of GPU lanes: any size, not the SIMD width.
+* Step callbacks, events, ``high_accuracy``, single precision and the
+  variational API raise ``NotImplementedError``; LLVM code-generation options
+  are accepted and ignored.
+* ``propagate_*`` run every lane to its own final time in one persistent
+  kernel launch (``prop_mode="persistent"``, the default) or with one kernel
+  launch per step (``prop_mode="plain"``).  Per-lane results follow the
+  reference's batch rules; the whole-batch rules that couple lanes are applied
+  afterwards: a step limit reached by any lane gives ``step_limit`` to every
+  lane, and lanes that finished before the batch's last iteration report
+  ``last_h == 0`` and the Taylor coefficients of their final state (the zero
+  steps the reference takes on them).  A non-finite state stops only its own
+  lane (the reference stops the whole batch at that iteration).
+"""
+
+from __future__ import annotations
+
+import copy as _copy
+import enum
+import math
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from .core import get_module, lanes_struct, stream_handle
+from .decompose import order_from_tol, taylor_decompose
+
+EPS = float(np.finfo(np.float64).eps)
+
+
+class taylor_outcome(enum.IntEnum):
+    """Outcome of a step or propagation (values of heyoka/core.cpp:324-329)."""
+
+    success = -4294967297
+    step_limit = -4294967298
+    time_limit = -4294967299
+    err_nf_state = -4294967300
+    cb_stop = -4294967301
+
+
+_LLVM_KWARGS = ("opt_level", "force_avx512", "slp_vectorize", "fast_math", "code_model", "parjit")
+
+
+def _to_f64_array(x, what):
+    a = np.asarray(x)
+    if a.dtype != np.float64:
+        a = a.astype(np.float64, casting="safe")
+    return a
+
+
+def _is_scalar(x):
+    return np.ndim(x) == 0
+
+
+def _dev_index(device):
+    if device is None:
+        if not torch.cuda.is_available():
+            raise _lib.HykError("the GPU batch integrator needs a CUDA device; none is available")
+        return torch.cuda.current_device()
+    d = torch.device(device)
+    if d.type != "cuda":
+        raise ValueError("the GPU batch integrator runs on CUDA devices only, not '{}'".format(device))
+    return d.index if d.index is not None else torch.cuda.current_device()
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _dadd(xh, xl, yh, yl):
+    s, e = _two_sum(xh, yh)
+    e = e + (xl + yl)
+    hi = s + e
+    return hi, e - (hi - s)
+
+
+class LaneArray(torch.Tensor):
+    """A device tensor that also accepts what the reference's NumPy views
+    accept: assignment from lists, tuples and NumPy arrays (converted to
+    float64 on the tensor's device), comparison with them, and conversion
+    with ``numpy.asarray``."""
+
+    def _coerce(self, value):
+        if isinstance(value, torch.Tensor):
+            return value.to(device=self.device, dtype=self.dtype)
+        a = np.asarray(value)
+        if a.dtype != np.float64:
+            a = a.astype(np.float64, casting="safe")
+        return torch.as_tensor(a, device=self.device)
+
+    def __setitem__(self, idx, value):
+        super().__setitem__(idx, self._coerce(value))
+
+    # Comparisons give host NumPy arrays, as comparisons of the reference's views do.
+    def __eq__(self, other):
+        return torch.Tensor.__eq__(self.as_subclass(torch.Tensor), self._coerce(other)).cpu().numpy()
+
+    def __ne__(self, other):
+        return torch.Tensor.__ne__(self.as_subclass(torch.Tensor), self._coerce(other)).cpu().numpy()
+
+    __hash__ = torch.Tensor.__hash__
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.detach().as_subclass(torch.Tensor).cpu().numpy()
+        return a if dtype is None else a.astype(dtype)
+
+
+class taylor_adaptive_batch:
+    """Adaptive Taylor integrator over a batch of lanes, one GPU thread per lane."""
+
+    def __init__(
+        self,
+        sys,
+        state,
+        time=None,
+        pars=None,
+        tol=0.0,
+        high_accuracy=False,
+        compact_mode=False,
+        t_events=[],  # noqa: B006 - mirrors the reference signature
+        nt_events=[],  # noqa: B006
+        parallel_mode=False,
+        *,
+        fp_type=float,
+        device=None,
+        prop_mode="persistent",
+        block_lanes=0,
+        pin_arith=False,
+        **kwargs,
+    ):
+        for k in list(kwargs):
+            if k in _LLVM_KWARGS:
+                kwargs.pop(k)
+                warnings.warn(
+                    "the LLVM option '{}' has no effect on the GPU batch integrator".format(k), stacklevel=2
+                )
+        if kwargs:
+            raise TypeError("unexpected keyword argument(s): {}".format(", ".join(sorted(kwargs))))
+        if fp_type not in (float, np.float64):
+            raise NotImplementedError("the GPU batch integrator supports double precision (fp_type=float) only")
+        if high_accuracy:
+            raise NotImplementedError("high_accuracy mode is not supported by the GPU batch integrator")
+        if len(t_events) or len(nt_events):
+            raise NotImplementedError("event detection is not supported by the GPU batch integrator")
+        if prop_mode not in ("persistent", "plain"):
+            raise ValueError("prop_mode must be 'persistent' or 'plain'")
+        if hasattr(sys, "vargs"):
+            raise NotImplementedError("variational systems are not supported by the GPU batch integrator")
+
+        st = _to_f64_array(state, "state")
+        if st.ndim != 2:
+            raise ValueError(
+                "Invalid state vector passed to the constructor of a batch integrator: "
+                "the expected number of dimensions is 2, but the input array has a dimension of {}".format(st.ndim)
+            )
+        B = st.shape[1]
+        self._dec = taylor_decompose(sys)
+        if st.shape[0] != self._dec.n_eq:
+            raise ValueError(
+                "Inconsistent sizes detected in the initialization of an adaptive Taylor integrator: "
+                "the state vector has a dimension of {}, while the number of equations is {}".format(
+                    st.shape[0], self._dec.n_eq
+                )
+            )
+        if B == 0:
+            raise ValueError("The batch size in an adaptive Taylor integrator cannot be zero")
+        np_ = self._dec.n_pars
+        if pars is not None:
+            pa = np.asarray(pars)
+            if pa.ndim != 2 or pa.shape[1] != B:
+                raise ValueError(
+                    "Invalid parameter vector passed to the constructor of a batch integrator: "
+                    "the expected array shape is (n, {}), but the input array has either the wrong "
+                    "number of dimensions or the wrong shape".format(B)
+                )
+            pa = _to_f64_array(pa, "pars")
+            if pa.shape[0] < np_:
+                raise ValueError(
+                    "Invalid number of parameter values passed to the constructor of an adaptive "
+                    "Taylor integrator: {} parameter value(s) were passed, but the ODE system contains "
+                    "{} parameter(s)".format(pa.shape[0] * B, np_ * B)
+                )
+        else:
+            pa = np.zeros((np_, B))
+        if time is not None:
+            ti = np.asarray(time)
+            if ti.ndim != 1 or ti.shape[0] != B:
+                raise ValueError(
+                    "Invalid time vector passed to the constructor of a batch integrator: "
+                    "the expected array shape is ({}), but the input array has either the wrong "
+                    "number of dimensions or the wrong shape".format(B)
+                )
+            ti = _to_f64_array(ti, "time")
+        else:
+            ti = np.zeros(B)
+        tol = float(tol)
+        if tol == 0.0:
+            tol = EPS
+        self._tol = tol
+        self._order = order_from_tol(tol)
+        self._dev = _dev_index(device)
+        self._tdev = torch.device("cuda", self._dev)
+        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith)
+        self._prop_mode = prop_mode
+        self._compact_mode = bool(compact_mode)
+        self._B = B
+        f64 = dict(dtype=torch.float64, device=self._tdev)
+        self._state = torch.tensor(st, **f64).contiguous()
+        self._pars = torch.tensor(pa, **f64).contiguous()
+        self._thi = torch.tensor(ti, **f64)
+        self._tlo = torch.zeros(B, **f64)
+        self._last_h = torch.zeros(B, **f64)
+        self._tc = torch.zeros((self._dec.n_eq, self._order + 1, B), **f64)
+        self._d_out = torch.zeros((self._dec.n_eq, B), **f64)
+        self._step_res = None
+        self._prop = None  # dict of device arrays of the last propagation
+        self._final_tc_mask = None  # lanes whose tc must be the final-state jets
+
+    # ------------------------------------------------------------------ properties
+    @property
+    def state(self):
+        return self._state.as_subclass(LaneArray)
+
+    @property
+    def pars(self):
+        return self._pars.as_subclass(LaneArray)
+
+    @property
+    def time(self):
+        a = self._thi.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def dtime(self):
+        hi, lo = self._thi.cpu().numpy(), self._tlo.cpu().numpy()
+        hi.flags.writeable = False
+        lo.flags.writeable = False
+        return hi, lo
+
+    @property
+    def order(self):
+        return self._order
+
+    @property
+    def tol(self):
+        return self._tol
+
+    @property
+    def dim(self):
+        return self._dec.n_eq
+
+    @property
+    def batch_size(self):
+        return self._B
+
+    @property
+    def compact_mode(self):
+        return self._compact_mode
+
+    @property
+    def high_accuracy(self):
+        return False
+
+    @property
+    def with_events(self):
+        return False
+
+    @property
+    def decomposition(self):
+        return self._dec.as_list()
+
+    @property
+    def sys(self):
+        return list(self._dec.sys)
+
+    @property
+    def is_variational(self):
+        return False
+
+    @property
+    def device(self):
+        return self._tdev
+
+    @property
+    def module_info(self):
+        """Compiled-kernel facts: block size, shared memory per lane, registers, flops per step."""
+        return self._mod.info_dict()
+
+    @property
+    def prop_mode(self):
+        return self._prop_mode
+
+    @prop_mode.setter
+    def prop_mode(self, v):
+        if v not in ("persistent", "plain"):
+            raise ValueError("prop_mode must be 'persistent' or 'plain'")
+        self._prop_mode = v
+
+    @property
+    def last_h(self):
+        a = self._last_h.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def tc(self):
+        self._refresh_final_tc()
+        a = self._tc.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def d_output(self):
+        a = self._d_out.cpu().numpy()
+        a.flags.writeable = False
+        return a
+
+    @property
+    def step_res(self):
+        if self._step_res is None:
+            return [(taylor_outcome.success, 0.0)] * self._B
+        oc, h = self._step_res
+        oc, h = oc.cpu().numpy(), h.cpu().numpy()
+        return [(taylor_outcome(int(o)), float(x)) for o, x in zip(oc, h)]
+
+    @property
+    def propagate_res(self):
+        if self._prop is None:
+            return [(taylor_outcome.success, math.inf, 0.0, 0)] * self._B
+        p = self._prop
+        oc = p["outcome"].cpu().numpy()
+        mn, mx = p["min_h"].cpu().numpy(), p["max_h"].cpu().numpy()
+        ns = p["n_steps"].cpu().numpy()
+        return [(taylor_outcome(int(a)), float(b), float(c), int(d)) for a, b, c, d in zip(oc, mn, mx, ns)]
+
+    @property
+    def propagate_res_tensors(self):
+        """Device tensors of the last propagation: outcome, min_h, max_h, n_steps, n_iter."""
+        if self._prop is None:
+            return None
+        return {k: self._prop[k] for k in ("outcome", "min_h", "max_h", "n_steps", "n_iter")}
+
+    # ------------------------------------------------------------------ time
+    def _lane_vec(self, v, what):
+        if _is_scalar(v):
+            return torch.full((self._B,), float(v), dtype=torch.float64, device=self._tdev)
+        a = _to_f64_array(v, what)
+        if a.ndim != 1 or a.shape[0] != self._B:
+            raise ValueError(
+                "Invalid {} passed to a batch integrator: the expected array shape is ({}), "
+                "but the input array has either the wrong number of dimensions or the wrong shape".format(
+                    what, self._B
+                )
+            )
+        return torch.tensor(a, dtype=torch.float64, device=self._tdev)
+
+    def set_time(self, time):
+        t = self._lane_vec(time, "time vector")
+        self._thi.copy_(t)
+        self._tlo.zero_()
+
+    def set_dtime(self, hi_time, lo_time):
+        if _is_scalar(hi_time) != _is_scalar(lo_time):
+            raise TypeError("The two arguments to the set_dtime() method must be of the same type")
+        hi = self._lane_vec(hi_time, "time vector")
+        lo = self._lane_vec(lo_time, "time vector")
+        if not (torch.isfinite(hi).all() and torch.isfinite(lo).all()):
+            raise ValueError("Non-finite time values passed to set_dtime()")
+        s, e = _two_sum(hi, lo)
+        self._thi.copy_(s)
+        self._tlo.copy_(e)
+
+    # ------------------------------------------------------------------ stepping
+    def _step(self, max_delta_t, backward, write_tc):
+        L = _lib.load()
+        B = self._B
+        oc = torch.empty(B, dtype=torch.int64, device=self._tdev)
+        h = torch.empty(B, dtype=torch.float64, device=self._tdev)
+        md = None
+        if max_delta_t is not None:
+            md = self._lane_vec(max_delta_t, "max_delta_t vector")
+            if torch.isnan(md).any():
+                raise ValueError("A NaN max_delta_t was passed to the step() function of an adaptive Taylor integrator")
+        lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
+        with torch.cuda.device(self._dev):
+            _lib.check(
+                L.hyk_step(
+                    self._mod.handle, lanes, None if md is None else md.data_ptr(), int(backward),
+                    oc.data_ptr(), h.data_ptr(), self._tc.data_ptr() if write_tc else None, stream_handle(self._dev),
+                ),
+                "hyk_step",
+            )
+        self._step_res = (oc, h)
+        self._last_h = h.clone()
+        if write_tc:
+            self._final_tc_mask = None
+
+    def step(self, max_delta_t=None, write_tc=False):
+        """One step on every lane (optionally clamped by a per-lane ``max_delta_t``)."""
+        if isinstance(max_delta_t, bool):
+            write_tc, max_delta_t = max_delta_t, None
+        if max_delta_t is not None and _is_scalar(max_delta_t):
+            raise TypeError("the max_delta_t argument of the batch step() function must be a vector")
+        self._step(max_delta_t, False, write_tc)
+
+    def step_backward(self, write_tc=False):
+        self._step(None, True, write_tc)
+
+    # ------------------------------------------------------------------ dense output
+    def update_d_output(self, t, rel_time=False):
+        self._refresh_final_tc()
+        tt = self._lane_vec(t, "time vector")
+        if rel_time:
+            dt = self._last_h + tt
+        else:
+            # (t - (time - last_h)) in double-length arithmetic.
+            sh, sl = _dadd(self._thi, self._tlo, -self._last_h, torch.zeros_like(self._last_h))
+            dt, _ = _dadd(tt, torch.zeros_like(tt), -sh, -sl)
+        L = _lib.load()
+        with torch.cuda.device(self._dev):
+            _lib.check(
+                L.hyk_dense_eval(
+                    self._tc.data_ptr(), self.dim, self._order, self._B, self._B, dt.contiguous().data_ptr(),
+                    self._d_out.data_ptr(), stream_handle(self._dev),
+                ),
+                "hyk_dense_eval",
+            )
+        return self.d_output
+
+    def _refresh_final_tc(self):
+        """Lanes that finished before the batch's last iteration: the reference's
+        tc holds the jets of their final state (computed by its zero steps)."""
+        mask = self._final_tc_mask
+        if mask is None:
+            return
+        self._final_tc_mask = None
+        if not bool(mask.any()):
+            return
+        tc = torch.empty_like(self._tc)
+        st, th, tl = self._state.clone(), self._thi.clone(), self._tlo.clone()
+        zero = torch.zeros(self._B, dtype=torch.float64, device=self._tdev)
+        oc = torch.empty(self._B, dtype=torch.int64, device=self._tdev)
+        h = torch.empty_like(zero)
+        L = _lib.load()
+        with torch.cuda.device(self._dev):
+            _lib.check(
+                L.hyk_step(
+                    self._mod.handle, lanes_struct(st, self._pars, th, tl), zero.data_ptr(), 0, oc.data_ptr(),
+                    h.data_ptr(), tc.data_ptr(), stream_handle(self._dev),
+                ),
+                "hyk_step",
+            )
+        self._tc = torch.where(mask.view(1, 1, -1), tc, self._tc)
+
+    # ------------------------------------------------------------------ propagation
+    def _check_prop_args(self, max_delta_t, callback):
+        if callback is not None:
+            raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
+        if max_delta_t is None or (not _is_scalar(max_delta_t) and len(max_delta_t) == 0):
+            return None
+        md = self._lane_vec(max_delta_t, "max_delta_t vector")
+        if torch.isnan(md).any():
+            raise ValueError("A nan max_delta_t was passed to the propagate_*() functions of an adaptive Taylor integrator")
+        if (md <= 0).any():
+            raise ValueError(
+                "A non-positive max_delta_t was passed to the propagate_*() functions of an adaptive Taylor integrator"
+            )
+        return md
+
+    def _alloc_prop(self, with_grid):
+        B, f = self._B, dict(device=self._tdev)
+        p = {
+            "rem_hi": torch.empty(B, dtype=torch.float64, **f),
+            "rem_lo": torch.empty(B, dtype=torch.float64, **f),
+            "outcome": torch.empty(B, dtype=torch.int64, **f),
+            "min_h": torch.empty(B, dtype=torch.float64, **f),
+            "max_h": torch.empty(B, dtype=torch.float64, **f),
+            "n_steps": torch.empty(B, dtype=torch.int64, **f),
+            "n_iter": torch.empty(B, dtype=torch.int64, **f),
+            "grid_idx": torch.empty(B, dtype=torch.int64, **f) if with_grid else None,
+            "last_h": torch.empty(B, dtype=torch.float64, **f),
+            "status": torch.empty(B, dtype=torch.int32, **f),
+        }
+        return p
+
+    def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None):
+        """Initialise and run a propagation of every lane to (tf_hi, tf_lo)."""
+        L = _lib.load()
+        if max_steps < 0:
+            raise ValueError("max_steps must be non-negative")
+        B, ne, order = self._B, self.dim, self._order
+        p = self._alloc_prop(grid is not None)
+        grid_out = None
+        if grid is not None:
+            grid_out = torch.empty((grid.shape[0], ne, B), dtype=torch.float64, device=self._tdev)
+        want_tc = write_tc or c_output
+        last_tc = torch.empty_like(self._tc) if want_tc else None
+        cap = 0
+        tcs = thi = tlo = None
+        if c_output:
+            cap = 64
+            tcs = torch.empty((cap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
+            thi = torch.empty((cap, B), dtype=torch.float64, device=self._tdev)
+            tlo = torch.empty((cap, B), dtype=torch.float64, device=self._tdev)
+        t0h, t0l = self._thi.clone(), self._tlo.clone()
+
+        def desc():
+            return _lib.hyk_prop_t(
+                tf_hi.data_ptr(), None if tf_lo is None else tf_lo.data_ptr(), None if md is None else md.data_ptr(),
+                int(max_steps),
+                None if grid is None else grid.data_ptr(), 0 if grid is None else grid.shape[0],
+                None if grid_out is None else grid_out.data_ptr(),
+                None if tcs is None else tcs.data_ptr(), None if thi is None else thi.data_ptr(),
+                None if tlo is None else tlo.data_ptr(), cap,
+                p["rem_hi"].data_ptr(), p["rem_lo"].data_ptr(), p["outcome"].data_ptr(), p["min_h"].data_ptr(),
+                p["max_h"].data_ptr(), p["n_steps"].data_ptr(), p["n_iter"].data_ptr(),
+                None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
+                None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
+            )
+
+        lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
+        mode = _lib.HYK_MODE_PERSISTENT if self._prop_mode == "persistent" else _lib.HYK_MODE_PLAIN
+        with torch.cuda.device(self._dev):
+            s = stream_handle(self._dev)
+            d = desc()
+            _lib.check(L.hyk_prop_init(self._mod.handle, lanes, d, s), "hyk_prop_init")
+            while True:
+                _lib.check(
+                    L.hyk_propagate(self._mod.handle, lanes, d, mode, self._mod.ws.data_ptr(), self._mod.ws_bytes, 16, None, s),
+                    "hyk_propagate",
+                )
+                if not c_output:
+                    break
+                full = (p["status"] & _lib.LANE_CAPACITY) != 0
+                if not bool(full.any()):
+                    break
+                # Grow the coefficient store and resume the lanes that filled it.
+                ncap = cap * 2
+                ntcs = torch.empty((ncap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
+                nthi = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
+                ntlo = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
+                ntcs[:cap] = tcs
+                nthi[:cap] = thi
+                ntlo[:cap] = tlo
+                tcs, thi, tlo, cap = ntcs, nthi, ntlo, ncap
+                p["status"] &= ~(_lib.LANE_CAPACITY | _lib.LANE_STOPPED)
+                d = desc()
+        self._finish_prop(p, group, last_tc)
+        res = {"grid_out": grid_out}
+        if c_output:
+            res["c_output"] = self._make_c_output(p, tcs, thi, tlo, t0h, t0l)
+        return res
+
+    def _finish_prop(self, p, group, last_tc):
+        """Apply the whole-batch rules that couple the lanes of a batch."""
+        B = self._B
+        G = B if group is None else group
+        ng = B // G
+        oc = p["outcome"].view(ng, G)
+        hit = (oc == int(taylor_outcome.step_limit)).any(dim=1, keepdim=True)
+        oc.copy_(torch.where(hit, torch.full_like(oc, int(taylor_outcome.step_limit)), oc))
+        nit = p["n_iter"].view(ng, G)
+        gmax = nit.max(dim=1, keepdim=True).values
+        early = (nit < gmax).view(B)
+        self._last_h = torch.where(early, torch.zeros_like(p["last_h"]), p["last_h"])
+        if last_tc is not None:
+            self._tc = last_tc
+            self._final_tc_mask = early | (p["n_iter"] == 0)
+        self._prop = p
+
+    def _make_c_output(self, p, tcs, thi, tlo, t0h, t0l):
+        from .c_output import continuous_output_batch
+
+        B = self._B
+        nit = p["n_iter"]
+        K = int(nit.max().item()) if B else 0
+        ne, order = self.dim, self._order
+        f64 = dict(dtype=torch.float64, device=self._tdev)
+        out_tcs = torch.empty((K, ne, order + 1, B), **f64)
+        out_thi = torch.empty((K + 1, B), **f64)
+        out_tlo = torch.empty((K + 1, B), **f64)
+        out_thi[0], out_tlo[0] = t0h, t0l
+        if K:
+            out_tcs.copy_(tcs[:K])
+            out_thi[1:].copy_(thi[:K])
+            out_tlo[1:].copy_(tlo[:K])
+            # Zero steps of lanes that finished early: final-state jets, final time.
+            self._final_tc_mask = (nit < K) | (nit == 0)
+            self._refresh_final_tc()
+            idx = torch.arange(K, device=self._tdev).view(K, 1)
+            pad = idx >= nit.view(1, B)
+            out_tcs = torch.where(pad.view(K, 1, 1, B), self._tc.unsqueeze(0), out_tcs)
+            out_thi[1:] = torch.where(pad, self._thi.view(1, B), out_thi[1:])
+            out_tlo[1:] = torch.where(pad, self._tlo.view(1, B), out_tlo[1:])
+        return continuous_output_batch(out_tcs, out_thi, out_tlo, order)
+
+    def _check_time(self, t, what):
+        tt = self._lane_vec(t, what)
+        if not bool(torch.isfinite(tt).all()):
+            raise ValueError(
+                "A non-finite time was passed to the propagate_until() function of an adaptive Taylor integrator"
+            )
+        return tt
+
+    def propagate_until(self, t, max_steps=0, max_delta_t=[], callback=None, write_tc=False, c_output=False):  # noqa: B006
+        """Propagate every lane up to its final time ``t`` (scalar or per lane).
+
+        Returns ``(c_output or None, None)``; per-lane results in ``propagate_res``
+        (reference: heyoka/expose_batch_integrators.cpp:279-314)."""
+        md = self._check_prop_args(max_delta_t, callback)
+        tf = self._check_time(t, "final time vector")
+        r = self._run(tf, None, max_steps, md, write_tc=write_tc, c_output=c_output)
+        return (r.get("c_output"), None)
+
+    def propagate_for(self, delta_t, max_steps=0, max_delta_t=[], callback=None, write_tc=False, c_output=False):  # noqa: B006
+        """Propagate every lane for ``delta_t`` (scalar or per lane); final time =
+        current time + delta_t in double-length arithmetic
+        (reference: heyoka/expose_batch_integrators.cpp:243-278)."""
+        md = self._check_prop_args(max_delta_t, callback)
+        dt = self._check_time(delta_t, "time interval vector")
+        hi, lo = _dadd(self._thi, self._tlo, dt, torch.zeros_like(dt))
+        r = self._run(hi, lo, max_steps, md, write_tc=write_tc, c_output=c_output)
+        return (r.get("c_output"), None)
+
+    def propagate_grid(self, grid, max_steps=0, max_delta_t=[], callback=None):  # noqa: B006
+        """Propagate over a per-lane time grid of shape ``(n, batch_size)``;
+        returns ``(None, out)`` with ``out`` of shape ``(n, dim, batch_size)``
+        (reference: heyoka/expose_batch_integrators.cpp:315-392)."""
+        md = self._check_prop_args(max_delta_t, callback)
+        g = np.asarray(grid) if not isinstance(grid, torch.Tensor) else grid
+        if g.ndim != 2:
+            raise ValueError(
+                "Invalid grid passed to the propagate_grid() method of a batch integrator: "
+                "the expected number of dimensions is 2, but the input array has a dimension of {}".format(g.ndim)
+            )
+        if g.shape[1] != self._B:
+            raise ValueError(
+                "Invalid grid passed to the propagate_grid() method of a batch integrator: "
+                "the shape must be ({}, {}) but the number of columns is {} instead".format("n", self._B, g.shape[1])
+            )
+        if isinstance(g, torch.Tensor):
+            gd = g.to(device=self._tdev, dtype=torch.float64).contiguous()
+        else:
+            gd = torch.tensor(_to_f64_array(g, "grid"), dtype=torch.float64, device=self._tdev)
+        if gd.shape[0] == 0:
+            raise ValueError("Cannot invoke propagate_grid() in a batch integrator if the time grid is empty")
+        if not bool(torch.isfinite(gd).all()):
+            raise ValueError("A non-finite time value was passed to propagate_grid() in an adaptive Taylor integrator")
+        if not bool(((gd[0] == self._thi) & (self._tlo == 0)).all() | (gd[0] == self._thi).all()):
+            raise ValueError(
+                "When invoking propagate_grid(), the first element of the time grid "
+                "must match the current time coordinate"
+            )
+        if gd.shape[0] > 1:
+            dg = gd[1:] - gd[:-1]
+            fwd = (dg > 0).all(dim=0)
+            bwd = (dg < 0).all(dim=0)
+            if not bool((fwd | bwd).all()):
+                raise ValueError("A non-monotonic time grid was passed to propagate_grid()")
+        tf = gd[-1].contiguous()
+        r = self._run(tf, None, max_steps, md, grid=gd)
+        return (None, r["grid_out"].cpu().numpy())
+
+    # ------------------------------------------------------------------ copies
+    def __copy__(self):
+        return self._clone(deep=False)
+
+    def __deepcopy__(self, memo):
+        return self._clone(deep=True, memo=memo)
+
+    def _clone(self, deep, memo=None):
+        new = object.__new__(type(self))
+        for k, v in self.__dict__.items():
+            if isinstance(v, torch.Tensor):
+                new.__dict__[k] = v.clone()
+            elif k in ("_mod", "_dec"):
+                new.__dict__[k] = v
+            elif k in ("_prop",):
+                new.__dict__[k] = None if v is None else {a: (None if b is None else b.clone()) for a, b in v.items()}
+            elif k == "_step_res":
+                new.__dict__[k] = None if v is None else (v[0].clone(), v[1].clone())
+            elif deep and not k.startswith("_"):
+                new.__dict__[k] = _copy.deepcopy(v, memo)
+            else:
+                new.__dict__[k] = v
+        return new
+
+    def __getstate__(self):
+        d = {}
+        for k, v in self.__dict__.items():
+            if k == "_mod":
+                continue
+            if isinstance(v, torch.Tensor):
+                d[k] = v.cpu()
+            elif k == "_prop":
+                d[k] = None if v is None else {a: (None if b is None else b.cpu()) for a, b in v.items()}
+            elif k == "_step_res":
+                d[k] = None if v is None else (v[0].cpu(), v[1].cpu())
+            else:
+                d[k] = v
+        return d
+
+    def __setstate__(self, d):
+        dev = torch.device("cuda", d["_dev"]) if torch.cuda.is_available() else None
+        self.__dict__.update(d)
+        if dev is None:
+            raise _lib.HykError("unpickling a GPU batch integrator needs a CUDA device")
+        for k, v in list(self.__dict__.items()):
+            if isinstance(v, torch.Tensor):
+                self.__dict__[k] = v.to(dev)
+        if self._prop is not None:
+            self._prop = {a: (None if b is None else b.to(dev)) for a, b in self._prop.items()}
+        if self._step_res is not None:
+            self._step_res = (self._step_res[0].to(dev), self._step_res[1].to(dev))
+        self._tdev = dev
+        self._mod = get_module(self._dec, self._order, self._dev)
+
+    def __repr__(self):
+        return (
+            "C++ datatype            : double (GPU, {})\n"
+            "Tolerance               : {!r}\n"
+            "High accuracy           : false\n"
+            "Compact mode            : {}\n"
+            "Taylor order            : {}\n"
+            "Dimension               : {}\n"
+            "Batch size              : {}\n"
+            "Time                    : {}\n"
+            "State                   : {}\n"
+        ).format(
+            self._tdev, self._tol, str(self._compact_mode).lower(), self._order, self.dim, self._B,
+            self.time.tolist() if self._B <= 8 else "[...]",
+            self._state.cpu().numpy().tolist() if self._B <= 8 else "[...]",
+        )

@@ -76,12 +76,7 @@ def nbody(n, Gconst=1.0, masses=None):
         sys += [(xs[i], vxs[i]), (ys[i], vys[i]), (zs[i], vzs[i])]
         for k, v in enumerate((vxs[i], vys[i], vzs[i])):
             sys.append((v, _e.sum(acc[i][k])))
-    # Reorder to the reference layout: per body x, y, z, vx, vy, vz.
-    out = []
-    for i in range(n):
-        blk = sys[6 * i: 6 * i + 6]
-        out += [blk[0], blk[2], blk[4], blk[1], blk[3], blk[5]]
-    return out
+    return sys
 
 
 def cr3bp(mu=1e-3):

@@ -224,8 +224,17 @@ int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_l
                    const double *dt, double *out, void *stream);
 
 /* Device FP64 FMA throughput microbenchmark (flop/s, 2 flops per FMA), used
- * as the roofline denominator.  Runs for about `millis` milliseconds. */
+ * as the roofline denominator.  Runs for about `millis` milliseconds; uses a
+ * one-double-per-CTA scratch buffer of its own. */
 int hyk_fp64_peak(int device, double millis, double *flops_per_s);
+
+/* Build check without a GPU: generate the module source for `d` at `order`
+ * (block size cfg->block_lanes, default 128) and compile it with NVRTC for
+ * sm_103a.  `log` receives the NVRTC log (ptxas register and spill
+ * statistics when `verbose`); `n_slot` the shared-memory doubles per lane,
+ * `flops` the algorithmic flops per step. */
+int hyk_codegen_check(const hyk_decomp_t *d, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
+                      size_t log_len, uint32_t *n_slot, double *flops);
 
 const char *hyk_last_error(void);
 const char *hyk_version(void);

@@ -1,0 +1,91 @@
+"""The C ABI library: loads without a GPU, exports every declared symbol,
+and its code generator emits CUDA that NVRTC compiles for sm_103a."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "hyk.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(hyk_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(libhyk):
+    syms = declared_symbols()
+    assert "hyk_module_create" in syms and "hyk_propagate" in syms
+    for s in syms:
+        assert hasattr(libhyk, s), s
+
+
+def test_python_binding_covers_header(libhyk):
+    from hyk import _lib
+
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_struct_layouts():
+    from hyk import _lib
+    from hyk.decompose import hyk_arg_t, hyk_decomp_t, hyk_uop_t
+
+    assert ctypes.sizeof(hyk_arg_t) == 16 and ctypes.sizeof(hyk_uop_t) == 40
+    assert ctypes.sizeof(hyk_decomp_t) == 32
+    assert ctypes.sizeof(_lib.hyk_lanes_t) == 48
+    assert ctypes.sizeof(_lib.hyk_prop_t) == 22 * 8
+
+
+def test_no_device_errors(libhyk):
+    import hyk
+    from hyk.decompose import taylor_decompose
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    d, keep = taylor_decompose(hyk.workloads.pendulum_sys()).as_c()
+    h = ctypes.c_void_p()
+    rc = libhyk.hyk_module_create(ctypes.byref(d), 20, None, 0, ctypes.byref(h))
+    assert rc != 0 and libhyk.hyk_last_error()
+
+
+@pytest.mark.parametrize("name", ["pendulum", "kepler", "forced", "cr3bp"])
+def test_codegen_compiles_for_sm103a(libhyk, name):
+    import hyk
+    from hyk import _lib, workloads as W
+    from hyk.decompose import taylor_decompose
+
+    x, v = hyk.make_vars("x", "v")
+    systems = {
+        "pendulum": (W.pendulum_sys(), 20),
+        "kepler": (W.kepler_sys(), 19),
+        "forced": ([(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))], 20),
+        "cr3bp": (W.cr3bp_sys(), 19),
+    }
+    sys_, order = systems[name]
+    d, keep = taylor_decompose(sys_).as_c()
+    for pin in (0, 1):
+        cfg = _lib.hyk_config_t(128, 0, pin, 0)
+        buf = ctypes.create_string_buffer(1 << 16)
+        ns, fl = ctypes.c_uint32(), ctypes.c_double()
+        rc = libhyk.hyk_codegen_check(ctypes.byref(d), order, ctypes.byref(cfg), 0, buf, len(buf), ctypes.byref(ns),
+                                      ctypes.byref(fl))
+        assert rc == 0, libhyk.hyk_last_error().decode()
+        assert ns.value > 0 and fl.value > 0
+
+
+def test_codegen_rejects_bad_input(libhyk):
+    from hyk.decompose import hyk_arg_t, hyk_decomp_t, hyk_uop_t
+
+    ops = (hyk_uop_t * 1)()
+    ops[0].op, ops[0].aux = 2, -1
+    ops[0].a.kind, ops[0].a.idx = 1, 5  # refers to a later u-variable
+    ops[0].b.kind, ops[0].b.idx = 1, 0
+    rhs = (hyk_arg_t * 1)()
+    rhs[0].kind, rhs[0].idx = 1, 1
+    d = hyk_decomp_t(1, 1, 0, 0, ctypes.cast(ops, ctypes.POINTER(hyk_uop_t)), ctypes.cast(rhs, ctypes.POINTER(hyk_arg_t)))
+    rc = libhyk.hyk_codegen_check(ctypes.byref(d), 10, None, 0, None, 0, None, None)
+    assert rc == -1 and b"invalid" in libhyk.hyk_last_error()

@@ -1,0 +1,233 @@
+"""The CPU oracle against the reference's own known-answer outputs.
+
+The reference cannot run here; its notebooks' recorded outputs
+(tests/golden/notebook_pins.json, extracted by tests/golden/make_golden.py)
+pin the oracle: step sizes bit-exact, step counts exact, min/max step sizes
+to a few ulp (they sit at the end of long chaotic or near-chaotic runs, where
+the reference's exact operation order, which is not observable, moves the
+last bits), printed 8-digit states exactly.
+"""
+
+import numpy as np
+import pytest
+
+import hyk
+from hyk.decompose import order_from_tol
+
+
+def traj_rel_err(a, b):
+    """Per-trajectory relative error: max |a - b| over the state / max |b|."""
+    return np.max(np.abs(a - b), axis=0) / np.max(np.abs(b), axis=0)
+
+
+def ulps(a, b):
+    return abs(a - b) / np.spacing(max(abs(a), abs(b)))
+
+
+def pend():
+    x, v = hyk.make_vars("x", "v")
+    return [(x, v), (v, -9.8 * hyk.sin(x))]
+
+
+def forced():
+    x, v = hyk.make_vars("x", "v")
+    return [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
+
+
+def test_order_rule(pins):
+    assert order_from_tol(2.220446049250313e-16) == pins["pendulum"]["order"] == 20
+    assert order_from_tol(1e-9) == pins["pendulum_tol1e-9"]["order"] == 12
+    assert order_from_tol(1e-15) == 19
+    with pytest.raises(ValueError):
+        order_from_tol(-1.0)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_scalar_pendulum_steps(oracle, pins, mode):
+    p = pins["pendulum"]
+    o = oracle.Oracle(pend(), [[0.05], [0.025]], order=20, mode=mode)
+    oc, h = o.step()
+    assert h[0] == p["first_h"] and oc[0] == hyk.taylor_outcome.success
+    oc, h = o.step(backward=True)
+    assert h[0] == p["back_h"]
+    oc, h = o.step(0.01)
+    assert h[0] == 0.01 and oc[0] == hyk.taylor_outcome.time_limit
+    oc, h = o.step(-0.02)
+    assert h[0] == -0.02 and oc[0] == hyk.taylor_outcome.time_limit
+    assert o.t_hi[0] == p["after_clamped_steps"]["time"]
+    assert np.all(np.round(o.state.ravel(), 8) == p["after_clamped_steps"]["state_8digits"])
+
+
+def test_scalar_pendulum_propagate(oracle, pins):
+    p = pins["pendulum"]
+    o = oracle.Oracle(pend(), [[0.05], [0.025]], order=20, mode=0)
+    r = o.propagate_for(5.0)
+    assert r["n_steps"][0] == p["for5"]["n_steps"]
+    assert r["min_h"][0] == p["for5"]["min_h"] and r["max_h"][0] == p["for5"]["max_h"]
+    assert r["outcome"][0] == hyk.taylor_outcome.time_limit and o.t_hi[0] == 5.0
+    r = o.propagate_until(20.0)
+    assert r["n_steps"][0] == p["until20"]["n_steps"]
+    assert r["min_h"][0] == p["until20"]["min_h"]
+    assert ulps(r["max_h"][0], p["until20"]["max_h"]) <= 4
+    r = o.propagate_until(0.0)
+    assert r["n_steps"][0] == p["until0"]["n_steps"]
+    assert ulps(r["min_h"][0], p["until0"]["min_h"]) <= 4
+    assert ulps(r["max_h"][0], p["until0"]["max_h"]) <= 4
+    # forward 20 and back: the state returns to the initial condition within a few ulp
+    assert np.allclose(o.state.ravel(), p["until0"]["state"], rtol=0, atol=1e-16 * 8)
+
+
+def test_scalar_pendulum_grid(oracle, pins):
+    p = pins["pendulum"]["grid"]
+    o = oracle.Oracle(pend(), [[0.05], [0.025]], order=20, mode=0)
+    r = o.propagate_grid(np.array(p["grid"]).reshape(-1, 1))
+    assert r["n_steps"][0] == p["n_steps"]
+    assert r["max_h"][0] == p["max_h"]
+    assert ulps(r["min_h"][0], p["min_h"]) <= 4
+    out = r["grid"][:, :, 0]
+    assert np.all(np.round(out, 8) == np.array(p["out_8digits"]))
+    assert np.all(out[0] == [0.05, 0.025])
+
+
+def test_tol_1e9_round_trip(oracle, pins):
+    p = pins["pendulum_tol1e-9"]
+    o = oracle.Oracle(pend(), [[0.05], [0.025]], order=order_from_tol(p["tol"]), mode=0)
+    o.propagate_until(10.0)
+    o.propagate_until(0.0)
+    # At tol 1e-9 the round-trip error (~1e-12) is truncation error, which
+    # the algorithm determines: the reference's printed state is reproduced
+    # to a relative 1e-12 of the error itself.
+    err = o.state.ravel() - np.array([0.05, 0.025])
+    ref = np.array(p["state_after_10_and_back"]) - np.array([0.05, 0.025])
+    assert np.all(np.abs(err - ref) <= 1e-3 * np.abs(ref))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_forced_pendulum(oracle, pins, mode):
+    q = pins["forced_pendulum_batch"]
+    o = oracle.Oracle(forced(), q["state"], pars=q["pars"], order=20, mode=mode)
+    oc, h = o.step()
+    assert list(h) == q["step_h"]
+    o.step([0.010, 0.011, 0.012, 0.013])
+    assert np.all(np.round(o.state, 8) == q["after_clamped_step"]["state_8digits"])
+    assert np.all(np.round(o.t_hi, 8) == q["after_clamped_step"]["time_8digits"])
+    r = o.propagate_for([10.0, 11.0, 12.0, 13.0])
+    for i, e in enumerate(q["for"]["res"]):
+        assert r["n_steps"][i] == e["n_steps"]
+        assert abs(r["min_h"][i] - e["min_h"]) <= 1e-14 * e["min_h"]
+        assert abs(r["max_h"][i] - e["max_h"]) <= 1e-14 * e["max_h"]
+    assert np.all(np.round(o.state, 8) == q["for"]["state_8digits"])
+    r = o.propagate_until([20.0, 21.0, 22.0, 23.0])
+    for i, e in enumerate(q["until"]["res"]):
+        assert r["n_steps"][i] == e["n_steps"]
+        assert abs(r["min_h"][i] - e["min_h"]) <= 1e-13 * e["min_h"]
+        assert abs(r["max_h"][i] - e["max_h"]) <= 1e-13 * e["max_h"]
+    assert np.all(np.round(o.state, 8) == q["until"]["state_8digits"])
+    assert np.all(o.t_hi == [20.0, 21.0, 22.0, 23.0])
+
+
+def test_batch_forced_pendulum_grid(oracle, pins):
+    q = pins["forced_pendulum_batch"]
+    o = oracle.Oracle(forced(), q["state"], pars=q["pars"], order=20, mode=0)
+    g = np.repeat(np.linspace(0, 100, 1000), 4).reshape(1000, -1)
+    r = o.propagate_grid(g)
+    for i, e in enumerate(q["grid"]["res"]):
+        assert r["n_steps"][i] == e["n_steps"]
+        # t = 100 of a chaotic system: agreement to 1e-12 relative
+        assert abs(r["min_h"][i] - e["min_h"]) <= 1e-12 * e["min_h"]
+        assert abs(r["max_h"][i] - e["max_h"]) <= 1e-12 * e["max_h"]
+    assert np.all(np.isfinite(r["grid"]))
+
+
+def test_batch_dense_and_continuous_output(oracle, pins):
+    q = pins["forced_pendulum_batch"]
+    o = oracle.Oracle(forced(), q["state"], pars=q["pars"], order=20, mode=0)
+    o.step()
+    assert np.all(o.tc[:, 0, :] == np.array(q["tc_order0"]))
+    # update_d_output(t) for absolute t right after one step from t = 0:
+    # Horner at offset t (the step started at 0).
+    dt = np.array([0.01, 0.02, 0.03, 0.04])
+    tc = o.tc
+    out = np.zeros((2, 4))
+    for i in range(2):
+        acc = tc[i, -1]
+        for n in range(tc.shape[1] - 2, -1, -1):
+            acc = acc * dt + tc[i, n]
+        out[i] = acc
+    assert np.all(np.round(out, 8) == q["d_output_8digits"])
+    # continuous output over [0, 10.x]: value at t = 0.03 of lane 2
+    o = oracle.Oracle(forced(), q["state"], pars=q["pars"], order=20, mode=0)
+    r = o.propagate_until(q["c_output"]["t"], c_output=True)
+    tcs, thi = r["c_tcs"], r["c_thi"]
+    lane, t = 2, 0.03
+    k = np.searchsorted(thi[:-1, lane], t, side="right") - 1
+    d = t - thi[k, lane]
+    acc = tcs[k, 1, -1, lane]
+    for n in range(tcs.shape[2] - 2, -1, -1):
+        acc = acc * d + tcs[k, 1, n, lane]
+    assert abs(acc - q["c_output"]["c_arr_0_1_2"]) <= 2 * np.spacing(acc)
+
+
+def test_gpu_arith_mode_matches_pin_mode(oracle):
+    """The GPU arithmetic (FMA, reciprocals) changes only the last bits."""
+    from hyk import workloads as W
+
+    st = W.kepler_ics(32)
+    a = oracle.Oracle(W.kepler_sys(), st, order=19, mode=0)
+    b = oracle.Oracle(W.kepler_sys(), st, order=19, mode=1)
+    ra, rb = a.propagate_until(20.0), b.propagate_until(20.0)
+    assert np.max(traj_rel_err(b.state, a.state)) < 1e-12
+    assert np.all(ra["n_steps"] == rb["n_steps"])
+
+
+def test_vector_and_scalar_overloads_identical(oracle):
+    o1 = oracle.Oracle(pend(), [[0.0, 0.1, 0.2, 0.3], [0.25, 0.26, 0.27, 0.28]], order=20)
+    o2 = oracle.Oracle(pend(), [[0.0, 0.1, 0.2, 0.3], [0.25, 0.26, 0.27, 0.28]], order=20)
+    r1 = o1.propagate_for([10.0] * 4, max_delta_t=[1e-1] * 4)
+    r2 = o2.propagate_for(10.0, max_delta_t=1e-1)
+    assert np.all(o1.state == o2.state)
+    for k in ("n_steps", "min_h", "max_h", "outcome"):
+        assert np.all(r1[k] == r2[k])
+
+
+def test_ensemble_equals_serial(oracle):
+    from hyk import workloads as W
+
+    st = W.pendulum_ics(24, seed=5)
+    ens = oracle.ensemble_until(W.pendulum_sys(), st, None, 0.0, 20.0, order=20, batch=4, n_threads=4, mode=0)
+    for b in range(6):
+        o = oracle.Oracle(W.pendulum_sys(), st[:, 4 * b: 4 * b + 4], order=20, mode=0)
+        r = o.propagate_until(20.0)
+        assert np.all(o.state == ens["state"][:, 4 * b: 4 * b + 4])
+        assert np.all(r["n_steps"] == ens["n_steps"][4 * b: 4 * b + 4])
+
+
+def test_max_steps_and_zero_duration(oracle):
+    o = oracle.Oracle(pend(), [[0.05, 0.06], [0.025, 0.02]], order=20)
+    r = o.propagate_until(10.0, max_steps=3)
+    assert np.all(r["outcome"] == hyk.taylor_outcome.step_limit)
+    assert np.all(r["n_steps"] == 3)
+    o.t_lo[:] = 0.0  # a time with no low part: the target is exactly the current time
+    r = o.propagate_until(o.t_hi.copy())
+    assert np.all(r["outcome"] == hyk.taylor_outcome.time_limit)
+    assert np.all(r["n_steps"] == 0) and np.all(r["min_h"] == np.inf) and np.all(r["max_h"] == 0)
+
+
+def test_non_finite_state(oracle):
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, hyk.log(x))]  # log of a negative number -> NaN
+    o = oracle.Oracle(sys_, [[-1.0, 1.0], [0.0, 0.0]], order=20)
+    r = o.propagate_until(1.0)
+    assert r["outcome"][0] == hyk.taylor_outcome.err_nf_state
+
+
+def test_quad_reference_error_kepler(oracle):
+    """Error of the double-precision run against a binary128 run at tol 1e-32."""
+    from hyk import workloads as W
+
+    st = W.kepler_ics(8)
+    d = oracle.Oracle(W.kepler_sys(), st, order=19, mode=1)
+    q = oracle.Oracle(W.kepler_sys(), st, order=order_from_tol(1e-32), prec=1, mode=0)
+    d.propagate_until(10.0)
+    q.propagate_until(10.0)
+    assert np.max(traj_rel_err(d.state, q.state)) < 1e-12
