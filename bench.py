@@ -1,0 +1,360 @@
+"""Benchmark: FP64 Taylor trajectory-steps/s on the 2^20-orbit Kepler ensemble.
+
+Workload (the reference metric's configuration): 3D Keplerian two-body, mu = 1,
+tol = 1e-15 (Taylor order 19), 2^20 orbits with a ~ U[0.5, 2], e ~ U[0, 0.6],
+i ~ U[0, pi/4], Omega, omega, M ~ U[0, 2 pi) (seeded synthetic elements
+converted to Cartesian), propagated from t = 0 to t = 200.  One bench "step"
+propagates the whole ensemble over 200 / K time units, so the K timed steps
+together are exactly the propagation to t = 200.  The ensemble stays resident
+in HBM; its per-lane state and bookkeeping (~170 MB) exceed the 129 MB L2.
+
+value: trajectory-steps/s (sum over lanes of accepted non-zero steps / time)
+of the persistent batched kernel.  e2e: the same metric through the public
+API with the state copied from pinned host memory before, and the state and
+step counts copied back after, every step.  paths.plain: the one-launch-per-
+step form on the same workload.  roofline: algorithmic FP64 flops of the
+propagation kernel / its CUDA-event duration, against the FP64 FMA peak
+measured in the same process.  cpu_baseline: the CPU restatement of the
+reference's algorithm (oracle, reference arithmetic, batches of 8 lanes,
+OpenMP over all host cores) on a bounded sample of the same orbits.
+
+--impl reference times that CPU restatement alone (the reference itself,
+heyoka.py over the heyoka C++ library, is not installable here).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "heyoka.py_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "FP64 Taylor trajectory-steps/s, 2^20-orbit Kepler ensemble (tol 1e-15, t=0..200)"
+UNIT = "trajectory-steps/s"
+T_END = 200.0
+TOL = 1e-15
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="hyk", choices=["hyk", "reference"])
+    ap.add_argument("--orbits", type=int, default=1 << 20)
+    ap.add_argument("--cpu-sample", type=int, default=2048)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def cpu_baseline(n_orbits, seed, t_end, steps=1):
+    """Time the CPU restatement on n_orbits of the same ensemble, all host threads."""
+    import numpy as np
+
+    import pyoracle
+    from hyk import workloads as W
+
+    st = W.kepler_ics(1 << 20, seed=seed)
+    idx = np.random.default_rng(123).choice(st.shape[1], n_orbits, replace=False)
+    sample = np.ascontiguousarray(st[:, np.sort(idx)])
+    threads = pyoracle.lib().hyko_max_threads()
+    best = None
+    tot_steps = 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r = pyoracle.ensemble_until(W.kepler_sys(), sample, None, 0.0, t_end, order=19, batch=8, n_threads=threads, mode=0)
+        dt = time.perf_counter() - t0
+        tot_steps = int(r["n_steps"].sum())
+        v = tot_steps / dt
+        best = v if best is None else max(best, v)
+    return {
+        "value": best,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": "{} of the 2^20 orbits (seeded subset), t=0..{:g}, batches of 8 lanes, {} trajectory-steps".format(
+            n_orbits, t_end, tot_steps
+        ),
+    }
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = (
+        "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+        "clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index):
+        self.p = None
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        cpu_baseline(min(args.cpu_sample, 256), 1, T_END)
+    vals = []
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args.cpu_sample, 1, T_END)["value"])
+    wall = time.perf_counter() - t_start
+    base = cpu_baseline(64, 1, 1.0)
+    v = statistics.median(vals)
+    line = {
+        "metric": METRIC,
+        "value": v,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Kepler elements)",
+        "config": {"workload": "kepler-2^20 tol=1e-15 t=0..200 (CPU sample of {} orbits per step)".format(args.cpu_sample)},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": base["cores"], "kind": "port",
+                         "sample": "{} seeded orbits of the ensemble per step, t=0..200, CPU restatement of the "
+                                   "reference's algorithm with the reference's arithmetic".format(args.cpu_sample)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "heyoka.py needs the heyoka C++ library, which is not installable offline; the timed CPU code is this "
+                "repository's restatement of its algorithm (oracle/hyk_oracle.cpp)",
+        "wall_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+    import torch
+
+    import hyk
+    from hyk import workloads as W
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    K, Wm = max(1, args.steps), max(3, args.warmup)
+    dt = T_END / K
+    n = args.orbits
+    st = W.kepler_ics(n, seed=1 + rank)
+    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    info = ta.module_info
+    flops_step = info["flops_per_step"]
+    peak = hyk.fp64_peak(dev, 300.0)
+
+    # warm-up on a copy (same kernel, same data)
+    wcopy = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    for k in range(Wm):
+        wcopy.propagate_until((k + 1) * dt)
+    del wcopy
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- timed: persistent kernel, device-resident ensemble
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    kevs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    steps_per = []
+    clk = Clocks(dev)
+    barrier()
+    t_wall = time.perf_counter()
+    for k in range(K):
+        evs[k][0].record(stream)
+        ta._launch_events = kevs[k]
+        ta.propagate_until((k + 1) * dt)
+        evs[k][1].record(stream)
+        steps_per.append(ta.propagate_res_tensors["n_steps"].sum())
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clocks = clk.stop()
+    ta._launch_events = None
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    kern_ms = [a.elapsed_time(b) for a, b in kevs]
+    n_steps = int(torch.stack(steps_per).sum().item())
+    t_gpu = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([t_gpu], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_gpu = t.item()
+        c = torch.tensor([n_steps], device="cuda", dtype=torch.float64)
+        dist.all_reduce(c)
+        total_steps = int(c.item())
+    else:
+        total_steps = n_steps
+    value = total_steps / t_gpu
+    outcomes_ok = bool((ta.propagate_res_tensors["outcome"] == int(hyk.taylor_outcome.time_limit)).all())
+    final_t_ok = bool(np.all(ta.time == T_END))
+    alg_flops = flops_step * n_steps
+    achieved = alg_flops / (sum(kern_ms) / 1e3)
+
+    # ---- e2e through the public API with host buffers (pinned), same workload
+    host_state = torch.tensor(st, dtype=torch.float64).pin_memory()
+    out_state = torch.empty_like(host_state).pin_memory()
+    out_steps = torch.empty(n, dtype=torch.int64).pin_memory()
+    ta2 = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    ta2.propagate_until(dt)  # warm
+    ta2.set_time(0.0)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    cur = host_state
+    e2e_steps = []
+    for k in range(K):
+        ta2.state.copy_(cur, non_blocking=True)
+        ta2.propagate_until((k + 1) * dt)
+        out_state.copy_(ta2.state, non_blocking=True)
+        out_steps.copy_(ta2.propagate_res_tensors["n_steps"], non_blocking=True)
+        e2e_steps.append(ta2.propagate_res_tensors["n_steps"].sum())
+        cur = out_state
+    e1.record(stream)
+    barrier()
+    e2e_t = e0.elapsed_time(e1) / 1e3
+    e2e_total = int(torch.stack(e2e_steps).sum().item())
+    e2e = {
+        "value": e2e_total * world / e2e_t if world > 1 else e2e_total / e2e_t,
+        "unit": UNIT,
+        "h2d_bytes_per_step": int(host_state.numel() * 8),
+        "d2h_bytes_per_step": int(out_state.numel() * 8 + out_steps.numel() * 8),
+    }
+    del ta2
+
+    # ---- plain (one launch per step) on the same workload, one pass 0..200
+    paths = {"persistent": value}
+    if not args.no_plain:
+        tp = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev), prop_mode="plain")
+        tp.propagate_until(1.0)
+        tp.set_time(0.0)
+        tp.state[:] = st
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        tp.propagate_until(T_END)
+        b.record(stream)
+        barrier()
+        ps = int(tp.propagate_res_tensors["n_steps"].sum().item())
+        paths["plain"] = ps / (a.elapsed_time(b) / 1e3)
+        paths["persistent_over_plain"] = value / paths["plain"]
+        del tp
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_sample, 1, T_END)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": K,
+            "warmup": Wm,
+            "ms_per_step": t_gpu / K * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded Kepler elements, per-rank seed)",
+            "config": {
+                "workload": "kepler-2^20 tol=1e-15 t=0..200",
+                "orbits_per_gpu": n,
+                "order": ta.order,
+                "step": "propagate the resident ensemble over {:g} time units (K steps = t 0..200)".format(dt),
+                "l2": "inputs larger than L2 (state + bookkeeping ~{:.0f} MB per GPU)".format(n * 21 * 8 / 1e6),
+                "block_lanes": info["block_lanes"],
+                "regs_per_thread": info["regs_per_thread"],
+                "smem_per_lane": info["smem_per_lane"],
+                "parallelism": "independent shards of orbits per GPU" if world > 1 else "single GPU",
+            },
+            "e2e": e2e,
+            "paths": paths,
+            "gpu_launches": 2 * K,
+            "roofline": {
+                "bound": "fp64",
+                "achieved": achieved / 1e12,
+                "peak": peak / 1e12,
+                "unit": "TFLOP/s",
+                "frac": achieved / peak,
+                "traffic": None,
+                "kernel": "hyk_prop_kernel (persistent)",
+                "flops_per_traj_step": flops_step,
+                "peak_source": "measured in-process FP64 FMA probe (hyk_fp64_peak), of measured",
+            },
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "checks": {"all_time_limit": outcomes_ok, "final_time_exact": final_t_ok, "total_traj_steps": total_steps},
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -309,6 +309,25 @@ struct Gen {
         }
     }
 
+    // Whether the order-j coefficient (or j * a_j) of an argument can be
+    // non-zero; checked before building an expression, so that no history is
+    // requested for a term that vanishes.
+    static bool nz(const Ref &r, uint32_t j) {
+        switch (r.kind) {
+        case HYK_ARG_U:
+            return true;
+        case HYK_ARG_TIME:
+            return j <= 1;
+        case HYK_ARG_NUM:
+        case HYK_ARG_PAR:
+            return j == 0;
+        }
+        return false;
+    }
+    static bool knz(const Ref &r, uint32_t j) {
+        return (r.kind == HYK_ARG_U && j >= 1) || (r.kind == HYK_ARG_TIME && j == 1);
+    }
+
     std::string fma(const std::string &x, const std::string &y, const std::string &c) const {
         if (pin) return "(" + c + " + " + x + " * " + y + ")";
         return "__fma_rn(" + x + ", " + y + ", " + c + ")";
@@ -377,7 +396,8 @@ struct Gen {
         }
         case HYK_OP_MUL: {
             Acc s{acc};
-            for (uint32_t j = 0; j <= n; ++j) term(s, cf(A, j, n), cf(B, n - j, n));
+            for (uint32_t j = 0; j <= n; ++j)
+                if (nz(A, j) && nz(B, n - j)) term(s, cf(A, j, n), cf(B, n - j, n));
             def(u, n, s.first ? z : acc);
             break;
         }
@@ -390,7 +410,8 @@ struct Gen {
                 break;
             }
             Acc s{acc};
-            for (uint32_t j = 1; j <= n; ++j) term(s, cf(B, j, n), ucoef(u, n - j, n));
+            for (uint32_t j = 1; j <= n; ++j)
+                if (nz(B, j)) term(s, cf(B, j, n), ucoef(u, n - j, n));
             const std::string av = an.empty() ? z : an;
             const std::string num = s.first ? av : "(" + av + " - " + acc + ")";
             if (!s.first) flops += 1;
@@ -400,19 +421,20 @@ struct Gen {
         }
         case HYK_OP_SQUARE: {
             Acc s{acc};
-            for (uint32_t j = 0; 2 * j < n; ++j) term(s, cf(A, j, n), cf(A, n - j, n));
+            for (uint32_t j = 0; 2 * j < n; ++j)
+                if (nz(A, j) && nz(A, n - j)) term(s, cf(A, j, n), cf(A, n - j, n));
             if (!s.first) {
                 o << "    " << acc << " = " << acc << " + " << acc << ";\n";
                 flops += 1;
             }
-            if (n % 2 == 0) term(s, cf(A, n / 2, n), cf(A, n / 2, n));
+            if (n % 2 == 0 && nz(A, n / 2)) term(s, cf(A, n / 2, n), cf(A, n / 2, n));
             def(u, n, s.first ? z : acc);
             break;
         }
         case HYK_OP_SQRT: {
             const std::string an = cf(A, n, n);
             if (n == 0) {
-                def(u, 0, "sqrt(" + an + ")");
+                def(u, 0, "sqrt(" + an + ")");  // IEEE square root in both arithmetics
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / (2.0 * " << vname(u, 0) << ");\n";
                 flops += 3;
                 break;
@@ -434,7 +456,7 @@ struct Gen {
             const double alpha = op.b.num;
             const std::string a0 = cf(A, 0, n);
             if (n == 0) {
-                def(u, 0, "pow(" + a0 + ", " + lit(alpha) + ")");
+                def(u, 0, (pin ? "pow(" : "hyk_dm_pow(") + a0 + ", " + lit(alpha) + ")");
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
                 flops += 21;
                 break;
@@ -462,28 +484,30 @@ struct Gen {
         }
         case HYK_OP_EXP: {
             if (n == 0) {
-                def(u, 0, "exp(" + cf(A, 0, n) + ")");
+                def(u, 0, (pin ? "exp(" : "hyk_dm_exp(") + cf(A, 0, n) + ")");
                 flops += 20;
                 break;
             }
             Acc s{acc};
-            for (uint32_t j = 1; j <= n; ++j) term(s, kcf(A, j, n), ucoef(u, n - j, n));
+            for (uint32_t j = 1; j <= n; ++j)
+                if (knz(A, j)) term(s, kcf(A, j, n), ucoef(u, n - j, n));
             def(u, n, s.first ? z : divn(acc, n));
             break;
         }
         case HYK_OP_LOG: {
             const std::string a0 = cf(A, 0, n), an = cf(A, n, n);
             if (n == 0) {
-                def(u, 0, "log(" + a0 + ")");
+                def(u, 0, (pin ? "log(" : "hyk_dm_log(") + a0 + ")");
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
                 flops += 21;
                 break;
             }
             Acc s{acc};
-            for (uint32_t j = 1; j < n; ++j) {
-                const Ref self{HYK_ARG_U, (int)u, false, 0, -1};
-                term(s, kcf(self, j, n), cf(A, n - j, n));
-            }
+            if (varying(A))
+                for (uint32_t j = 1; j < n; ++j) {
+                    const Ref self{HYK_ARG_U, (int)u, false, 0, -1};
+                    if (nz(A, n - j)) term(s, kcf(self, j, n), cf(A, n - j, n));
+                }
             const std::string av = an.empty() ? z : an;
             std::string num = av;
             if (!s.first) {
@@ -503,7 +527,8 @@ struct Gen {
                 if (u < partner) {
                     const uint32_t su = is_sin ? u : partner, cu = is_sin ? partner : u;
                     o << "    double " << vname(su, 0) << "_m, " << vname(cu, 0) << "_m;\n";
-                    o << "    sincos(" << cf(A, 0, n) << ", &" << vname(su, 0) << "_m, &" << vname(cu, 0) << "_m);\n";
+                    o << "    " << (pin ? "sincos(" : "hyk_dm_sincos(") << cf(A, 0, n) << ", &" << vname(su, 0) << "_m, &"
+                      << vname(cu, 0) << "_m);\n";
                     o << "    const double " << vname(su, 0) << " = " << vname(su, 0) << "_m;\n";
                     o << "    const double " << vname(cu, 0) << " = " << vname(cu, 0) << "_m;\n";
                     flops += 40;
@@ -511,7 +536,8 @@ struct Gen {
                 break;
             }
             Acc s{acc};
-            for (uint32_t j = 1; j <= n; ++j) term(s, kcf(A, j, n), ucoef(partner, n - j, n));
+            for (uint32_t j = 1; j <= n; ++j)
+                if (knz(A, j)) term(s, kcf(A, j, n), ucoef(partner, n - j, n));
             if (s.first)
                 def(u, n, z);
             else
@@ -563,6 +589,11 @@ const char *kTemplate =
 #include "kernel_template.inc"
     ;
 
+// hyk_dmath.h as a string (generated at build time from the header).
+const char *kDmath =
+#include "hyk_dmath.inc"
+    ;
+
 }  // namespace
 
 uint32_t count_slots(const Dec &d, uint32_t order) {
@@ -587,10 +618,15 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
       << "\n#define HYK_BLK " << blk << "\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
       << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
       << lit(1.0 / (p - 1.0)) << "\n";
-    if (pin_arith)
+    if (pin_arith) {
         h << "#define HYK_FMA_ACC(a, b, c) ((a) * (b) + (c))\n";
-    else
+        h << "#define HYK_RHO(mp, mq, num) (1.0 / pow((mq) / (num), HYK_INV_PM1) < 1.0 / pow((mp) / (num), HYK_INV_P) "
+             "? 1.0 / pow((mq) / (num), HYK_INV_PM1) : 1.0 / pow((mp) / (num), HYK_INV_P))\n";
+    } else {
         h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
+        h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
+    }
+    h << kDmath << "\n";
     h << kTemplate << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
     g.emit_jets();

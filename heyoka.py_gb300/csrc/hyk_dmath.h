@@ -1,0 +1,239 @@
+/*
+ * hyk_dmath.h - deterministic double-precision elementary functions.
+ *
+ * One source, compiled three ways: into the NVRTC-generated step kernels,
+ * into libhyk's nvcc kernels, and into the CPU oracle.  Every function uses
+ * only IEEE-754 operations that are correctly rounded on both the GPU and
+ * the host (+, -, *, /, sqrt, fused multiply-add) plus bit manipulation, in
+ * a fixed order, so a GPU kernel and the oracle that both use these functions
+ * produce bit-identical results.  The host build must not contract or
+ * reassociate floating-point expressions (-ffp-contract=off, no fast-math);
+ * the device build uses --fmad=false.
+ *
+ * Methods (written for this project from the textbook mathematics):
+ *  exp:  x = k ln2 + r, k = nearest integer to x / ln2 (two-constant
+ *        Cody-Waite reduction, |r| <= ln2/2); e^r by its Taylor series to
+ *        degree 13 (truncation < 5e-18); scaling by 2^k through the exponent bits.
+ *  log:  x = 2^e m with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
+ *        s = (m - 1) / (m + 1), by the odd series to s^23 (|s| <= 0.1716);
+ *        e ln2 added with a two-part ln2.
+ *  sin/cos: x = k pi/2 + r with a three-part pi/2 (accurate for |x| < 2^30),
+ *        Taylor series to r^17 (sine) and r^18 (cosine) on |r| <= pi/4,
+ *        quadrant selection from k mod 4.
+ *  pow with a constant exponent: integer and half-integer exponents by
+ *        products, one square root and one division; other exponents as
+ *        exp(alpha log x).
+ * Accuracy (checked against 300-bit references in the test suite): exp, log,
+ * sin, cos within 2 ulp on their reduced-argument ranges of use.
+ */
+#ifndef HYK_DMATH_H
+#define HYK_DMATH_H
+
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define HYK_DM_FN static __device__ __forceinline__
+#define HYK_DM_FMA(a, b, c) __fma_rn((a), (b), (c))
+#define HYK_DM_SQRT(x) __dsqrt_rn(x)
+#define HYK_DM_BITS(x) ((unsigned long long)__double_as_longlong(x))
+#define HYK_DM_FROM(u) __longlong_as_double((long long)(u))
+#else
+#include <cmath>
+#include <cstring>
+#define HYK_DM_FN static inline
+#define HYK_DM_FMA(a, b, c) std::fma((a), (b), (c))
+#define HYK_DM_SQRT(x) std::sqrt(x)
+static inline unsigned long long hyk_dm_bits_(double x) {
+    unsigned long long u;
+    std::memcpy(&u, &x, sizeof u);
+    return u;
+}
+static inline double hyk_dm_from_(unsigned long long u) {
+    double x;
+    std::memcpy(&x, &u, sizeof x);
+    return x;
+}
+#define HYK_DM_BITS(x) hyk_dm_bits_(x)
+#define HYK_DM_FROM(u) hyk_dm_from_(u)
+#endif
+
+#define HYK_DM_NAN HYK_DM_FROM(0x7ff8000000000000ULL)
+#define HYK_DM_INF HYK_DM_FROM(0x7ff0000000000000ULL)
+/* 1.5 * 2^52: adding it rounds a double of magnitude < 2^51 to an integer
+ * held in the low mantissa bits. */
+#define HYK_DM_RND 6755399441055744.0
+
+HYK_DM_FN int hyk_dm_isnan(double x) { return (HYK_DM_BITS(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL; }
+
+/* 2^k for integer k in [-1022, 1023]. */
+HYK_DM_FN double hyk_dm_pow2i(int k) { return HYK_DM_FROM((unsigned long long)(long long)(k + 1023) << 52); }
+
+HYK_DM_FN double hyk_dm_exp(double x) {
+    if (hyk_dm_isnan(x)) return x;
+    if (x > 709.782712893384) return HYK_DM_INF;
+    if (x < -745.1332191019412) return 0.0;
+    const double t = HYK_DM_FMA(x, 1.4426950408889634, HYK_DM_RND);
+    const double kd = t - HYK_DM_RND;
+    const int k = (int)((long long)(HYK_DM_BITS(t) << 32) >> 32); /* low 32 bits, signed */
+    double r = HYK_DM_FMA(-kd, 0.6931471805599453, x);
+    r = HYK_DM_FMA(-kd, 2.3190468138462996e-17, r);
+    double p = 1.6059043836821613e-10;  // 1/13!
+    p = HYK_DM_FMA(p, r, 2.08767569878681e-09);
+    p = HYK_DM_FMA(p, r, 2.505210838544172e-08);
+    p = HYK_DM_FMA(p, r, 2.755731922398589e-07);
+    p = HYK_DM_FMA(p, r, 2.7557319223985893e-06);
+    p = HYK_DM_FMA(p, r, 2.48015873015873e-05);
+    p = HYK_DM_FMA(p, r, 0.0001984126984126984);
+    p = HYK_DM_FMA(p, r, 0.001388888888888889);
+    p = HYK_DM_FMA(p, r, 0.008333333333333333);
+    p = HYK_DM_FMA(p, r, 0.041666666666666664);
+    p = HYK_DM_FMA(p, r, 0.16666666666666666);
+    p = HYK_DM_FMA(p, r, 0.5);
+    p = HYK_DM_FMA(p, r, 1.0);
+    p = HYK_DM_FMA(p, r, 1.0);
+    if (k >= -1022 && k <= 1023) return p * hyk_dm_pow2i(k);
+    /* Results near the overflow or underflow limits: scale in two factors. */
+    const int k1 = k / 2, k2 = k - k1;
+    return (p * hyk_dm_pow2i(k1)) * hyk_dm_pow2i(k2);
+}
+
+HYK_DM_FN double hyk_dm_log(double x) {
+    unsigned long long u = HYK_DM_BITS(x);
+    if (hyk_dm_isnan(x)) return x;
+    if (u >> 63) return (u << 1) == 0 ? -HYK_DM_INF : HYK_DM_NAN; /* -0 or negative */
+    if (u == 0) return -HYK_DM_INF;
+    if (u == 0x7ff0000000000000ULL) return x;
+    int e = 0;
+    if ((u >> 52) == 0) { /* subnormal: scale by 2^54 */
+        x = x * 18014398509481984.0;
+        u = HYK_DM_BITS(x);
+        e = -54;
+    }
+    e += (int)(u >> 52) - 1023;
+    double m = HYK_DM_FROM((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL); /* [1, 2) */
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        e += 1;
+    }
+    const double f = m - 1.0; /* exact */
+    const double s = f / (2.0 + f);
+    const double t = s * s;
+    double q = 0.043478260869565216;  // 1/23
+    q = HYK_DM_FMA(q, t, 0.047619047619047616);
+    q = HYK_DM_FMA(q, t, 0.05263157894736842);
+    q = HYK_DM_FMA(q, t, 0.058823529411764705);
+    q = HYK_DM_FMA(q, t, 0.06666666666666667);
+    q = HYK_DM_FMA(q, t, 0.07692307692307693);
+    q = HYK_DM_FMA(q, t, 0.09090909090909091);
+    q = HYK_DM_FMA(q, t, 0.1111111111111111);
+    q = HYK_DM_FMA(q, t, 0.14285714285714285);
+    q = HYK_DM_FMA(q, t, 0.2);
+    q = HYK_DM_FMA(q, t, 0.3333333333333333);
+    const double a = s + s;
+    const double lm = HYK_DM_FMA(a * t, q, a); /* 2 atanh(s) */
+    const double ed = (double)e;
+    return HYK_DM_FMA(ed, 0.6931471805599453, HYK_DM_FMA(ed, 2.3190468138462996e-17, lm));
+}
+
+/* sin and cos of x together. */
+HYK_DM_FN void hyk_dm_sincos(double x, double *sp, double *cp) {
+    const unsigned long long u = HYK_DM_BITS(x);
+    if ((u & 0x7ff0000000000000ULL) == 0x7ff0000000000000ULL) { /* inf or nan */
+        *sp = HYK_DM_NAN;
+        *cp = HYK_DM_NAN;
+        return;
+    }
+    const double t = HYK_DM_FMA(x, 0.6366197723675814, HYK_DM_RND);
+    const double kd = t - HYK_DM_RND;
+    const unsigned q = (unsigned)(HYK_DM_BITS(t) & 3ULL);
+    double r = HYK_DM_FMA(-kd, 1.5707963267948966, x);
+    r = HYK_DM_FMA(-kd, 6.123233995736766e-17, r);
+    r = HYK_DM_FMA(-kd, -1.4973849048591698e-33, r);
+    const double z = r * r;
+    double ps = 2.8114572543455206e-15;  // 1/17!
+    ps = HYK_DM_FMA(ps, z, -7.647163731819816e-13);
+    ps = HYK_DM_FMA(ps, z, 1.6059043836821613e-10);
+    ps = HYK_DM_FMA(ps, z, -2.505210838544172e-08);
+    ps = HYK_DM_FMA(ps, z, 2.7557319223985893e-06);
+    ps = HYK_DM_FMA(ps, z, -0.0001984126984126984);
+    ps = HYK_DM_FMA(ps, z, 0.008333333333333333);
+    ps = HYK_DM_FMA(ps, z, -0.16666666666666666);
+    const double s = HYK_DM_FMA(r * z, ps, r);
+    double pc = -1.5619206968586225e-16;  // -1/18!
+    pc = HYK_DM_FMA(pc, z, 4.779477332387385e-14);
+    pc = HYK_DM_FMA(pc, z, -1.1470745597729725e-11);
+    pc = HYK_DM_FMA(pc, z, 2.08767569878681e-09);
+    pc = HYK_DM_FMA(pc, z, -2.755731922398589e-07);
+    pc = HYK_DM_FMA(pc, z, 2.48015873015873e-05);
+    pc = HYK_DM_FMA(pc, z, -0.001388888888888889);
+    pc = HYK_DM_FMA(pc, z, 0.041666666666666664);
+    pc = HYK_DM_FMA(pc, z, -0.5);
+    const double c = HYK_DM_FMA(z, pc, 1.0);
+    switch (q) {
+    case 0:
+        *sp = s;
+        *cp = c;
+        break;
+    case 1:
+        *sp = c;
+        *cp = -s;
+        break;
+    case 2:
+        *sp = -s;
+        *cp = -c;
+        break;
+    default:
+        *sp = -c;
+        *cp = s;
+        break;
+    }
+}
+
+/* x^n for a non-negative integer n by binary powering (fixed product order). */
+HYK_DM_FN double hyk_dm_powi(double x, unsigned n) {
+    double r = 1.0, b = x;
+    bool first = true;
+    while (n) {
+        if (n & 1u) {
+            r = first ? b : r * b;
+            first = false;
+        }
+        n >>= 1;
+        if (n) b = b * b;
+    }
+    return r;
+}
+
+/* x^alpha for a constant alpha. */
+HYK_DM_FN double hyk_dm_pow(double x, double alpha) {
+    const double a2 = alpha + alpha;
+    const bool integral = alpha <= 64.0 && alpha >= -64.0 && alpha == (double)(long long)alpha;
+    const bool half = !integral && a2 <= 129.0 && a2 >= -129.0 && a2 == (double)(long long)a2;
+    if (integral) {
+        const long long n = (long long)alpha;
+        if (n >= 0) return hyk_dm_powi(x, (unsigned)n);
+        return 1.0 / hyk_dm_powi(x, (unsigned)(-n));
+    }
+    if (half) {
+        const long long n2 = (long long)a2; /* odd */
+        const double sq = HYK_DM_SQRT(x);
+        if (n2 > 0) {
+            const unsigned m = (unsigned)((n2 - 1) / 2);
+            return m == 0 ? sq : hyk_dm_powi(x, m) * sq;
+        }
+        const unsigned m = (unsigned)((-n2 - 1) / 2);
+        return 1.0 / (m == 0 ? sq : hyk_dm_powi(x, m) * sq);
+    }
+    if (x < 0.0) return HYK_DM_NAN;
+    if (x == 0.0) return alpha > 0.0 ? 0.0 : HYK_DM_INF;
+    return hyk_dm_exp(alpha * hyk_dm_log(x));
+}
+
+/* Jorba-Zou rho from the infinity norms: min over o in {p-1, p} of
+ * (num / m_o)^(1/o), evaluated as exp(-max(log(m_o / num) / o)). */
+HYK_DM_FN double hyk_dm_rho(double m_p, double m_pm1, double num, double inv_p, double inv_pm1) {
+    const double e1 = hyk_dm_log(m_p / num) * inv_p;
+    const double e2 = hyk_dm_log(m_pm1 / num) * inv_pm1;
+    const double e = e2 > e1 ? e2 : e1;
+    return hyk_dm_exp(-e);
+}
+
+#endif /* HYK_DMATH_H */

@@ -8,6 +8,8 @@
 #include <cstdint>
 #include <cstdio>
 
+#include "hyk_dmath.h"
+
 namespace {
 
 // out[i][l] = sum_n tc[i][n][l] dt[l]^n, Horner with fused multiply-adds (the
@@ -35,6 +37,21 @@ __global__ void count_finished_kernel(const uint32_t *__restrict__ status, uint6
 
 __global__ void zero_u32(uint32_t *p) { *p = 0; }
 
+__global__ void dmath_kernel(int fn, const double *__restrict__ x, const double *__restrict__ a, double *__restrict__ out,
+                             uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s, c;
+    switch (fn) {
+    case 0: out[i] = hyk_dm_exp(x[i]); break;
+    case 1: out[i] = hyk_dm_log(x[i]); break;
+    case 2: hyk_dm_sincos(x[i], &s, &c); out[i] = s; break;
+    case 3: hyk_dm_sincos(x[i], &s, &c); out[i] = c; break;
+    case 4: out[i] = hyk_dm_pow(x[i], a[i]); break;
+    default: out[i] = hyk_dm_rho(x[i], a[i], 1.0, 1.0 / 20, 1.0 / 19); break;
+    }
+}
+
 // FP64 FMA throughput: each thread runs 8 independent dependency chains of
 // `iters` fused multiply-adds.  The values stay bounded (a*x + b with a < 1).
 __global__ void fp64_fma_kernel(double *sink, uint64_t iters, double a, double b) {
@@ -61,6 +78,12 @@ extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t 
     const unsigned blk = 128;
     const uint64_t grid = (n_lanes + blk - 1) / blk;
     dense_eval_kernel<<<(unsigned)grid, blk, 0, (cudaStream_t)stream>>>(tc, n_eq, order, n_lanes, ld, dt, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream) {
+    if (n == 0) return 0;
+    dmath_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(fn, x, a, out, n);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 

@@ -33,6 +33,7 @@ extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t 
                                       const double *dt, double *out, void *stream);
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
+extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
 
 namespace {
 
@@ -121,6 +122,7 @@ struct KParams {
     uint64_t iters_per_launch;
     uint64_t *queue;
     uint32_t *finished;
+    const uint64_t *lane_order;
     int persistent;
 };
 
@@ -435,6 +437,7 @@ static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const 
     k.last_h = p->last_h;
     k.last_tc = p->last_tc;
     k.status = p->status;
+    k.lane_order = p->lane_order;
     (void)m;
     return 0;
 }
@@ -530,6 +533,10 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err)) return fail(HYK_ERR_INVALID, err);
     if (n_slot) *n_slot = g.n_slot;
     if (flops) *flops = g.flops;
+    if (verbose == 2) {  // source only, no compilation
+        if (log && log_len) std::snprintf(log, log_len, "%s", g.src.c_str());
+        return 0;
+    }
     if (verbose) setenv("HYK_PTXAS_VERBOSE", "1", 1);
     std::string cubin, lg;
     const int rc = compile_nvrtc(g.src, "hyk_check.cu", cubin, lg);
@@ -538,6 +545,13 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         std::snprintf(log, log_len, "%s", lg.c_str());
     }
     return rc;
+}
+
+int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream) {
+    if (fn < 0 || fn > 5) return fail(HYK_ERR_INVALID, "unknown function index");
+    if (n && (!x || !out || ((fn == 4 || fn == 5) && !a))) return fail(HYK_ERR_INVALID, "null argument");
+    if (hyk_generic_dmath(fn, x, a, out, n, stream)) return fail(HYK_ERR_CUDA, "dmath kernel launch failed");
+    return 0;
 }
 
 int hyk_fp64_peak(int device, double millis, double *flops_per_s) {

@@ -12,6 +12,14 @@ from .decompose import taylor_decompose, order_from_tol  # noqa: F401
 from . import model, workloads  # noqa: F401
 from .integrator import taylor_adaptive_batch, taylor_outcome  # noqa: F401
 from .c_output import continuous_output_batch  # noqa: F401
+from .ensemble import (  # noqa: F401
+    ensemble_propagate_for,
+    ensemble_propagate_for_batch,
+    ensemble_propagate_grid,
+    ensemble_propagate_grid_batch,
+    ensemble_propagate_until,
+    ensemble_propagate_until_batch,
+)
 
 
 def recommended_simd_size(fp_type=float):

@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["hyk_generic.cu", "hyk_runtime.cpp", "hyk_codegen.cpp"]
-DEPS = SOURCES + ["kernel_template.inc", "hyk_internal.hpp"]
+DEPS = SOURCES + ["kernel_template.inc", "hyk_internal.hpp", "hyk_dmath.h"]
 
 
 def _stale() -> bool:
@@ -43,7 +43,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     obj_dir = os.path.join(LIB_DIR, "obj")
     os.makedirs(obj_dir, exist_ok=True)
-    common = [NVCC, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC] + GENCODE
+    # The deterministic math header is also compiled into every generated
+    # module: embed its text as a C++ raw string.
+    with open(os.path.join(CSRC, "hyk_dmath.h")) as f:
+        dm = f.read()
+    with open(os.path.join(obj_dir, "hyk_dmath.inc"), "w") as f:
+        f.write('R"HYKDM(' + dm + ')HYKDM"\n')
+    # --fmad=false: device arithmetic exactly as written (no contraction), so
+    # the shared math gives the same bits as the host build of the oracle.
+    common = [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+    common += ["-I", obj_dir]
+    common += GENCODE
 
     def compile_one(src):
         obj = os.path.join(obj_dir, src + ".o")

@@ -95,6 +95,7 @@ class hyk_prop_t(ctypes.Structure):
         ("last_h", c_vp),
         ("last_tc", c_vp),
         ("status", c_vp),
+        ("lane_order", c_vp),
     ]
 
 
@@ -113,6 +114,7 @@ SIGNATURES = {
     ),
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
+    "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),
     "hyk_codegen_check": (
         c_int,
         [P(hyk_decomp_t), c_u32, P(hyk_config_t), c_int, ctypes.c_char_p, ctypes.c_size_t, P(c_u32), P(c_d)],

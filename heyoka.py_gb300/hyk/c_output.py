@@ -38,7 +38,7 @@ def _dsub_hi(ah, bh, bl):
 
 
 class continuous_output_batch:
-    def __init__(self, tcs, t_hi, t_lo, order):
+    def __init__(self, tcs, t_hi, t_lo, order, n_iter=None):
         self._tcs = tcs.contiguous()
         self._thi = t_hi.contiguous()
         self._tlo = t_lo.contiguous()
@@ -47,6 +47,7 @@ class continuous_output_batch:
         self._B = t_hi.shape[1]
         self._dim = tcs.shape[1]
         self._out = None
+        self._nit = n_iter
         n = self._tcs.shape[0]
         if n:
             # Search keys: start times of the steps, sign-normalised per lane
@@ -111,6 +112,9 @@ class continuous_output_batch:
             raise ValueError("Cannot use a default-constructed continuous_output_batch object")
         if isinstance(tm, torch.Tensor):
             t = tm.to(device=self._dev, dtype=torch.float64)
+        elif np.ndim(tm) == 0:
+            # a scalar time applies to every lane (heyoka/taylor_expose_c_output.cpp:272-296)
+            t = torch.full((self._B,), float(tm), dtype=torch.float64, device=self._dev)
         else:
             a = np.asarray(tm)
             if a.dtype != np.float64:
@@ -141,6 +145,18 @@ class continuous_output_batch:
         a = res.cpu().numpy()
         a.flags.writeable = False
         return a
+
+    def lanes(self, sl):
+        """The continuous output of a contiguous subset of lanes (one batch of
+        an ensemble), trimmed to that subset's own number of iterations."""
+        if self._nit is None:
+            k = self.n_steps
+        else:
+            k = int(self._nit[sl].max().item()) if self._nit[sl].numel() else 0
+        return continuous_output_batch(
+            self._tcs[:k, :, :, sl].contiguous(), self._thi[: k + 1, sl].contiguous(),
+            self._tlo[: k + 1, sl].contiguous(), self._order, None if self._nit is None else self._nit[sl],
+        )
 
     def __copy__(self):
         return continuous_output_batch(self._tcs.clone(), self._thi.clone(), self._tlo.clone(), self._order)

@@ -1,0 +1,183 @@
+"""Ensemble propagations: ``ensemble_propagate_{until,for,grid}[_batch]``.
+
+Same signatures, argument validation and return values as the reference
+(heyoka/__init__.py:251-336, heyoka/_ensemble_impl.py:23-138): the generator
+``gen(ta_copy, i)`` prepares iteration i from a copy of the template
+integrator, and the result is a list with one ``(ta_i, ...)`` tuple per
+iteration, exactly what the reference's thread or process pools return.
+
+On the GPU the iterations are not separate tasks: the copies handed to the
+generator are host-side (their tensors live on the CPU, so the generator only
+sets state, parameters and time), then every iteration's lanes are
+concatenated into one device batch, propagated by a single persistent kernel
+launch and split back into per-iteration integrators.  The batch rules that
+couple the lanes of one reference integrator (step limit for the whole batch,
+last step of lanes that finished early) are applied per iteration.
+``algorithm`` and ``max_workers`` are accepted for compatibility and do not
+change the computation; ``chunksize`` is accepted with ``algorithm="process"``
+only, as in the reference.
+"""
+
+from __future__ import annotations
+
+from collections.abc import Iterable
+
+import numpy as np
+import torch
+
+from .integrator import taylor_adaptive_batch
+
+
+def _host_copy(ta):
+    new = object.__new__(type(ta))
+    for k, v in ta.__dict__.items():
+        if isinstance(v, torch.Tensor):
+            new.__dict__[k] = v.detach().to("cpu", copy=True)
+        elif k in ("_prop", "_step_res", "_final_tc_mask", "_launch_events"):
+            new.__dict__[k] = None
+        else:
+            new.__dict__[k] = v
+    new.__dict__["_tdev"] = torch.device("cpu")
+    return new
+
+
+def _validate(tp, arg, n_iter, kwargs):
+    if not isinstance(n_iter, int):
+        raise TypeError(
+            "The n_iter parameter must be an integer, but an object of type {} was provided instead".format(
+                type(n_iter)
+            )
+        )
+    if n_iter < 0:
+        raise ValueError("The n_iter parameter must be non-negative, but it is {} instead".format(n_iter))
+    if tp in ("until", "for"):
+        if isinstance(arg, Iterable):
+            raise TypeError(
+                "Cannot perform an ensemble propagate_until/for(): the final epoch/time interval must be a "
+                "scalar, not an iterable object"
+            )
+    else:
+        arg = np.array(arg)
+        if arg.ndim != 1:
+            raise ValueError(
+                "Cannot perform an ensemble propagate_grid(): the input time grid must be one-dimensional, "
+                "but instead it has {} dimensions".format(arg.ndim)
+            )
+    if "max_delta_t" in kwargs and isinstance(kwargs["max_delta_t"], Iterable):
+        raise TypeError(
+            'Cannot perform an ensemble propagate_until/for/grid(): the "max_delta_t" argument must be a '
+            "scalar, not an iterable object"
+        )
+    algo = kwargs.pop("algorithm", "thread")
+    if algo not in ("thread", "process"):
+        raise ValueError(
+            "The parallelisation algorithm must be one of {}, but '{}' was provided instead".format(
+                ["thread", "process"], algo
+            )
+        )
+    kwargs.pop("max_workers", None)
+    if algo == "process":
+        kwargs.pop("chunksize", None)
+    return arg
+
+
+def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
+    if not isinstance(ta, taylor_adaptive_batch):
+        raise TypeError("the GPU ensemble propagation needs a hyk.taylor_adaptive_batch template integrator")
+    arg = _validate(tp, arg, n_iter, kwargs)
+    allowed = {"max_steps", "max_delta_t", "callback", "write_tc", "c_output"}
+    if tp == "grid":
+        allowed = {"max_steps", "max_delta_t", "callback"}
+    for k in kwargs:
+        if k not in allowed:
+            raise TypeError("propagate_{}() got an unexpected keyword argument '{}'".format(tp, k))
+    if kwargs.get("callback") is not None:
+        raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
+    if n_iter == 0:
+        return []
+    B = ta.batch_size
+    copies = [gen(_host_copy(ta), i) for i in range(n_iter)]
+    for c in copies:
+        if not isinstance(c, taylor_adaptive_batch) or c.batch_size != B or c._dec is not ta._dec:
+            raise TypeError("the ensemble generator must return the integrator it was given")
+    dev = ta._tdev
+    # One device batch over all iterations.
+    big = object.__new__(type(ta))
+    big.__dict__.update(ta.__dict__)
+    big._B = n_iter * B
+    cat = lambda name: torch.cat([getattr(c, name).to(dev) for c in copies], dim=-1).contiguous()  # noqa: E731
+    big._state = cat("_state")
+    big._pars = cat("_pars")
+    big._thi = cat("_thi")
+    big._tlo = cat("_tlo")
+    big._last_h = cat("_last_h")
+    big._tc = cat("_tc")
+    big._d_out = cat("_d_out")
+    big._step_res = None
+    big._prop = None
+    big._final_tc_mask = None
+    big._launch_events = None
+    md = kwargs.get("max_delta_t", [])
+    md = big._check_prop_args(md, None)
+    ms = int(kwargs.get("max_steps", 0))
+    if tp == "grid":
+        g = torch.tensor(np.repeat(arg.astype(np.float64), n_iter * B).reshape(-1, n_iter * B), device=dev)
+        if not bool((g[0] == big._thi).all()):
+            raise ValueError(
+                "When invoking propagate_grid(), the first element of the time grid "
+                "must match the current time coordinate"
+            )
+        res = big._run(g[-1].contiguous(), None, ms, md, grid=g, group=B)
+    else:
+        tt = torch.full((n_iter * B,), float(arg), dtype=torch.float64, device=dev)
+        if tp == "until":
+            tf_hi, tf_lo = tt, None
+        else:
+            from .integrator import _dadd
+
+            tf_hi, tf_lo = _dadd(big._thi, big._tlo, tt, torch.zeros_like(tt))
+        res = big._run(tf_hi, tf_lo, ms, md, write_tc=bool(kwargs.get("write_tc", False)),
+                       c_output=bool(kwargs.get("c_output", False)), group=B)
+    big._refresh_final_tc()
+    out = []
+    for i, c in enumerate(copies):
+        sl = slice(i * B, (i + 1) * B)
+        ti = object.__new__(type(ta))
+        ti.__dict__.update(c.__dict__)
+        ti._tdev = dev
+        ti._state = big._state[:, sl].contiguous()
+        ti._pars = big._pars[:, sl].contiguous()
+        ti._thi = big._thi[sl].contiguous()
+        ti._tlo = big._tlo[sl].contiguous()
+        ti._last_h = big._last_h[sl].contiguous()
+        ti._tc = big._tc[:, :, sl].contiguous()
+        ti._d_out = big._d_out[:, sl].contiguous()
+        ti._prop = {k: (None if v is None else v[sl].contiguous()) for k, v in big._prop.items()}
+        ti._step_res = None
+        ti._final_tc_mask = None
+        ti._launch_events = None
+        if tp == "grid":
+            out.append((ti, None, res["grid_out"][:, :, sl].cpu().numpy()))
+        else:
+            c_out = None
+            if "c_output" in res:
+                c_out = res["c_output"].lanes(sl)
+            out.append((ti, c_out, None))
+    return out
+
+
+def ensemble_propagate_until(ta, t, n_iter, gen, **kwargs):
+    return _ensemble("until", ta, t, n_iter, gen, **kwargs)
+
+
+def ensemble_propagate_for(ta, delta_t, n_iter, gen, **kwargs):
+    return _ensemble("for", ta, delta_t, n_iter, gen, **kwargs)
+
+
+def ensemble_propagate_grid(ta, grid, n_iter, gen, **kwargs):
+    return _ensemble("grid", ta, grid, n_iter, gen, **kwargs)
+
+
+ensemble_propagate_until_batch = ensemble_propagate_until
+ensemble_propagate_for_batch = ensemble_propagate_for
+ensemble_propagate_grid_batch = ensemble_propagate_grid

@@ -142,6 +142,7 @@ class taylor_adaptive_batch:
         prop_mode="persistent",
         block_lanes=0,
         pin_arith=False,
+        schedule="lpt",
         **kwargs,
     ):
         for k in list(kwargs):
@@ -160,6 +161,8 @@ class taylor_adaptive_batch:
             raise NotImplementedError("event detection is not supported by the GPU batch integrator")
         if prop_mode not in ("persistent", "plain"):
             raise ValueError("prop_mode must be 'persistent' or 'plain'")
+        if schedule not in ("lpt", "fifo"):
+            raise ValueError("schedule must be 'lpt' or 'fifo'")
         if hasattr(sys, "vargs"):
             raise NotImplementedError("variational systems are not supported by the GPU batch integrator")
 
@@ -218,6 +221,7 @@ class taylor_adaptive_batch:
         self._tdev = torch.device("cuda", self._dev)
         self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith)
         self._prop_mode = prop_mode
+        self._schedule = schedule
         self._compact_mode = bool(compact_mode)
         self._B = B
         f64 = dict(dtype=torch.float64, device=self._tdev)
@@ -231,6 +235,7 @@ class taylor_adaptive_batch:
         self._step_res = None
         self._prop = None  # dict of device arrays of the last propagation
         self._final_tc_mask = None  # lanes whose tc must be the final-state jets
+        self._launch_events = None
 
     # ------------------------------------------------------------------ properties
     @property
@@ -500,7 +505,8 @@ class taylor_adaptive_batch:
         }
         return p
 
-    def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None):
+    def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None,
+             lane_order=None):
         """Initialise and run a propagation of every lane to (tf_hi, tf_lo)."""
         L = _lib.load()
         if max_steps < 0:
@@ -533,19 +539,27 @@ class taylor_adaptive_batch:
                 p["max_h"].data_ptr(), p["n_steps"].data_ptr(), p["n_iter"].data_ptr(),
                 None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
+                None if lane_order is None else lane_order.data_ptr(),
             )
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
         mode = _lib.HYK_MODE_PERSISTENT if self._prop_mode == "persistent" else _lib.HYK_MODE_PLAIN
+        if lane_order is None and mode == _lib.HYK_MODE_PERSISTENT and self._schedule == "lpt" and B >= 4096:
+            lane_order = self._lpt_order(tf_hi, tf_lo)
         with torch.cuda.device(self._dev):
             s = stream_handle(self._dev)
             d = desc()
             _lib.check(L.hyk_prop_init(self._mod.handle, lanes, d, s), "hyk_prop_init")
+            ev = self._launch_events  # optional (start, end) CUDA events around the propagation launch(es)
+            if ev is not None:
+                ev[0].record(torch.cuda.current_stream(self._dev))
             while True:
                 _lib.check(
                     L.hyk_propagate(self._mod.handle, lanes, d, mode, self._mod.ws.data_ptr(), self._mod.ws_bytes, 16, None, s),
                     "hyk_propagate",
                 )
+                if ev is not None:
+                    ev[1].record(torch.cuda.current_stream(self._dev))
                 if not c_output:
                     break
                 full = (p["status"] & _lib.LANE_CAPACITY) != 0
@@ -567,6 +581,27 @@ class taylor_adaptive_batch:
         if c_output:
             res["c_output"] = self._make_c_output(p, tcs, thi, tlo, t0h, t0l)
         return res
+
+    def _lpt_order(self, tf_hi, tf_lo):
+        """Longest-first queue order for the persistent kernel: lanes sorted by
+        the estimated number of steps |t_final - t| / h, h the size of a step
+        from the current state (one extra step evaluation, not applied)."""
+        L = _lib.load()
+        B = self._B
+        st, th, tl = self._state.clone(), self._thi.clone(), self._tlo.clone()
+        oc = torch.empty(B, dtype=torch.int64, device=self._tdev)
+        h = torch.empty(B, dtype=torch.float64, device=self._tdev)
+        with torch.cuda.device(self._dev):
+            _lib.check(
+                L.hyk_step(self._mod.handle, lanes_struct(st, self._pars, th, tl), None, 0, oc.data_ptr(),
+                           h.data_ptr(), None, stream_handle(self._dev)),
+                "hyk_step",
+            )
+        rem = (tf_hi - self._thi).abs()
+        if tf_lo is not None:
+            rem = (rem + tf_lo.abs())
+        est = torch.nan_to_num(rem / h.abs(), nan=0.0, posinf=1e300)
+        return torch.argsort(est, descending=True).contiguous()
 
     def _finish_prop(self, p, group, last_tc):
         """Apply the whole-batch rules that couple the lanes of a batch."""
@@ -609,7 +644,7 @@ class taylor_adaptive_batch:
             out_tcs = torch.where(pad.view(K, 1, 1, B), self._tc.unsqueeze(0), out_tcs)
             out_thi[1:] = torch.where(pad, self._thi.view(1, B), out_thi[1:])
             out_tlo[1:] = torch.where(pad, self._tlo.view(1, B), out_tlo[1:])
-        return continuous_output_batch(out_tcs, out_thi, out_tlo, order)
+        return continuous_output_batch(out_tcs, out_thi, out_tlo, order, nit.clone())
 
     def _check_time(self, t, what):
         tt = self._lane_vec(t, what)

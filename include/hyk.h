@@ -191,6 +191,9 @@ typedef struct hyk_prop {
     double *last_h;      /* h of the last iteration */
     double *last_tc;     /* (n_eq, order+1, ld) Taylor coefficients of the last step, or NULL */
     uint32_t *status;    /* per-lane status bits HYK_LANE_* */
+    /* persistent form only: order in which lanes are taken from the queue
+     * (a permutation of 0..n_lanes-1, e.g. longest-first), or NULL */
+    const uint64_t *lane_order;
 } hyk_prop_t;
 
 #define HYK_LANE_DONE 1u     /* reached the final time */
@@ -223,6 +226,12 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
                    const double *dt, double *out, void *stream);
 
+/* The deterministic elementary functions the kernels use, evaluated on the
+ * device for validation: fn 0 exp, 1 log, 2 sin, 3 cos, 4 pow(x[i], a[i]),
+ * 5 the step-size rho(m_p = x[i], m_pm1 = a[i], num = 1, order 20).
+ * x, a, out are device arrays of n doubles. */
+int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
+
 /* Device FP64 FMA throughput microbenchmark (flop/s, 2 flops per FMA), used
  * as the roofline denominator.  Runs for about `millis` milliseconds; uses a
  * one-double-per-CTA scratch buffer of its own. */
@@ -231,8 +240,9 @@ int hyk_fp64_peak(int device, double millis, double *flops_per_s);
 /* Build check without a GPU: generate the module source for `d` at `order`
  * (block size cfg->block_lanes, default 128) and compile it with NVRTC for
  * sm_103a.  `log` receives the NVRTC log (ptxas register and spill
- * statistics when `verbose`); `n_slot` the shared-memory doubles per lane,
- * `flops` the algorithmic flops per step. */
+ * statistics when `verbose` is 1; the generated source, without compiling,
+ * when `verbose` is 2); `n_slot` the shared-memory doubles per lane, `flops`
+ * the algorithmic flops per step. */
 int hyk_codegen_check(const hyk_decomp_t *d, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
                       size_t log_len, uint32_t *n_slot, double *flops);
 

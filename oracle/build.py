@@ -19,10 +19,11 @@ LIB = os.path.join(OUT_DIR, "libhyk_oracle.so")
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "hyk_oracle.cpp")
     hdr = os.path.join(ROOT, "include", "hyk.h")
+    dm = os.path.join(ROOT, "heyoka.py_gb300", "csrc", "hyk_dmath.h")
     if (
         not force
         and os.path.exists(LIB)
-        and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr))
+        and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr), os.path.getmtime(dm))
     ):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
@@ -37,6 +38,8 @@ def build(force: bool = False) -> str:
         "-shared",
         "-I",
         os.path.join(ROOT, "include"),
+        "-I",
+        os.path.join(ROOT, "heyoka.py_gb300", "csrc"),
         src,
         "-o",
         LIB + ".tmp",

@@ -42,10 +42,11 @@
 //         as a fused multiply-add, divisions by n replaced by multiplication
 //         with the double nearest 1/n, and divisions by an order-0 value b0 at
 //         orders n >= 1 replaced by multiplication with 1/b0 (one division per
-//         step).  This is, operation for operation, what the CUDA kernels
-//         compute (they are compiled with --fmad=false and explicit FMAs), so
-//         GPU and oracle differ only through the libm transcendental
-//         functions (sin, cos, exp, log, pow, sqrt is exact in both).
+//         step), and exp, log, sin, cos, pow and the step-size exponentials
+//         evaluated by the deterministic functions of hyk_dmath.h.  This is,
+//         operation for operation, what the CUDA kernels compute (they are
+//         compiled with --fmad=false, explicit FMAs and the same hyk_dmath.h),
+//         so the GPU and the oracle in this mode agree bit for bit.
 //
 // Precision: double, or binary128 (__float128 on x86-64, long double on
 // aarch64) for the high-precision error reference.
@@ -53,6 +54,7 @@
 // Build: oracle/build.py (g++ -O3 -fopenmp -ffp-contract=off, no -march flags).
 
 #include "hyk.h"
+#include "hyk_dmath.h"  // the deterministic elementary functions of the CUDA kernels
 
 #include <algorithm>
 #include <cmath>
@@ -119,6 +121,38 @@ template <> struct M<qreal> {
 #endif
     static qreal inf() { return (qreal)std::numeric_limits<double>::infinity(); }
     static qreal nan() { return (qreal)std::numeric_limits<double>::quiet_NaN(); }
+};
+
+// Transcendental functions per arithmetic mode: "pin" uses the C library
+// (the reference's arithmetic), "gpu" the deterministic functions shared with
+// the CUDA kernels.  binary128 always uses the quad-precision library.
+template <typename T> struct F {
+    static T exp(T x, int) { return M<T>::exp(x); }
+    static T log(T x, int) { return M<T>::log(x); }
+    static T pow(T x, T a, int) { return M<T>::pow(x, a); }
+    static void sincos(T x, T &s, T &c, int) {
+        s = M<T>::sin(x);
+        c = M<T>::cos(x);
+    }
+    static bool rho(T, T, T, T, T, int, T &) { return false; }
+};
+template <> struct F<double> {
+    static double exp(double x, int m) { return m ? hyk_dm_exp(x) : std::exp(x); }
+    static double log(double x, int m) { return m ? hyk_dm_log(x) : std::log(x); }
+    static double pow(double x, double a, int m) { return m ? hyk_dm_pow(x, a) : std::pow(x, a); }
+    static void sincos(double x, double &s, double &c, int m) {
+        if (m) {
+            hyk_dm_sincos(x, &s, &c);
+        } else {
+            s = std::sin(x);
+            c = std::cos(x);
+        }
+    }
+    static bool rho(double mp, double mq, double num, double ip, double iq, int m, double &out) {
+        if (!m) return false;
+        out = hyk_dm_rho(mp, mq, num, ip, iq);
+        return true;
+    }
 };
 
 // ------------------------------------------------------ double-length time
@@ -218,6 +252,7 @@ template <typename T> struct Batch {
     std::vector<T> numrows;             // constant rows for NUM arguments
     std::vector<int64_t> numrow_of;     // (op*2 + which) -> row index, -1
     std::vector<int64_t> rhs_numrow;    // per rhs
+    std::vector<T> s_acc, s_num, s_tmp, s_den;  // per-lane scratch rows
     T rhofac;
 
     Batch(const Dec &dd, uint32_t order, uint32_t b, int md) : d(dd), p(order), B(b), nu(dd.n_u()), mode(md) {
@@ -232,6 +267,10 @@ template <typename T> struct Batch {
         ones.assign(B, T(1));
         inv.assign(p + 2, T(0));
         for (uint32_t n = 1; n <= p + 1; ++n) inv[n] = T(1) / T(n);
+        s_acc.assign(B, T(0));
+        s_num.assign(B, T(0));
+        s_tmp.assign(B, T(0));
+        s_den.assign(B, T(0));
         numrow_of.assign((size_t)d.n_ops * 2, -1);
         rhs_numrow.assign(d.n_eq, -1);
         auto add_row = [&](double v) {
@@ -331,7 +370,7 @@ template <typename T> struct Batch {
         const uint32_t u = d.n_eq + k;
         T *c = jr(u, n);
         const int64_t ra = numrow_of[2 * k], rb = numrow_of[2 * k + 1];
-        std::vector<T> acc(B);
+        std::vector<T> &acc = s_acc;
         bool first = true;
         switch (o.op) {
         case HYK_OP_ADD:
@@ -369,7 +408,7 @@ template <typename T> struct Batch {
                 break;
             }
             for (uint32_t j = 1; j <= n; ++j) term(acc.data(), row(o.b, rb, j), jr(u, n - j), first);
-            std::vector<T> num(B);
+            std::vector<T> &num = s_num;
             for (uint32_t l = 0; l < B; ++l) {
                 const T av = an ? an[l] : T(0);
                 num[l] = first ? av : av - acc[l];
@@ -400,7 +439,7 @@ template <typename T> struct Batch {
             if (!first)
                 for (uint32_t l = 0; l < B; ++l) acc[l] = acc[l] + acc[l];
             if (n % 2 == 0) term(acc.data(), jr(u, n / 2), jr(u, n / 2), first);
-            std::vector<T> num(B), den(B);
+            std::vector<T> &num = s_num, &den = s_den;
             const T *c0 = jr(u, 0);
             for (uint32_t l = 0; l < B; ++l) {
                 const T av = an ? an[l] : T(0);
@@ -416,13 +455,13 @@ template <typename T> struct Batch {
             if (n == 0) {
                 T *iv = &I0[(size_t)u * B];
                 for (uint32_t l = 0; l < B; ++l) {
-                    c[l] = M<T>::pow(a0[l], alpha);
+                    c[l] = F<T>::pow(a0[l], alpha, mode);
                     iv[l] = T(1) / a0[l];
                 }
                 break;
             }
             // c_n = (1/(n a_0)) sum_{j=0}^{n-1} (n*alpha - j*(alpha+1)) a_{n-j} c_j
-            std::vector<T> tmp(B);
+            std::vector<T> &tmp = s_tmp;
             for (uint32_t j = 0; j < n; ++j) {
                 const T *an_j = row(o.a, ra, n - j);
                 if (!an_j) continue;
@@ -435,7 +474,7 @@ template <typename T> struct Batch {
                 break;
             }
             if (mode) {
-                std::vector<T> t2(B);
+                std::vector<T> &t2 = s_num;
                 divn(t2.data(), acc.data(), n);
                 div0(c, t2.data(), a0, u);
             } else {
@@ -447,7 +486,7 @@ template <typename T> struct Batch {
         case HYK_OP_EXP: {
             if (n == 0) {
                 const T *a0 = row(o.a, ra, 0);
-                for (uint32_t l = 0; l < B; ++l) c[l] = M<T>::exp(a0[l]);
+                for (uint32_t l = 0; l < B; ++l) c[l] = F<T>::exp(a0[l], mode);
                 break;
             }
             for (uint32_t j = 1; j <= n; ++j) term(acc.data(), karow(o.a, j), jr(u, n - j), first);
@@ -463,14 +502,14 @@ template <typename T> struct Batch {
             if (n == 0) {
                 T *iv = &I0[(size_t)u * B];
                 for (uint32_t l = 0; l < B; ++l) {
-                    c[l] = M<T>::log(a0[l]);
+                    c[l] = F<T>::log(a0[l], mode);
                     iv[l] = T(1) / a0[l];
                 }
                 break;
             }
             // l_n = (a_n - (1/n) sum_{j=1}^{n-1} (j l_j) a_{n-j}) / a_0
             for (uint32_t j = 1; j < n; ++j) term(acc.data(), kr(u, j), row(o.a, ra, n - j), first);
-            std::vector<T> num(B);
+            std::vector<T> &num = s_num;
             if (!first) divn(acc.data(), acc.data(), n);
             for (uint32_t l = 0; l < B; ++l) {
                 const T av = an ? an[l] : T(0);
@@ -484,7 +523,11 @@ template <typename T> struct Batch {
             const uint32_t partner = (uint32_t)o.aux;
             if (n == 0) {
                 const T *a0 = row(o.a, ra, 0);
-                for (uint32_t l = 0; l < B; ++l) c[l] = o.op == HYK_OP_SIN ? M<T>::sin(a0[l]) : M<T>::cos(a0[l]);
+                for (uint32_t l = 0; l < B; ++l) {
+                    T sv, cv;
+                    F<T>::sincos(a0[l], sv, cv, mode);
+                    c[l] = o.op == HYK_OP_SIN ? sv : cv;
+                }
                 break;
             }
             // s_n = (1/n) sum_{j=1}^n j a_j c_{n-j};  c_n = -(1/n) sum_{j=1}^n j a_j s_{n-j}
@@ -520,9 +563,11 @@ template <typename T> struct Batch {
         for (uint32_t i = 0; i < d.n_eq; ++i) std::memcpy(jr(i, 0), &state[(size_t)i * B], sizeof(T) * B);
         // sin/cos pairs: the partner of a u-variable at order n must exist
         // before it is used at order n+1 only, so plain decomposition order works.
-        for (uint32_t n = 0; n <= p; ++n) {
+        // Intermediate u-variables are needed up to order p-1 only (the
+        // state's order p comes from the right-hand sides at order p-1).
+        for (uint32_t n = 0; n < p; ++n) {
             for (uint32_t k = 0; k < d.n_ops; ++k) op_coef(k, n);
-            if (n < p) state_next(n);
+            state_next(n);
         }
     }
 
@@ -539,9 +584,12 @@ template <typename T> struct Batch {
                 if (!(apm1 <= mpm1)) mpm1 = apm1;
             }
             const T num = ms < T(1) ? T(1) : ms;
-            const T rho_o = T(1) / M<T>::pow(mp / num, T(1) / T(p));
-            const T rho_om1 = T(1) / M<T>::pow(mpm1 / num, T(1) / T(p - 1));
-            const T rho_m = rho_om1 < rho_o ? rho_om1 : rho_o;
+            T rho_m;
+            if (!F<T>::rho(mp, mpm1, num, inv[p], inv[p - 1], mode, rho_m)) {
+                const T rho_o = T(1) / M<T>::pow(mp / num, T(1) / T(p));
+                const T rho_om1 = T(1) / M<T>::pow(mpm1 / num, T(1) / T(p - 1));
+                rho_m = rho_om1 < rho_o ? rho_om1 : rho_o;
+            }
             h[l] = rho_m * rhofac;
         }
     }
@@ -824,6 +872,22 @@ int hyko_propagate(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, u
 }
 
 void hyko_free(void *p) { std::free(p); }
+
+// Evaluate one of the deterministic elementary functions on the host:
+// fn 0 exp, 1 log, 2 sin, 3 cos, 4 pow(x, a[i]), 5 rho(x, a, num=1, 1/20, 1/19).
+void hyko_dm_eval(int fn, const double *x, const double *a, double *out, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) {
+        double s, c;
+        switch (fn) {
+        case 0: out[i] = hyk_dm_exp(x[i]); break;
+        case 1: out[i] = hyk_dm_log(x[i]); break;
+        case 2: hyk_dm_sincos(x[i], &s, &c); out[i] = s; break;
+        case 3: hyk_dm_sincos(x[i], &s, &c); out[i] = c; break;
+        case 4: out[i] = hyk_dm_pow(x[i], a[i]); break;
+        default: out[i] = hyk_dm_rho(x[i], a[i], 1.0, 1.0 / 20, 1.0 / 19); break;
+        }
+    }
+}
 
 // Ensemble propagate_until over n_lanes lanes split into batches of B lanes
 // (the reference's ensemble of batch integrators, heyoka/_ensemble_impl.py:23-68),

@@ -1,0 +1,117 @@
+"""Ensemble propagations against serial propagations, as the reference tests
+them (heyoka/_test_ensemble.py:13-178): bit-identical states, times,
+propagate_res, grid output and continuous output."""
+
+import numpy as np
+import pytest
+import torch
+
+import hyk
+
+pytestmark = pytest.mark.gpu
+
+
+def pend():
+    x, v = hyk.make_vars("x", "v")
+    return [(x, v), (v, -9.8 * hyk.sin(x))]
+
+
+@pytest.fixture(scope="module")
+def setup(libhyk):
+    assert torch.cuda.is_available()
+    ta = hyk.taylor_adaptive_batch(pend(), [[0.0] * 4] * 2)
+    ics = np.zeros((10, 2, 4))
+    for i in range(10):
+        ics[i, 0] = [0.05 + i / 100, 0.051 + i / 100, 0.052 + i / 100, 0.053 + i / 100.0]
+        ics[i, 1] = [0.025 + i / 100, 0.026 + i / 100, 0.027 + i / 100, 0.028 + i / 100.0]
+    return ta, ics
+
+
+@pytest.mark.parametrize("algo", ["thread", "process"])
+def test_until_and_for(setup, algo):
+    ta, ics = setup
+
+    def gen(t, idx):
+        t.set_time(0.0)
+        t.state[:] = ics[idx]
+        return t
+
+    kw = {"max_workers": 8} if algo == "thread" else {"max_workers": 8, "chunksize": 3}
+    ret = hyk.ensemble_propagate_until_batch(ta, 20.0, 10, gen, algorithm=algo, **kw)
+    assert len(ret) == 10
+    for i in range(10):
+        ta.set_time(0.0)
+        ta.state[:] = ics[i]
+        ta.propagate_until(20.0)
+        assert np.all(ret[i][0].time == 20.0)
+        assert np.all(ta.state == ret[i][0].state)
+        assert ret[i][1] is None
+        assert ta.propagate_res == ret[i][0].propagate_res
+
+    ret = hyk.ensemble_propagate_until_batch(ta, 20.0, 10, gen, algorithm=algo, c_output=True, **kw)
+    for i in range(10):
+        ta.set_time(0.0)
+        ta.state[:] = ics[i]
+        loc = ta.propagate_until(20.0, c_output=True)
+        assert np.all(ta.state == ret[i][0].state)
+        assert ret[i][1] is not None
+        assert np.all(loc[0](5.0) == ret[i][1](5.0))
+
+    def gen10(t, idx):
+        t.set_time(10.0)
+        t.state[:] = ics[idx]
+        return t
+
+    ret = hyk.ensemble_propagate_for_batch(ta, 20.0, 10, gen10, algorithm=algo, **kw)
+    for i in range(10):
+        ta.set_time(10.0)
+        ta.state[:] = ics[i]
+        ta.propagate_for(20.0)
+        assert np.all(ret[i][0].time == 30.0)
+        assert np.all(ta.state == ret[i][0].state)
+        assert ta.propagate_res == ret[i][0].propagate_res
+
+
+def test_grid(setup):
+    ta, ics = setup
+    grid = np.linspace(0.0, 20.0, 80)
+    splat = np.repeat(grid, 4).reshape(-1, 4)
+
+    def gen(t, idx):
+        t.set_time(0.0)
+        t.state[:] = ics[idx]
+        return t
+
+    ret = hyk.ensemble_propagate_grid_batch(ta, grid, 10, gen)
+    for i in range(10):
+        ta.set_time(0.0)
+        ta.state[:] = ics[i]
+        loc = ta.propagate_grid(splat)
+        assert np.all(loc[1] == ret[i][2])
+        assert np.all(ta.state == ret[i][0].state)
+        assert ta.propagate_res == ret[i][0].propagate_res
+
+
+def test_errors(setup):
+    ta, _ = setup
+
+    def gen(t, idx):
+        return t
+
+    with pytest.raises(TypeError, match="The n_iter parameter must be an integer"):
+        hyk.ensemble_propagate_until(ta, 20.0, "a", gen)
+    with pytest.raises(ValueError, match="The n_iter parameter must be non-negative"):
+        hyk.ensemble_propagate_until(ta, 20.0, -1, gen)
+    with pytest.raises(TypeError, match="must be a scalar, not an iterable object"):
+        hyk.ensemble_propagate_until(ta, [20.0], 10, gen)
+    with pytest.raises(TypeError, match="must be a scalar, not an iterable object"):
+        hyk.ensemble_propagate_for(ta, [20.0], 10, gen)
+    with pytest.raises(ValueError, match="one-dimensional, but instead it has 2 dimensions"):
+        hyk.ensemble_propagate_grid(ta, [[20.0, 20.0]], 10, gen)
+    with pytest.raises(TypeError, match='"max_delta_t" argument must be a scalar'):
+        hyk.ensemble_propagate_until(ta, 20.0, 10, gen, max_delta_t=[10])
+    with pytest.raises(TypeError):
+        hyk.ensemble_propagate_until(ta, 20.0, 10, gen, chunksize=1)
+    with pytest.raises(ValueError, match="parallelisation algorithm must be one of"):
+        hyk.ensemble_propagate_until(ta, 20.0, 10, gen, algorithm="foo")
+    assert hyk.ensemble_propagate_until(ta, 20.0, 0, gen) == []

@@ -46,15 +46,18 @@ def test_order_rule(pins):
 def test_scalar_pendulum_steps(oracle, pins, mode):
     p = pins["pendulum"]
     o = oracle.Oracle(pend(), [[0.05], [0.025]], order=20, mode=mode)
+    # pin arithmetic reproduces the reference's step sizes bit for bit; the
+    # gpu arithmetic's own exp/log differ from the C library by at most 2 ulp
+    tol_ulp = 0 if mode == 0 else 2
     oc, h = o.step()
-    assert h[0] == p["first_h"] and oc[0] == hyk.taylor_outcome.success
+    assert ulps(h[0], p["first_h"]) <= tol_ulp and oc[0] == hyk.taylor_outcome.success
     oc, h = o.step(backward=True)
-    assert h[0] == p["back_h"]
+    assert ulps(h[0], p["back_h"]) <= tol_ulp
     oc, h = o.step(0.01)
     assert h[0] == 0.01 and oc[0] == hyk.taylor_outcome.time_limit
     oc, h = o.step(-0.02)
     assert h[0] == -0.02 and oc[0] == hyk.taylor_outcome.time_limit
-    assert o.t_hi[0] == p["after_clamped_steps"]["time"]
+    assert ulps(o.t_hi[0], p["after_clamped_steps"]["time"]) <= 16 * tol_ulp
     assert np.all(np.round(o.state.ravel(), 8) == p["after_clamped_steps"]["state_8digits"])
 
 
@@ -107,7 +110,7 @@ def test_batch_forced_pendulum(oracle, pins, mode):
     q = pins["forced_pendulum_batch"]
     o = oracle.Oracle(forced(), q["state"], pars=q["pars"], order=20, mode=mode)
     oc, h = o.step()
-    assert list(h) == q["step_h"]
+    assert max(ulps(a, b) for a, b in zip(h, q["step_h"])) <= (0 if mode == 0 else 2)
     o.step([0.010, 0.011, 0.012, 0.013])
     assert np.all(np.round(o.state, 8) == q["after_clamped_step"]["state_8digits"])
     assert np.all(np.round(o.t_hi, 8) == q["after_clamped_step"]["time_8digits"])
