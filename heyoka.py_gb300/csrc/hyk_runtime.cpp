@@ -34,6 +34,7 @@ extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t 
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
 extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
+extern "C" int hyk_noalloc_scratch(int device, void **ptr, size_t *bytes, char *err, size_t errlen);
 
 namespace {
 
@@ -510,6 +511,27 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     }
     if (iters) *iters = n;
     return 0;
+}
+
+// Propagation without a caller workspace: the counters hyk_propagate keeps in
+// its workspace come from libhyk's file-scope device scratch array
+// (hyk_noalloc.cu).  Nothing here allocates: the scratch address is looked up
+// once per device, the counters are cleared by hyk_propagate itself at the
+// start of every call, and the rest is hyk_propagate unchanged.
+int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, uint32_t check_every,
+                          uint64_t *iters, void *stream) {
+    if (!m) return fail(HYK_ERR_INVALID, "null module");
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    void *ws = nullptr;
+    size_t cap = 0;
+    char buf[256] = {0};
+    if (hyk_noalloc_scratch(m->device, &ws, &cap, buf, sizeof buf)) return fail(HYK_ERR_CUDA, buf);
+    const size_t need = hyk_propagate_workspace_size(m, lanes ? lanes->n_lanes : 0, mode);
+    if (need > cap)
+        return fail(HYK_ERR_INVALID, "hyk_propagate_noalloc: this propagation needs " + std::to_string(need) +
+                                         " bytes of scratch, more than the " + std::to_string(cap) +
+                                         " bytes the no-allocation entry point holds; use hyk_propagate with a workspace");
+    return hyk_propagate(m, lanes, p, mode, ws, cap, check_every, iters, stream);
 }
 
 int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld, const double *dt,

@@ -25,7 +25,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["hyk_generic.cu", "hyk_runtime.cpp", "hyk_codegen.cpp"]
+SOURCES = ["hyk_generic.cu", "hyk_noalloc.cu", "hyk_runtime.cpp", "hyk_codegen.cpp"]
 DEPS = SOURCES + ["kernel_template.inc", "hyk_internal.hpp", "hyk_dmath.h"]
 
 

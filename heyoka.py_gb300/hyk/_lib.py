@@ -112,6 +112,7 @@ SIGNATURES = {
         c_int,
         [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_vp, ctypes.c_size_t, c_u32, P(c_u64), c_vp],
     ),
+    "hyk_propagate_noalloc": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_u32, P(c_u64), c_vp]),
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),

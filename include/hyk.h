@@ -219,6 +219,25 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
                   void *workspace, size_t workspace_bytes, uint32_t check_every, uint64_t *iters,
                   void *stream);
 
+/* hyk_propagate without a workspace, for callers that cannot allocate device
+ * memory (code that runs inside another allocator's pool, a real-time loop
+ * that must not allocate, a host integration without a CUDA allocator).  No
+ * counterpart in the reference: it has no device memory at all.
+ * The counters hyk_propagate keeps in its workspace live instead in one
+ * file-scope device array of HYK_NOALLOC_SCRATCH_BYTES (4096) bytes, held by
+ * every GPU that loads libhyk until the process exits; a propagation whose
+ * hyk_propagate_workspace_size() exceeds it is rejected with HYK_ERR_INVALID.
+ * The current kernels need 256 bytes whatever the number of lanes.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  Every call clears the counters it
+ * needs before using them, so a call never sees the previous call's values,
+ * but all calls share the one array: calls that overlap on the GPU (other
+ * streams, other threads) race and give wrong results.  It allocates nothing
+ * and calls no allocating CUDA or library routine. */
+#define HYK_NOALLOC_SCRATCH_BYTES 4096
+int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode,
+                          uint32_t check_every, uint64_t *iters, void *stream);
+
 /* Dense output: out[i][l] = sum_n tc[i][n][l] * dt[l]^n (Horner), the
  * evaluator behind update_d_output / continuous output
  * (heyoka/expose_batch_integrators.cpp:519-541,
