@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="kepler", choices=["kepler", "serve"],
+                    help="kepler: the headline metric; serve: the Poisson request stream (p50/p99 latency)")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
+    ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
+    ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
     return ap.parse_args()
 
 
@@ -64,6 +69,17 @@ def dist_init(n):
     return rank, world
 
 
+_ICS = {}
+
+
+def _ensemble_ics(seed):
+    from hyk import workloads as W
+
+    if seed not in _ICS:
+        _ICS[seed] = W.kepler_ics(1 << 20, seed=seed)
+    return _ICS[seed]
+
+
 def cpu_baseline(n_orbits, seed, t_end, steps=1):
     """Time the CPU restatement on n_orbits of the same ensemble, all host threads."""
     import numpy as np
@@ -71,7 +87,7 @@ def cpu_baseline(n_orbits, seed, t_end, steps=1):
     import pyoracle
     from hyk import workloads as W
 
-    st = W.kepler_ics(1 << 20, seed=seed)
+    st = _ensemble_ics(seed)
     idx = np.random.default_rng(123).choice(st.shape[1], n_orbits, replace=False)
     sample = np.ascontiguousarray(st[:, np.sort(idx)])
     threads = pyoracle.lib().hyko_max_threads()
@@ -176,11 +192,107 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def serve_stream(rate, duration, seed=4):
+    """Poisson arrivals; size ~ round(logU[1, 4096]); system ~ U{pendulum, kepler,
+    cr3bp} with the workload initial-condition laws; horizon ~ logU[1, 1000]."""
+    import math
+
+    import numpy as np
+
+    from hyk import serve
+    from hyk import workloads as W
+
+    rng = np.random.default_rng(seed)
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        size = int(round(math.exp(rng.uniform(0.0, math.log(4096.0)))))
+        kind = ["pendulum", "kepler", "cr3bp"][int(rng.integers(3))]
+        tf = float(math.exp(rng.uniform(0.0, math.log(1000.0))))
+        s = int(rng.integers(1 << 30))
+        if kind == "pendulum":
+            st, pa = W.pendulum_ics(size, seed=s), None
+        elif kind == "kepler":
+            st, pa = W.kepler_ics(size, seed=s), None
+        else:
+            st, pa = W.cr3bp_ics(size, seed=s)
+        reqs.append(serve.Request(kind, st, tf, pars=pa, arrival=t, rid=len(reqs)))
+    return reqs
+
+
+def run_serve(args):
+    import numpy as np
+    import torch
+
+    import hyk
+    from hyk import serve
+    from hyk import workloads as W
+
+    systems = {"pendulum": (W.pendulum_sys(), 1e-15), "kepler": (W.kepler_sys(), 1e-15), "cr3bp": (W.cr3bp_sys(), 1e-15)}
+    reqs = serve_stream(args.rate, args.duration)
+    srv = serve.Server(systems, hbm_budget=4 << 30, slice_iters=args.slice)
+    srv.run(serve_stream(50.0, 0.2, seed=99), realtime=False)  # warm-up: compile, first launches
+    for p in srv.pools.values():
+        p.lane_steps = 0
+    clk = Clocks(0)
+    t0 = time.perf_counter()
+    res = srv.run(reqs, realtime=True)
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    stats = serve.latency_stats(res)
+    steps = srv.trajectory_steps()
+    # isolated solve time of a sample of the same requests (alone on the GPU)
+    rng = np.random.default_rng(5)
+    sample = rng.choice(len(reqs), size=min(40, len(reqs)), replace=False)
+    by_id = {r.rid: r for r in res}
+    ratios, iso = [], []
+    for i in sample:
+        r = reqs[int(i)]
+        sys_, tol = systems[r.system]
+        ta = hyk.taylor_adaptive_batch(sys_, r.state, pars=r.pars, tol=tol)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        ta.propagate_until(r.t_final)
+        ta.state.cpu()
+        b = time.perf_counter()
+        iso.append(b - a)
+        ratios.append(by_id[r.rid].latency / (b - a))
+    line = {
+        "metric": "serving: FP64 trajectory-steps/s and p50/p99 request latency, Poisson stream",
+        "value": steps / wall,
+        "unit": UNIT,
+        "n_gpus": 1,
+        "higher_is_better": True,
+        "dtype": "f64",
+        "data": "synthetic (seeded request stream)",
+        "config": {
+            "workload": "serve: Poisson {:g} req/s for {:g} s, size round(logU[1,4096]), system U{{pendulum,kepler,cr3bp}}, "
+                        "horizon logU[1,1000], tol 1e-15".format(args.rate, args.duration),
+            "requests": len(reqs),
+            "slice_iters": args.slice,
+            "pool_capacity": {k: p.C for k, p in srv.pools.items()},
+        },
+        "latency": stats,
+        "isolated_solve_ms": {"p50": float(np.percentile(iso, 50) * 1e3), "p99": float(np.percentile(iso, 99) * 1e3)},
+        "latency_over_isolated": {"p50": float(np.percentile(ratios, 50)), "p99": float(np.percentile(ratios, 99))},
+        "offered_traj_per_s": sum(r.state.shape[1] for r in reqs) / args.duration,
+        "wall_s": wall,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "serve":
+        if rank == 0:
+            run_serve(args)
         return
     import numpy as np
     import torch

@@ -124,6 +124,7 @@ struct KParams {
     uint64_t *queue;
     uint32_t *finished;
     const uint64_t *lane_order;
+    uint64_t n_order;
     int persistent;
 };
 
@@ -439,6 +440,7 @@ static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const 
     k.last_tc = p->last_tc;
     k.status = p->status;
     k.lane_order = p->lane_order;
+    k.n_order = p->lane_order ? p->n_order : lanes->n_lanes;
     (void)m;
     return 0;
 }
@@ -480,7 +482,7 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (mode == HYK_MODE_PERSISTENT) {
         HYK_CU(drv().cuMemsetD32Async((CUdeviceptr)workspace, 0, 4, s));
         k.persistent = 1;
-        k.iters_per_launch = ~0ULL;
+        k.iters_per_launch = p->slice_iters ? p->slice_iters : ~0ULL;
         const uint64_t grid = (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm;
         rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
         if (rc) return rc;

@@ -9,6 +9,8 @@ with NVRTC for sm_103a (libhyk.so, C ABI in include/hyk.h).
 """
 from .expr import expression, make_vars, par, time, sin, cos, exp, log, sqrt, square, sum, prod  # noqa: F401
 from .decompose import taylor_decompose, order_from_tol  # noqa: F401
+from .expr import diff  # noqa: F401
+from .var import var_args, var_ode_sys  # noqa: F401
 from . import model, workloads  # noqa: F401
 from .integrator import taylor_adaptive_batch, taylor_outcome  # noqa: F401
 from .c_output import continuous_output_batch  # noqa: F401

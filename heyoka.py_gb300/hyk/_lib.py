@@ -96,6 +96,8 @@ class hyk_prop_t(ctypes.Structure):
         ("last_tc", c_vp),
         ("status", c_vp),
         ("lane_order", c_vp),
+        ("n_order", c_u64),
+        ("slice_iters", c_u64),
     ]
 
 

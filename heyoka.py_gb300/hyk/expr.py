@@ -397,3 +397,53 @@ def get_variables(e) -> list:
             out.add(n.value)
         stack.extend(n.args)
     return sorted(out)
+
+
+def diff(e, v):
+    """Symbolic derivative of ``e`` with respect to a variable or parameter
+    (reference: heyoka/expose_expression.cpp:531)."""
+    e, v = _ex(e), _ex(v)
+    if v.kind not in (VAR, PAR):
+        raise ValueError("Derivatives can be taken only with respect to variables or parameters")
+    memo = {}
+
+    def d(n):
+        if n in memo:
+            return memo[n]
+        if n.kind in (VAR, PAR):
+            r = expression(1.0) if n == v else expression(0.0)
+        elif n.kind in (NUM, TIME):
+            r = expression(0.0)
+        else:
+            f, a = n.value, n.args
+            if f == "add":
+                r = d(a[0]) + d(a[1])
+            elif f == "sub":
+                r = d(a[0]) - d(a[1])
+            elif f == "neg":
+                r = -d(a[0])
+            elif f == "mul":
+                r = d(a[0]) * a[1] + a[0] * d(a[1])
+            elif f == "div":
+                r = d(a[0]) / a[1] - a[0] * d(a[1]) / square(a[1])
+            elif f == "square":
+                r = 2.0 * a[0] * d(a[0])
+            elif f == "sqrt":
+                r = d(a[0]) / (2.0 * n)
+            elif f == "pow":
+                alpha = a[1].value
+                r = alpha * a[0] ** (alpha - 1.0) * d(a[0])
+            elif f == "exp":
+                r = n * d(a[0])
+            elif f == "log":
+                r = d(a[0]) / a[0]
+            elif f == "sin":
+                r = cos(a[0]) * d(a[0])
+            elif f == "cos":
+                r = -(sin(a[0]) * d(a[0]))
+            else:  # pragma: no cover
+                raise NotImplementedError(f)
+        memo[n] = r
+        return r
+
+    return d(e)

@@ -163,8 +163,11 @@ class taylor_adaptive_batch:
             raise ValueError("prop_mode must be 'persistent' or 'plain'")
         if schedule not in ("lpt", "fifo"):
             raise ValueError("schedule must be 'lpt' or 'fifo'")
-        if hasattr(sys, "vargs"):
-            raise NotImplementedError("variational systems are not supported by the GPU batch integrator")
+        from .var import var_ode_sys
+
+        self._vsys = sys if isinstance(sys, var_ode_sys) else None
+        if self._vsys is not None:
+            sys = self._vsys.sys
 
         st = _to_f64_array(state, "state")
         if st.ndim != 2:
@@ -174,6 +177,9 @@ class taylor_adaptive_batch:
             )
         B = st.shape[1]
         self._dec = taylor_decompose(sys)
+        if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
+            # the variational part starts from the identity (state arguments) and zero (parameters)
+            st = np.concatenate([st, self._vsys.initial_variational_state(B)])
         if st.shape[0] != self._dec.n_eq:
             raise ValueError(
                 "Inconsistent sizes detected in the initialization of an adaptive Taylor integrator: "
@@ -297,7 +303,29 @@ class taylor_adaptive_batch:
 
     @property
     def is_variational(self):
-        return False
+        return self._vsys is not None
+
+    @property
+    def n_orig_sv(self):
+        return self._vsys.n_orig_sv if self._vsys is not None else self.dim
+
+    @property
+    def vargs(self):
+        return list(self._vsys.vargs) if self._vsys is not None else []
+
+    @property
+    def vorder(self):
+        return self._vsys.order if self._vsys is not None else 0
+
+    def get_vslice(self, order, component=None):
+        if self._vsys is None:
+            raise ValueError("The integrator is not variational")
+        return self._vsys.vslice(order, component)
+
+    def get_mindex(self, i):
+        if self._vsys is None:
+            raise ValueError("The integrator is not variational")
+        return self._vsys.mindex(i)
 
     @property
     def device(self):
@@ -540,6 +568,7 @@ class taylor_adaptive_batch:
                 None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
+                0 if lane_order is None else lane_order.numel(), 0,
             )
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)

@@ -191,9 +191,16 @@ typedef struct hyk_prop {
     double *last_h;      /* h of the last iteration */
     double *last_tc;     /* (n_eq, order+1, ld) Taylor coefficients of the last step, or NULL */
     uint32_t *status;    /* per-lane status bits HYK_LANE_* */
-    /* persistent form only: order in which lanes are taken from the queue
-     * (a permutation of 0..n_lanes-1, e.g. longest-first), or NULL */
+    /* persistent form only: the lanes to run, in the order they are taken
+     * from the queue (lane_order[0..n_order), e.g. longest-first or the
+     * active slots of a serving pool), or NULL for all lanes in index order */
     const uint64_t *lane_order;
+    uint64_t n_order;
+    /* persistent form only: at most this many iterations per lane per call
+     * (0 = until done).  A lane that reaches it is stored unfinished and the
+     * next call continues it; used to time-slice a continuously refilled
+     * batch (serving). */
+    uint64_t slice_iters;
 } hyk_prop_t;
 
 #define HYK_LANE_DONE 1u     /* reached the final time */
