@@ -143,7 +143,12 @@ struct Gen {
     std::ostringstream o;
     double flops = 0;
 
-    Gen(const Dec &dd, uint32_t order, bool pin_arith) : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith) {
+    bool adj = false;  // also emit the reverse sweep (adjoint module)
+    std::vector<int> aslot, akslot;
+    uint32_t abase = 0;
+
+    Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false)
+        : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint) {
         base.resize(NU);
         negf.assign(NU, 0);
         alias.assign(NU, 0);
@@ -229,6 +234,23 @@ struct Gen {
                 break;
             }
         }
+        if (adj) {
+            // Values the reverse sweep reads besides the forward histories:
+            // the factor multiplied by a parameter (for the parameter's
+            // adjoint), the quotient by a parameter, and the logarithm.
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                const uint32_t u = N + k;
+                if (alias[u]) continue;
+                const auto &op = d.ops[k];
+                const Ref A = res(op.a), B = res(op.b);
+                if (op.op == HYK_OP_MUL) {
+                    if (A.kind == HYK_ARG_PAR && B.kind == HYK_ARG_U) hist[B.u] = 1;
+                    if (B.kind == HYK_ARG_PAR && A.kind == HYK_ARG_U) hist[A.u] = 1;
+                }
+                if (op.op == HYK_OP_DIV && B.kind == HYK_ARG_PAR) hist[u] = 1;
+                if (op.op == HYK_OP_LOG) hist[u] = 1;
+            }
+        }
         // Slots: state variables (orders 0..p), other histories (orders
         // 0..p-2: order p-1 is only read within its own block and order p of
         // intermediates is never computed), j*a_j histories (orders 1..p-2),
@@ -240,7 +262,8 @@ struct Gen {
             slot[i] = (int)s;
             s += p + 1;
         }
-        const uint32_t hl = p >= 2 ? p - 1 : 1, kl = p >= 3 ? p - 2 : 0;
+        // The adjoint module keeps every history up to order p-1.
+        const uint32_t hl = adj ? p : (p >= 2 ? p - 1 : 1), kl = adj ? p - 1 : (p >= 3 ? p - 2 : 0);
         for (uint32_t u = N; u < NU; ++u)
             if (hist[u] && !alias[u]) {
                 slot[u] = (int)s;
@@ -253,6 +276,22 @@ struct Gen {
             }
         par_slot = s;
         s += d.n_pars;
+        if (adj) {
+            // Adjoint accumulators: orders 0..p of every history, of every j*a_j.
+            abase = s;
+            aslot.assign(NU, -1);
+            akslot.assign(NU, -1);
+            for (uint32_t u = 0; u < NU; ++u)
+                if (hist[u] && !alias[u]) {
+                    aslot[u] = (int)s;
+                    s += p + 1;
+                }
+            for (uint32_t u = 0; u < NU; ++u)
+                if (needka[u] && !alias[u]) {
+                    akslot[u] = (int)s;
+                    s += p + 1;
+                }
+        }
         nslot = s;
     }
 
@@ -358,11 +397,12 @@ struct Gen {
     void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
 
     void store_hist(uint32_t u, uint32_t n) {
-        if (u >= N && hist[u] && n + 2 <= p) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
+        const uint32_t lim = adj ? p : p - 1;  // stored orders: 0..lim-1
+        if (u >= N && hist[u] && n + 1 <= lim) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
         if (needka[u] && n >= 1) {
             o << "    const double " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
             flops += 1;
-            if (kslot[u] >= 0 && n + 2 <= p) o << "    " << smem((uint32_t)kslot[u] + n - 1) << " = " << kname(u, n) << ";\n";
+            if (kslot[u] >= 0 && n + 1 <= lim) o << "    " << smem((uint32_t)kslot[u] + n - 1) << " = " << kname(u, n) << ";\n";
         }
     }
 
@@ -573,7 +613,7 @@ struct Gen {
                     o << "    const double " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
                       << vname(i, n + 1) << ";\n";
                     flops += 1;
-                    if (kslot[i] >= 0 && n + 1 + 2 <= p)
+                    if (kslot[i] >= 0 && n + 1 + (adj ? 1u : 2u) <= p)
                         o << "    " << smem((uint32_t)kslot[i] + n) << " = " << kname(i, n + 1) << ";\n";
                 }
             }
@@ -581,6 +621,239 @@ struct Gen {
             // warp barrier keeps the compiler from carrying them in registers.
             o << "    __syncwarp();\n";
         }
+        o << "}\n";
+    }
+
+    // ------------------------------------------------------------------
+    // Reverse sweep (adjoint module).  Reads the forward coefficients from
+    // shared memory only, accumulates the adjoint of every stored
+    // coefficient in its own slot and of same-order temporaries in
+    // registers, and walks the orders and the operations backwards.  The
+    // step size is held fixed: the derivative is that of the Taylor map
+    // x_{k+1} = sum_n x^[n](x_k, p, t_k) h_k^n at the taped h_k.
+    std::string val(const Ref &r, uint32_t j) const {
+        switch (r.kind) {
+        case HYK_ARG_U: {
+            const std::string s = smem((uint32_t)slot[r.u] + j);
+            return r.neg ? "(-" + s + ")" : s;
+        }
+        case HYK_ARG_NUM:
+            return j == 0 ? lit(r.num) : "0.0";
+        case HYK_ARG_PAR:
+            return j == 0 ? "HYK_PAR(" + std::to_string(r.par) + ")" : "0.0";
+        case HYK_ARG_TIME:
+            return j == 0 ? "t0" : (j == 1 ? "1.0" : "0.0");
+        }
+        return "0.0";
+    }
+    std::string kval(const Ref &r, uint32_t j) const {
+        if (r.kind == HYK_ARG_U) {
+            const std::string s = smem((uint32_t)kslot[r.u] + j - 1);
+            return r.neg ? "(-" + s + ")" : s;
+        }
+        return (r.kind == HYK_ARG_TIME && j == 1) ? "1.0" : "0.0";
+    }
+    std::string aref(uint32_t u, uint32_t j) const { return smem((uint32_t)aslot[u] + j); }
+    std::string akref(uint32_t u, uint32_t j) const { return smem((uint32_t)akslot[u] + j); }
+    std::string gname(uint32_t u, uint32_t n) const { return "g" + std::to_string(u) + "_" + std::to_string(n); }
+    // adjoint(r, order j) += x * y
+    void acc(const Ref &r, uint32_t j, uint32_t n, const std::string &x, const std::string &y) {
+        if (r.kind == HYK_ARG_U) {
+            const uint32_t u = (uint32_t)r.u;
+            const std::string xx = r.neg ? "(-" + x + ")" : x;
+            std::string t;
+            if (hist[u])
+                t = aref(u, j);
+            else {
+                if (j != n) {
+                    std::fprintf(stderr, "hyk codegen: adjoint of a non-stored value at another order (u%u)\n", u);
+                    std::abort();
+                }
+                t = gname(u, n);
+            }
+            o << "    " << t << " = __fma_rn(" << xx << ", " << y << ", " << t << ");\n";
+        } else if (r.kind == HYK_ARG_PAR && j == 0) {
+            o << "    pb[" << r.par << "] = __fma_rn(" << x << ", " << y << ", pb[" << r.par << "]);\n";
+        }
+    }
+    void acck(const Ref &r, uint32_t j, const std::string &x, const std::string &y) {
+        if (r.kind != HYK_ARG_U) return;
+        const std::string xx = r.neg ? "(-" + x + ")" : x;
+        o << "    " << akref((uint32_t)r.u, j) << " = __fma_rn(" << xx << ", " << y << ", " << akref((uint32_t)r.u, j)
+          << ");\n";
+    }
+
+    void emit_op_bw(uint32_t k, uint32_t n) {
+        const auto &op = d.ops[k];
+        const uint32_t u = N + k;
+        if (alias[u]) return;
+        const Ref A = res(op.a), B = res(op.b);
+        const Ref self{HYK_ARG_U, (int)u, false, 0, -1};
+        // A function of a constant is constant: nothing flows back above order 0.
+        const bool unary_fn = op.op == HYK_OP_SQRT || op.op == HYK_OP_POW || op.op == HYK_OP_EXP ||
+                              op.op == HYK_OP_LOG || op.op == HYK_OP_SIN || op.op == HYK_OP_COS;
+        if (unary_fn && n >= 1 && !varying(A)) return;
+        const std::string G = "G" + std::to_string(u) + "_" + std::to_string(n);
+        std::string gsrc = hist[u] ? aref(u, n) : gname(u, n);
+        if (needka[u] && n >= 1) gsrc = "__fma_rn(" + lit((double)n) + ", " + akref(u, n) + ", " + gsrc + ")";
+        o << "    const double " << G << " = " << gsrc << ";\n";
+        const std::string W = "W" + std::to_string(u) + "_" + std::to_string(n);
+        const std::string inv = "i" + std::to_string(u);
+        switch (op.op) {
+        case HYK_OP_ADD:
+            if (nz(A, n)) acc(A, n, n, G, "1.0");
+            if (nz(B, n)) acc(B, n, n, G, "1.0");
+            break;
+        case HYK_OP_SUB:
+            if (nz(A, n)) acc(A, n, n, G, "1.0");
+            if (nz(B, n)) acc(B, n, n, G, "(-1.0)");
+            break;
+        case HYK_OP_NEG:
+            if (nz(A, n)) acc(A, n, n, G, "(-1.0)");
+            break;
+        case HYK_OP_MUL:
+            for (uint32_t j = 0; j <= n; ++j)
+                if (nz(A, j) && nz(B, n - j)) {
+                    acc(A, j, n, G, val(B, n - j));
+                    acc(B, n - j, n, G, val(A, j));
+                }
+            break;
+        case HYK_OP_DIV:
+            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
+            if (nz(A, n)) acc(A, n, n, W, "1.0");
+            for (uint32_t j = 1; j <= n; ++j)
+                if (nz(B, j)) {
+                    acc(B, j, n, "(-" + W + ")", val(self, n - j));
+                    acc(self, n - j, n, "(-" + W + ")", val(B, j));
+                }
+            acc(B, 0, n, "(-" + W + ")", val(self, n));
+            break;
+        case HYK_OP_SQUARE:
+            for (uint32_t j = 0; j <= n; ++j)
+                if (nz(A, j) && nz(A, n - j)) acc(A, j, n, "(2.0 * " + G + ")", val(A, n - j));
+            break;
+        case HYK_OP_SQRT:
+            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
+            if (nz(A, n)) acc(A, n, n, W, "1.0");
+            if (n >= 1) {
+                for (uint32_t j = 1; j < n; ++j) acc(self, j, n, "(-2.0 * " + W + ")", val(self, n - j));
+                acc(self, 0, n, "(-2.0 * " + W + ")", val(self, n));
+            }
+            break;
+        case HYK_OP_POW: {
+            const double alpha = op.b.num;
+            if (n == 0) {
+                acc(A, 0, 0, "(" + G + " * " + lit(alpha) + ")", "(" + val(self, 0) + " * " + inv + ")");
+                break;
+            }
+            o << "    const double " << W << " = (" << G << " * " << inv << ") * " << lit(1.0 / (double)n) << ";\n";
+            for (uint32_t j = 0; j < n; ++j) {
+                if (!nz(A, n - j)) continue;
+                const double coef = (double)n * alpha - (double)j * (alpha + 1.0);
+                const std::string wc = "(" + W + " * " + lit(coef) + ")";
+                acc(A, n - j, n, wc, val(self, j));
+                acc(self, j, n, wc, val(A, n - j));
+            }
+            acc(A, 0, n, "(-" + G + " * " + inv + ")", val(self, n));
+            break;
+        }
+        case HYK_OP_EXP:
+            if (n == 0) {
+                acc(A, 0, 0, G, val(self, 0));
+                break;
+            }
+            o << "    const double " << W << " = " << G << " * " << lit(1.0 / (double)n) << ";\n";
+            for (uint32_t j = 1; j <= n; ++j)
+                if (knz(A, j)) {
+                    acck(A, j, W, val(self, n - j));
+                    acc(self, n - j, n, W, kval(A, j));
+                }
+            break;
+        case HYK_OP_LOG:
+            if (n == 0) {
+                acc(A, 0, 0, G, inv);
+                break;
+            }
+            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
+            if (nz(A, n)) acc(A, n, n, W, "1.0");
+            if (varying(A))
+                for (uint32_t j = 1; j < n; ++j) {
+                    if (!nz(A, n - j)) continue;
+                    const std::string t = "(-" + W + " * " + lit(1.0 / (double)n) + ")";
+                    acck(self, j, t, val(A, n - j));
+                    acc(A, n - j, n, t, kval(self, j));
+                }
+            acc(A, 0, n, "(-" + G + " * " + inv + ")", val(self, n));
+            break;
+        case HYK_OP_SIN:
+        case HYK_OP_COS: {
+            const Ref P{HYK_ARG_U, op.aux, false, 0, -1};
+            const bool is_sin = op.op == HYK_OP_SIN;
+            if (n == 0) {
+                acc(A, 0, 0, is_sin ? G : "(-" + G + ")", val(P, 0));
+                break;
+            }
+            o << "    const double " << W << " = " << G << " * " << lit((is_sin ? 1.0 : -1.0) / (double)n) << ";\n";
+            for (uint32_t j = 1; j <= n; ++j)
+                if (knz(A, j)) {
+                    acck(A, j, W, val(P, n - j));
+                    acc(P, n - j, n, W, kval(A, j));
+                }
+            break;
+        }
+        default:
+            break;
+        }
+    }
+
+    void emit_inverses(bool only_used) {
+        (void)only_used;
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const auto &op = d.ops[k];
+            const uint32_t u = N + k;
+            if (alias[u]) continue;
+            const Ref A = res(op.a), B = res(op.b);
+            const std::string inv = "i" + std::to_string(u);
+            if (op.op == HYK_OP_DIV) o << "    const double " << inv << " = 1.0 / " << val(B, 0) << ";\n";
+            if (op.op == HYK_OP_POW || op.op == HYK_OP_LOG) o << "    const double " << inv << " = 1.0 / " << val(A, 0) << ";\n";
+            if (op.op == HYK_OP_SQRT) o << "    const double " << inv << " = 1.0 / (2.0 * sqrt(" << val(A, 0) << "));\n";
+        }
+    }
+
+    // One function per order keeps each compiled block small (compile time
+    // grows faster than linearly with the size of a straight-line block).
+    void emit_bw() {
+        for (uint32_t n = 0; n < p; ++n) {
+            o << "static __device__ __noinline__ void hyk_bw_o" << n
+              << "(double *__restrict__ S, const double t0, double *__restrict__ pb) {\n";
+            o << "    (void)t0;\n";
+            emit_inverses(true);
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                const uint32_t u = N + k;
+                if (!alias[u] && !hist[u]) o << "    double " << gname(u, n) << " = 0.0;\n";
+            }
+            for (uint32_t ii = N; ii-- > 0;) {
+                const uint32_t i = ii;
+                if (needka[i])
+                    o << "    " << aref(i, n + 1) << " = __fma_rn(" << lit((double)(n + 1)) << ", " << akref(i, n + 1) << ", "
+                      << aref(i, n + 1) << ");\n";
+                const Ref r = res(d.rhs[i]);
+                if (nz(r, n)) acc(r, n, n, aref(i, n + 1), lit(1.0 / (double)(n + 1)));
+            }
+            for (uint32_t kk = d.n_ops; kk-- > 0;) emit_op_bw(kk, n);
+            o << "}\n";
+        }
+        o << "static __device__ __noinline__ void hyk_jets_bw(double *__restrict__ S, const double t0, const double h, "
+             "double *__restrict__ lam, double *__restrict__ pb) {\n";
+        o << "#pragma unroll 1\n    for (int s = " << abase << "; s < " << nslot << "; ++s) S[s * HYK_BLK] = 0.0;\n";
+        // Horner update x_new_i = sum_n x_i^[n] h^n
+        o << "    double hp = 1.0;\n";
+        for (uint32_t n = 0; n <= p; ++n) {
+            for (uint32_t i = 0; i < N; ++i) o << "    " << aref(i, n) << " = lam[" << i << "] * hp;\n";
+            if (n < p) o << "    hp = hp * h;\n";
+        }
+        for (uint32_t nn = p; nn-- > 0;) o << "    hyk_bw_o" << nn << "(S, t0, pb);\n";
+        for (uint32_t i = 0; i < N; ++i) o << "    lam[" << i << "] = " << aref(i, 0) << ";\n";
         o << "}\n";
     }
 };
@@ -596,18 +869,18 @@ const char *kDmath =
 
 }  // namespace
 
-uint32_t count_slots(const Dec &d, uint32_t order) {
-    Gen g(d, order, false);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint) {
+    Gen g(d, order, false, adjoint);
     return g.nslot;
 }
 
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err) {
+              std::string &err, bool adjoint) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
     }
-    Gen g(d, order, pin_arith);
+    Gen g(d, order, pin_arith, adjoint);
     const double p = (double)order;
     const double e1 = std::exp(1.0);
     const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
@@ -626,10 +899,12 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
         h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
         h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
     }
+    if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << kDmath << "\n";
     h << kTemplate << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
     g.emit_jets();
+    if (adjoint) g.emit_bw();
     // The template's kernels call hyk_jets(); declare-before-use ordering is
     // satisfied by emitting the jets function first.
     std::string body = g.o.str();
@@ -648,6 +923,53 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     // Per-step flops: recurrences + Horner (2 per coefficient) + step size
     // (two pow and the norm arithmetic) + double-length time update.
     out.flops = g.flops + 2.0 * d.n_eq * order + 46.0 + 10.0;
+    return true;
+}
+
+
+// Host translation unit of the same generated recurrences (forward jets and,
+// with the adjoint, the reverse sweep) for CPU checks of the generator: one
+// lane, HYK_BLK = 1, the CUDA intrinsics mapped to their host equivalents.
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err) {
+    if (order < 2) {
+        err = "the Taylor order must be at least 2";
+        return false;
+    }
+    Gen g(d, order, false, adjoint);
+    const double p = (double)order;
+    const double e1 = std::exp(1.0);
+    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+    std::ostringstream h;
+    h << "#include <cmath>\n#include <cstdint>\n#define __device__\n#define __noinline__\n"
+         "#define __forceinline__ inline\n#define __restrict__\n"
+         "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
+         "static inline void __syncwarp() {}\n";
+    h << kDmath << "\n";
+    h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
+      << "\n#define HYK_BLK 1\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
+      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
+      << lit(1.0 / (p - 1.0)) << "\n";
+    h << "#define HYK_SX(i, n) S[((i) * (HYK_ORDER + 1) + (n)) * HYK_BLK]\n#define HYK_PAR(k) S[(HYK_PAR_SLOT + (k)) * HYK_BLK]\n";
+    h << "static inline double hyk_inf() { return HUGE_VAL; }\n";
+    g.emit_jets();
+    if (adjoint) g.emit_bw();
+    h << g.o.str();
+    h << "extern \"C\" int hyk_host_nslot(void) { return HYK_NSLOT; }\n";
+    h << "extern \"C\" void hyk_host_step(double *S, const double *x0, const double *pars, double t0, double h, double *x1) {\n"
+         "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
+         "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
+         "    hyk_jets(S, t0);\n"
+         "    for (int i = 0; i < HYK_NEQ; ++i) {\n"
+         "        double acc = HYK_SX(i, HYK_ORDER);\n"
+         "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
+         "        x1[i] = acc;\n    }\n}\n";
+    if (adjoint)
+        h << "extern \"C\" void hyk_host_adjoint(double *S, const double *x0, const double *pars, double t0, double h, "
+             "double *lam, double *pb) {\n"
+             "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
+             "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
+             "    hyk_jets(S, t0);\n    hyk_jets_bw(S, t0, h, lam, pb);\n}\n";
+    src = h.str();
     return true;
 }
 

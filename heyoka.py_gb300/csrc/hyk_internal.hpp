@@ -29,9 +29,14 @@ struct GenOut {
 
 // Shared-memory slots per lane for a decomposition at a given order (the
 // block size does not change it).
-uint32_t count_slots(const Dec &d, uint32_t order);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false);
 
+// adjoint: also emit the reverse sweep hyk_jets_bw() and the adjoint kernel
+// (and keep every history up to order p-1 for it).
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err);
+              std::string &err, bool adjoint = false);
+
+// Host (CPU) translation unit of the same recurrences, for checks of the generator.
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err);
 
 }  // namespace hyk

@@ -125,6 +125,10 @@ struct KParams {
     uint32_t *finished;
     const uint64_t *lane_order;
     uint64_t n_order;
+    double *ck_x, *ck_t, *ck_h;
+    uint64_t ck_cap;
+    const int64_t *adj_steps;
+    double *adj_lambda, *adj_pbar;
     int persistent;
 };
 
@@ -214,7 +218,8 @@ struct hyk_module {
     int device = 0;
     Device *dv = nullptr;
     CUmodule mod = nullptr;
-    CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr;
+    CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
+    int adj_ctas_per_sm = 0;
     std::string src, log;
     uint32_t blk = 0, nslot = 0;
     size_t smem = 0;
@@ -241,7 +246,8 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (rc) return rc;
     const Device &dv = *m->dv;
 
-    const uint32_t nslot = hyk::count_slots(m->d, order);
+    const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
+    const uint32_t nslot = hyk::count_slots(m->d, order, adjoint);
     const size_t lane_bytes = (size_t)nslot * sizeof(double);
     uint32_t blk = m->cfg.block_lanes;
     if (blk == 0) {
@@ -276,7 +282,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         return fail(HYK_ERR_UNSUPPORTED, "shared memory per CTA (" + std::to_string(m->smem) + ") exceeds the device limit");
 
     hyk::GenOut g;
-    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err))
+    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err, adjoint))
         return fail(HYK_ERR_INVALID, err);
     m->src = g.src;
     m->flops = g.flops;
@@ -328,6 +334,13 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuFuncGetAttribute(&m->regs, CU_FUNC_ATTRIBUTE_NUM_REGS, m->f_prop));
     HYK_CU(drv().cuFuncGetAttribute(&m->local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, m->f_prop));
     HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->ctas_per_sm, m->f_prop, (int)blk, m->smem));
+    if (adjoint) {
+        HYK_CU(drv().cuModuleGetFunction(&m->f_adj, m->mod, "hyk_adjoint_kernel"));
+        HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
+        HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+        HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->adj_ctas_per_sm, m->f_adj, (int)blk, m->smem));
+        if (m->adj_ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the adjoint kernel cannot be resident on an SM");
+    }
     if (m->ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the propagation kernel cannot be resident on an SM");
     *out = m.release();
     return 0;
@@ -441,6 +454,11 @@ static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const 
     k.status = p->status;
     k.lane_order = p->lane_order;
     k.n_order = p->lane_order ? p->n_order : lanes->n_lanes;
+    k.ck_x = p->ck_x;
+    k.ck_t = p->ck_t;
+    k.ck_h = p->ck_h;
+    k.ck_cap = p->ck_capacity;
+    if (p->ck_x && (!p->ck_t || !p->ck_h)) return fail(HYK_ERR_INVALID, "the checkpoint tape needs ck_x, ck_t and ck_h");
     (void)m;
     return 0;
 }
@@ -536,6 +554,34 @@ int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
     return hyk_propagate(m, lanes, p, mode, ws, cap, check_every, iters, stream);
 }
 
+int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,
+                const int64_t *n_steps, double *lambda, double *pbar, void *workspace, size_t workspace_bytes,
+                void *stream) {
+    int rc = check_lanes(m, lanes);
+    if (rc) return rc;
+    if (!m->f_adj) return fail(HYK_ERR_INVALID, "the module was not created with HYK_CFG_ADJOINT");
+    if (lanes->n_lanes == 0) return 0;
+    if (!ck_x || !ck_t || !ck_h || !n_steps || !lambda || (m->d.n_pars && !pbar))
+        return fail(HYK_ERR_INVALID, "null tape, step-count, adjoint or parameter-adjoint pointer");
+    if (!workspace || workspace_bytes < 256 || (reinterpret_cast<uintptr_t>(workspace) & 255u))
+        return fail(HYK_ERR_INVALID, "the workspace must be at least 256 bytes, 256-byte aligned");
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    KParams k;
+    fill_lanes(k, lanes);
+    k.ck_x = const_cast<double *>(ck_x);
+    k.ck_t = const_cast<double *>(ck_t);
+    k.ck_h = const_cast<double *>(ck_h);
+    k.ck_cap = (uint64_t)INT64_MAX;  // the caller's tape holds n_steps[lane] steps for every lane
+    k.adj_steps = n_steps;
+    k.adj_lambda = lambda;
+    k.adj_pbar = pbar;
+    k.queue = reinterpret_cast<uint64_t *>(workspace);
+    const CUstream s = (CUstream)stream;
+    HYK_CU(drv().cuMemsetD32Async((CUdeviceptr)workspace, 0, 2, s));
+    const uint64_t grid = (uint64_t)m->dv->n_sm * (uint64_t)m->adj_ctas_per_sm;
+    return launch(m, m->f_adj, grid, m->blk, m->smem, k, stream);
+}
+
 int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld, const double *dt,
                    double *out, void *stream) {
     if (n_lanes == 0) return 0;
@@ -553,10 +599,17 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (order < 2 || order > 200) return fail(HYK_ERR_INVALID, "the Taylor order must be in [2, 200]");
     const uint32_t blk = (cfg && cfg->block_lanes) ? cfg->block_lanes : 128;
     const bool pin = cfg && (cfg->flags & HYK_CFG_PIN_ARITH);
+    const bool adjoint = cfg && (cfg->flags & HYK_CFG_ADJOINT);
     hyk::GenOut g;
-    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err)) return fail(HYK_ERR_INVALID, err);
+    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint)) return fail(HYK_ERR_INVALID, err);
     if (n_slot) *n_slot = g.n_slot;
     if (flops) *flops = g.flops;
+    if (verbose == 3) {  // host translation unit (CPU checks of the generator)
+        std::string hs;
+        if (!hyk::generate_host(d, order, adjoint, hs, err)) return fail(HYK_ERR_INVALID, err);
+        if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
+        return 0;
+    }
     if (verbose == 2) {  // source only, no compilation
         if (log && log_len) std::snprintf(log, log_len, "%s", g.src.c_str());
         return 0;

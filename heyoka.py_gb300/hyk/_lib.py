@@ -30,6 +30,7 @@ c_u32, c_u64, c_i64, c_int, c_d, c_vp = (
 HYK_MODE_PLAIN = 0
 HYK_MODE_PERSISTENT = 1
 HYK_CFG_PIN_ARITH = 1
+HYK_CFG_ADJOINT = 2
 
 LANE_DONE, LANE_STOPPED, LANE_CAPACITY = 1, 2, 4
 
@@ -97,6 +98,10 @@ class hyk_prop_t(ctypes.Structure):
         ("status", c_vp),
         ("lane_order", c_vp),
         ("n_order", c_u64),
+        ("ck_x", c_vp),
+        ("ck_t", c_vp),
+        ("ck_h", c_vp),
+        ("ck_capacity", c_u64),
         ("slice_iters", c_u64),
     ]
 
@@ -115,6 +120,7 @@ SIGNATURES = {
         [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_vp, ctypes.c_size_t, c_u32, P(c_u64), c_vp],
     ),
     "hyk_propagate_noalloc": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_u32, P(c_u64), c_vp]),
+    "hyk_adjoint": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_size_t, c_vp]),
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),

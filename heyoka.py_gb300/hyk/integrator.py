@@ -568,7 +568,7 @@ class taylor_adaptive_batch:
                 None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
-                0 if lane_order is None else lane_order.numel(), 0,
+                0 if lane_order is None else lane_order.numel(), None, None, None, 0, 0,
             )
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)

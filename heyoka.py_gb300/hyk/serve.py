@@ -202,7 +202,7 @@ class LanePool:
                 a["rem_hi"].data_ptr(), a["rem_lo"].data_ptr(), a["outcome"].data_ptr(), a["min_h"].data_ptr(),
                 a["max_h"].data_ptr(), a["n_steps"].data_ptr(), a["n_iter"].data_ptr(), None,
                 a["last_h"].data_ptr(), None, a["status"].data_ptr(), order.data_ptr(), order.numel(),
-                self.slice_iters,
+                None, None, None, 0, self.slice_iters,
             )
             lanes = lanes_struct(self.state, self.pars, self.thi, self.tlo)
             with torch.cuda.device(self.dev):

@@ -106,6 +106,7 @@ typedef struct hyk_config {
 } hyk_config_t;
 
 #define HYK_CFG_PIN_ARITH 1u /* oracle "pin" arithmetic: no FMA, divide by n (slower; for cross-checks) */
+#define HYK_CFG_ADJOINT 2u   /* also generate the adjoint (reverse-mode) kernel for hyk_adjoint() */
 
 typedef struct hyk_module_info {
     uint32_t n_eq, n_pars, order, n_u;
@@ -196,6 +197,13 @@ typedef struct hyk_prop {
      * active slots of a serving pool), or NULL for all lanes in index order */
     const uint64_t *lane_order;
     uint64_t n_order;
+    /* optional checkpoint tape for the adjoint: the state (ck_capacity,
+     * n_eq, ld), time (hi part) and step size (ck_capacity, ld) at the start
+     * of every iteration; a lane that fills it stops with HYK_LANE_CAPACITY */
+    double *ck_x;
+    double *ck_t;
+    double *ck_h;
+    uint64_t ck_capacity;
     /* persistent form only: at most this many iterations per lane per call
      * (0 = until done).  A lane that reaches it is stored unfinished and the
      * next call continues it; used to time-slice a continuously refilled
@@ -245,6 +253,21 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode,
                           uint32_t check_every, uint64_t *iters, void *stream);
 
+/* Discrete adjoint of a taped propagation (module created with
+ * HYK_CFG_ADJOINT).  For every lane, runs backwards over its n_steps[lane]
+ * taped steps: recomputes the step's Taylor coefficients from the taped
+ * state, then propagates the adjoint through the Horner update and the
+ * Taylor recurrences in reverse, with the taped step sizes held fixed.
+ *   lambda: (n_eq, ld) in: dL/dx(t_final); out: dL/dx(t_0)
+ *   pbar:   (n_pars, ld) out: dL/dpars (NULL when n_pars == 0)
+ * workspace: hyk_propagate_workspace_size() bytes, 256-byte aligned.
+ * Gradient of the reference's propagation, which has no adjoint: no
+ * counterpart in the reference (it offers forward variational equations,
+ * heyoka/expose_var_ode_sys.cpp:29-59). */
+int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,
+                const int64_t *n_steps, double *lambda, double *pbar, void *workspace, size_t workspace_bytes,
+                void *stream);
+
 /* Dense output: out[i][l] = sum_n tc[i][n][l] * dt[l]^n (Horner), the
  * evaluator behind update_d_output / continuous output
  * (heyoka/expose_batch_integrators.cpp:519-541,
@@ -267,8 +290,9 @@ int hyk_fp64_peak(int device, double millis, double *flops_per_s);
  * (block size cfg->block_lanes, default 128) and compile it with NVRTC for
  * sm_103a.  `log` receives the NVRTC log (ptxas register and spill
  * statistics when `verbose` is 1; the generated source, without compiling,
- * when `verbose` is 2); `n_slot` the shared-memory doubles per lane, `flops`
- * the algorithmic flops per step. */
+ * when `verbose` is 2; a host C++ translation unit of the same recurrences,
+ * for CPU checks, when `verbose` is 3); `n_slot` the shared-memory doubles
+ * per lane, `flops` the algorithmic flops per step. */
 int hyk_codegen_check(const hyk_decomp_t *d, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
                       size_t log_len, uint32_t *n_slot, double *flops);
 

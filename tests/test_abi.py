@@ -36,7 +36,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(hyk_arg_t) == 16 and ctypes.sizeof(hyk_uop_t) == 40
     assert ctypes.sizeof(hyk_decomp_t) == 32
     assert ctypes.sizeof(_lib.hyk_lanes_t) == 48
-    assert ctypes.sizeof(_lib.hyk_prop_t) == 25 * 8
+    assert ctypes.sizeof(_lib.hyk_prop_t) == 29 * 8
 
 
 def test_no_device_errors(libhyk):

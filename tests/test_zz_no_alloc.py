@@ -45,7 +45,7 @@ def _desc(tf, a):
         tf.data_ptr(), None, None, 0, None, 0, None, None, None, None, 0,
         a["rem_hi"].data_ptr(), a["rem_lo"].data_ptr(), a["outcome"].data_ptr(), a["min_h"].data_ptr(),
         a["max_h"].data_ptr(), a["n_steps"].data_ptr(), a["n_iter"].data_ptr(), None, a["last_h"].data_ptr(),
-        None, a["status"].data_ptr(), None, 0, 0,
+        None, a["status"].data_ptr(), None, 0, None, None, None, 0, 0,
     )
 
 
