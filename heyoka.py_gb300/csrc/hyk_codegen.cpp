@@ -147,8 +147,16 @@ struct Gen {
     std::vector<int> aslot, akslot;
     uint32_t abase = 0;
 
+    // Large systems: one function per Taylor order (a single straight-line
+    // function of tens of thousands of operations takes ptxas many minutes).
+    // Order n then reloads the state's order-n coefficients from the jet
+    // store and the 1/b_0 factors from slots of their own.
+    bool split = false;
+    std::vector<int> islot;
+
     Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false)
-        : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint) {
+        : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint),
+          split((uint64_t)dd.n_ops * order > 3000) {
         base.resize(NU);
         negf.assign(NU, 0);
         alias.assign(NU, 0);
@@ -274,6 +282,13 @@ struct Gen {
                 kslot[u] = (int)s;
                 s += kl;
             }
+        islot.assign(NU, -1);
+        if (split)
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                const int o = d.ops[k].op;
+                if (!alias[N + k] && (o == HYK_OP_DIV || o == HYK_OP_SQRT || o == HYK_OP_POW || o == HYK_OP_LOG))
+                    islot[N + k] = (int)s++;
+            }
         par_slot = s;
         s += d.n_pars;
         if (adj) {
@@ -297,7 +312,7 @@ struct Gen {
 
     std::string vname(uint32_t u, uint32_t n) const { return "v" + std::to_string(u) + "_" + std::to_string(n); }
     std::string kname(uint32_t u, uint32_t n) const { return "k" + std::to_string(u) + "_" + std::to_string(n); }
-    std::string smem(uint32_t s) const { return "S[" + std::to_string(s) + " * HYK_BLK]"; }
+    std::string smem(uint32_t s) const { return "S[" + std::to_string(s) + " * HYK_STRIDE]"; }
 
     // Coefficient of order j of u-variable u (not an alias) while emitting block n.
     std::string ucoef(uint32_t u, uint32_t j, uint32_t n) const {
@@ -393,6 +408,10 @@ struct Gen {
         return "(" + x + " * " + lit(1.0 / (double)n) + ")";
     }
     std::string inv0(uint32_t u) const { return "i" + std::to_string(u); }
+    // After defining 1/b_0 at order 0: keep it for the later order functions.
+    void keep_inv0(uint32_t u) {
+        if (split && !pin && islot[u] >= 0) o << "    " << smem((uint32_t)islot[u]) << " = " << inv0(u) << ";\n";
+    }
 
     void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
 
@@ -447,6 +466,7 @@ struct Gen {
                 def(u, 0, "(" + an + " / " + b0 + ")");
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << b0 << ";\n";
                 flops += 2;
+                keep_inv0(u);
                 break;
             }
             Acc s{acc};
@@ -477,6 +497,7 @@ struct Gen {
                 def(u, 0, "sqrt(" + an + ")");  // IEEE square root in both arithmetics
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / (2.0 * " << vname(u, 0) << ");\n";
                 flops += 3;
+                keep_inv0(u);
                 break;
             }
             Acc s{acc};
@@ -499,6 +520,7 @@ struct Gen {
                 def(u, 0, (pin ? "pow(" : "hyk_dm_pow(") + a0 + ", " + lit(alpha) + ")");
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
                 flops += 21;
+                keep_inv0(u);
                 break;
             }
             Acc s{acc};
@@ -540,6 +562,7 @@ struct Gen {
                 def(u, 0, (pin ? "log(" : "hyk_dm_log(") + a0 + ")");
                 if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
                 flops += 21;
+                keep_inv0(u);
                 break;
             }
             Acc s{acc};
@@ -590,14 +613,25 @@ struct Gen {
     }
 
     void emit_jets() {
-        o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
-        for (uint32_t i = 0; i < N; ++i) {
-            o << "    const double " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
-            if (needka[i]) {
-                // k_i_0 is never read (sums start at j = 1).
-            }
+        if (!split) {
+            o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
+            for (uint32_t i = 0; i < N; ++i) o << "    const double " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
         }
         for (uint32_t n = 0; n < p; ++n) {
+            if (split) {
+                o << "static __device__ __noinline__ void hyk_jets_o" << n
+                  << "(double *__restrict__ S, const double t0) {\n";
+                for (uint32_t i = 0; i < N; ++i) {
+                    o << "    const double " << vname(i, n) << " = HYK_SX(" << i << ", " << n << ");\n";
+                    // The same product the previous order formed (k_i_0 is never read).
+                    if (needka[i] && n >= 1)
+                        o << "    const double " << kname(i, n) << " = " << lit((double)n) << " * " << vname(i, n)
+                          << ";\n";
+                }
+                if (!pin && n >= 1)
+                    for (uint32_t u = N; u < NU; ++u)
+                        if (islot[u] >= 0) o << "    const double " << inv0(u) << " = " << smem((uint32_t)islot[u]) << ";\n";
+            }
             o << "    // ---- order " << n << "\n";
             for (uint32_t k = 0; k < d.n_ops; ++k) {
                 emit_op(k, n);
@@ -620,6 +654,11 @@ struct Gen {
             // Values of earlier orders are re-read from shared memory: the
             // warp barrier keeps the compiler from carrying them in registers.
             o << "    __syncwarp();\n";
+            if (split) o << "}\n";
+        }
+        if (split) {
+            o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
+            for (uint32_t n = 0; n < p; ++n) o << "    hyk_jets_o" << n << "(S, t0);\n";
         }
         o << "}\n";
     }
@@ -845,7 +884,7 @@ struct Gen {
         }
         o << "static __device__ __noinline__ void hyk_jets_bw(double *__restrict__ S, const double t0, const double h, "
              "double *__restrict__ lam, double *__restrict__ pb) {\n";
-        o << "#pragma unroll 1\n    for (int s = " << abase << "; s < " << nslot << "; ++s) S[s * HYK_BLK] = 0.0;\n";
+        o << "#pragma unroll 1\n    for (int s = " << abase << "; s < " << nslot << "; ++s) S[s * HYK_STRIDE] = 0.0;\n";
         // Horner update x_new_i = sum_n x_i^[n] h^n
         o << "    double hp = 1.0;\n";
         for (uint32_t n = 0; n <= p; ++n) {
@@ -875,7 +914,7 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint) {
 }
 
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint) {
+              std::string &err, bool adjoint, uint64_t gmem_stride) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -888,7 +927,9 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     h << "// Generated by libhyk: " << d.n_eq << " equations, " << d.n_ops << " u-operations, order " << order
       << (pin_arith ? ", pin arithmetic" : "") << "\n";
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
-      << "\n#define HYK_BLK " << blk << "\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
+      << "\n#define HYK_BLK " << blk << "\n#define HYK_TPB " << blk << "\n#define HYK_GMEM " << (gmem_stride ? 1 : 0)
+      << "\n#define HYK_STRIDE " << (gmem_stride ? std::to_string(gmem_stride) + "ULL" : std::to_string(blk))
+      << "\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
       << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
       << lit(1.0 / (p - 1.0)) << "\n";
     if (pin_arith) {
@@ -946,10 +987,10 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
          "static inline void __syncwarp() {}\n";
     h << kDmath << "\n";
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
-      << "\n#define HYK_BLK 1\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
+      << "\n#define HYK_BLK 1\n#define HYK_STRIDE 1\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
       << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
       << lit(1.0 / (p - 1.0)) << "\n";
-    h << "#define HYK_SX(i, n) S[((i) * (HYK_ORDER + 1) + (n)) * HYK_BLK]\n#define HYK_PAR(k) S[(HYK_PAR_SLOT + (k)) * HYK_BLK]\n";
+    h << "#define HYK_SX(i, n) S[((i) * (HYK_ORDER + 1) + (n)) * HYK_STRIDE]\n#define HYK_PAR(k) S[(HYK_PAR_SLOT + (k)) * HYK_STRIDE]\n";
     h << "static inline double hyk_inf() { return HUGE_VAL; }\n";
     g.emit_jets();
     if (adjoint) g.emit_bw();

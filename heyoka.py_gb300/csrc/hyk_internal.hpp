@@ -33,8 +33,10 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false);
 
 // adjoint: also emit the reverse sweep hyk_jets_bw() and the adjoint kernel
 // (and keep every history up to order p-1 for it).
+// gmem_stride != 0: Taylor coefficients in a global-memory buffer with that
+// slot stride (the number of threads of the fixed grid) instead of shared memory.
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint = false);
+              std::string &err, bool adjoint = false, uint64_t gmem_stride = 0);
 
 // Host (CPU) translation unit of the same recurrences, for checks of the generator.
 bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err);

@@ -45,7 +45,7 @@ thread_local std::string g_err;
 // driver entry point goes through this table.
 #define HYK_STR2(x) #x
 #define HYK_STR(x) HYK_STR2(x)
-#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree)
 
 struct DriverApi {
 #define HYK_DECL(f) decltype(&::f) f = nullptr;
@@ -129,6 +129,7 @@ struct KParams {
     uint64_t ck_cap;
     const int64_t *adj_steps;
     double *adj_lambda, *adj_pbar;
+    double *jets;
     int persistent;
 };
 
@@ -220,6 +221,9 @@ struct hyk_module {
     CUmodule mod = nullptr;
     CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
     int adj_ctas_per_sm = 0;
+    bool gmem = false;           // Taylor coefficients in a global buffer (large systems)
+    uint64_t gmem_threads = 0;   // threads of the fixed grid in that mode
+    CUdeviceptr jets = 0;        // the module's coefficient buffer (gmem mode)
     std::string src, log;
     uint32_t blk = 0, nslot = 0;
     size_t smem = 0;
@@ -250,7 +254,15 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const uint32_t nslot = hyk::count_slots(m->d, order, adjoint);
     const size_t lane_bytes = (size_t)nslot * sizeof(double);
     uint32_t blk = m->cfg.block_lanes;
-    if (blk == 0) {
+    // Systems whose coefficients do not fit 32 lanes of shared memory keep
+    // them in a global buffer owned by the module: one slot stride for the
+    // whole fixed grid, so a warp still reads 32 consecutive doubles.
+    m->gmem = lane_bytes * 32 > (size_t)dv.smem_optin;
+    if (m->gmem) {
+        if (blk == 0) blk = 128;
+        const uint32_t ctas = m->cfg.persist_ctas ? m->cfg.persist_ctas : 1;
+        m->gmem_threads = (uint64_t)dv.n_sm * ctas * blk;
+    } else if (blk == 0) {
         // Pick the block size maximising resident lanes per SM under the
         // shared-memory budget (1 KiB per CTA is reserved by the hardware),
         // capped at 512 lanes per SM and 256 per CTA.
@@ -277,12 +289,13 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (blk % 32 != 0 || blk > 1024) return fail(HYK_ERR_INVALID, "block_lanes must be a multiple of 32, <= 1024");
     m->blk = blk;
     m->nslot = nslot;
-    m->smem = (size_t)blk * lane_bytes;
+    m->smem = m->gmem ? 0 : (size_t)blk * lane_bytes;
     if (m->smem > (size_t)dv.smem_optin)
         return fail(HYK_ERR_UNSUPPORTED, "shared memory per CTA (" + std::to_string(m->smem) + ") exceeds the device limit");
 
     hyk::GenOut g;
-    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err, adjoint))
+    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err, adjoint,
+                       m->gmem ? m->gmem_threads : 0))
         return fail(HYK_ERR_INVALID, err);
     m->src = g.src;
     m->flops = g.flops;
@@ -324,6 +337,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     m->compile_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 
     HYK_CU(drv().cuModuleLoadData(&m->mod, cubin.data()));
+    if (m->gmem) HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->gmem_threads * lane_bytes));
     HYK_CU(drv().cuModuleGetFunction(&m->f_step, m->mod, "hyk_step_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_prop, m->mod, "hyk_prop_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
@@ -334,12 +348,22 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuFuncGetAttribute(&m->regs, CU_FUNC_ATTRIBUTE_NUM_REGS, m->f_prop));
     HYK_CU(drv().cuFuncGetAttribute(&m->local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, m->f_prop));
     HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->ctas_per_sm, m->f_prop, (int)blk, m->smem));
+    if (m->gmem) {
+        const int want = (int)(m->gmem_threads / ((uint64_t)dv.n_sm * blk));
+        if (m->ctas_per_sm < want) return fail(HYK_ERR_UNSUPPORTED, "the global-memory grid cannot be resident");
+        m->ctas_per_sm = want;
+    }
     if (adjoint) {
         HYK_CU(drv().cuModuleGetFunction(&m->f_adj, m->mod, "hyk_adjoint_kernel"));
         HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
         HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
         HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->adj_ctas_per_sm, m->f_adj, (int)blk, m->smem));
         if (m->adj_ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the adjoint kernel cannot be resident on an SM");
+        if (m->gmem) {
+            if (m->adj_ctas_per_sm < m->ctas_per_sm)
+                return fail(HYK_ERR_UNSUPPORTED, "the global-memory adjoint grid cannot be resident");
+            m->adj_ctas_per_sm = m->ctas_per_sm;
+        }
     }
     if (m->ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the propagation kernel cannot be resident on an SM");
     *out = m.release();
@@ -352,6 +376,7 @@ int hyk_module_destroy(hyk_module *m) {
         drv().cuCtxSetCurrent(m->dv->ctx);
         drv().cuModuleUnload(m->mod);
     }
+    if (m->jets) drv().cuMemFree(m->jets);
     delete m;
     return 0;
 }
@@ -364,7 +389,7 @@ int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info) {
     info->order = m->order;
     info->n_u = m->d.n_u();
     info->block_lanes = m->blk;
-    info->smem_per_lane = m->nslot * 8;
+    info->smem_per_lane = m->gmem ? 0u : m->nslot * 8;
     info->regs_per_thread = (uint32_t)m->regs;
     info->ctas_per_sm = (uint32_t)m->ctas_per_sm;
     info->n_sm = (uint32_t)m->dv->n_sm;
@@ -397,6 +422,9 @@ static void fill_lanes(KParams &k, const hyk_lanes_t *l) {
 
 static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k, void *stream) {
     if (grid == 0) return 0;
+    k.jets = reinterpret_cast<double *>(m->jets);
+    // In global-memory mode every kernel runs on the fixed grid the buffer is sized for.
+    if (m->gmem && f != m->f_init) grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * m->ctas_per_sm);
     if (grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
     void *args[] = {&k};
     HYK_CU(drv().cuLaunchKernel(f, (unsigned)grid, 1, 1, blk, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr));
@@ -600,8 +628,14 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const uint32_t blk = (cfg && cfg->block_lanes) ? cfg->block_lanes : 128;
     const bool pin = cfg && (cfg->flags & HYK_CFG_PIN_ARITH);
     const bool adjoint = cfg && (cfg->flags & HYK_CFG_ADJOINT);
+    // The same choice as the runtime: coefficients in global memory when 32
+    // lanes do not fit the opt-in shared memory of an SM (227 KB), with the
+    // slot stride of a 152-SM grid.
+    const uint32_t slots = hyk::count_slots(d, order, adjoint);
+    const uint64_t gstride = (uint64_t)slots * 8 * 32 > 227u * 1024 ? 152ull * blk : 0;
     hyk::GenOut g;
-    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint)) return fail(HYK_ERR_INVALID, err);
+    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride))
+        return fail(HYK_ERR_INVALID, err);
     if (n_slot) *n_slot = g.n_slot;
     if (flops) *flops = g.flops;
     if (verbose == 3) {  // host translation unit (CPU checks of the generator)

@@ -51,7 +51,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         f.write('R"HYKDM(' + dm + ')HYKDM"\n')
     # --fmad=false: device arithmetic exactly as written (no contraction), so
     # the shared math gives the same bits as the host build of the oracle.
-    common = [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+    # -ffp-contract=off: the code generator's host arithmetic (the literals it
+    # prints) is the same on x86-64 and on AArch64, where GCC would otherwise
+    # fuse multiply-adds.
+    common = [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "-I", INCLUDE, "-I", CSRC]
     common += ["-I", obj_dir]
     common += GENCODE
 

@@ -108,3 +108,17 @@ def oss_ics(n, seed=2):
     st = base.reshape(36, 1) * (1.0 + 1e-6 * rng.normal(size=(36, n)))
     t_end = np.exp(rng.uniform(math.log(1e3), math.log(1e5), n))
     return st, t_end
+
+
+def oss_energy(st):
+    """Total energy of outer-solar-system states, shape (36, n)."""
+    st = np.asarray(st, dtype=np.float64)
+    m = np.asarray(OSS_MASSES).reshape(-1, 1)
+    b = st.reshape(6, 6, -1)
+    kin = 0.5 * np.sum(m * np.sum(b[:, 3:6] ** 2, axis=1), axis=0)
+    pot = np.zeros(st.shape[1])
+    for i in range(6):
+        for j in range(i + 1, 6):
+            r = np.sqrt(np.sum((b[i, 0:3] - b[j, 0:3]) ** 2, axis=0))
+            pot -= OSS_G * m[i, 0] * m[j, 0] / r
+    return kin + pot

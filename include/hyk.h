@@ -111,7 +111,9 @@ typedef struct hyk_config {
 typedef struct hyk_module_info {
     uint32_t n_eq, n_pars, order, n_u;
     uint32_t block_lanes;        /* threads per CTA used by the kernels */
-    uint32_t smem_per_lane;      /* bytes of shared-memory jet storage per lane */
+    uint32_t smem_per_lane;      /* bytes of shared-memory jet storage per lane; 0 when the system is
+                                    too large for shared memory and its coefficients live in a
+                                    module-owned global buffer */
     uint32_t regs_per_thread;    /* from the compiled kernel */
     uint32_t ctas_per_sm;        /* resident CTAs per SM of the propagate kernel */
     uint32_t n_sm;
