@@ -297,6 +297,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err, adjoint,
                        m->gmem ? m->gmem_threads : 0))
         return fail(HYK_ERR_INVALID, err);
+    if (g.n_slot != nslot) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
     m->src = g.src;
     m->flops = g.flops;
 
