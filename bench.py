@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
+    ap.add_argument("--team-size", type=int, default=0,
+                    help="threads per trajectory (0: chosen per system, 1: lane form, 2..32: team form)")
     return ap.parse_args()
 
 
@@ -388,7 +390,7 @@ def run_oss(args):
     n = 65536
     st, t_end = W.oss_ics(n, seed=2)
     grid = np.linspace(0.0, 1.0, 100).reshape(-1, 1) * t_end.reshape(1, -1)
-    ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15)
+    ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=args.team_size)
     gd = torch.tensor(grid, device="cuda")
     sd = torch.tensor(st, device="cuda")
     ta.propagate_grid(gd[:, :].clone() * 1e-3)  # warm-up: compile, short run
@@ -424,8 +426,9 @@ def run_oss(args):
         "value": steps / t_dev, "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
         "data": "synthetic (near-circular orbits, 1e-6 relative Gaussian perturbations, seed 2)",
         "config": {"workload": "oss-6body-65536 propagate_grid", "order": ta.order,
+                   "threads_per_trajectory": info["team_size"],
                    "jets": "global memory" if info["smem_per_lane"] == 0 else "shared memory",
-                   "block_lanes": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"]},
+                   "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"]},
         "trajectory_steps": steps, "device_s": t_dev, "wall_s": float(np.median(walls)),
         "roofline": {"bound": "fp64", "achieved": fl / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": fl / peak, "traffic": None},
@@ -458,13 +461,13 @@ def main():
     dt = T_END / K
     n = args.orbits
     st = W.kepler_ics(n, seed=1 + rank)
-    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev), team_size=args.team_size)
     info = ta.module_info
     flops_step = info["flops_per_step"]
     peak = hyk.fp64_peak(dev, 300.0)
 
     # warm-up on a copy (same kernel, same data)
-    wcopy = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    wcopy = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev), team_size=args.team_size)
     for k in range(Wm):
         wcopy.propagate_until((k + 1) * dt)
     del wcopy
@@ -520,7 +523,7 @@ def main():
     host_state = torch.tensor(st, dtype=torch.float64).pin_memory()
     out_state = torch.empty_like(host_state).pin_memory()
     out_steps = torch.empty(n, dtype=torch.int64).pin_memory()
-    ta2 = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev))
+    ta2 = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev), team_size=args.team_size)
     ta2.propagate_until(dt)  # warm
     ta2.set_time(0.0)
     barrier()

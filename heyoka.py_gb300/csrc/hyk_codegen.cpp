@@ -33,6 +33,8 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <algorithm>
 #include <sstream>
 
 #include "hyk_internal.hpp"
@@ -897,8 +899,553 @@ struct Gen {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Team form.  HYK_TEAM consecutive threads of a warp integrate one trajectory
+// together: the u-operations of one dependency level are spread over the
+// team, one operation per thread and round, and every coefficient lives in
+// the trajectory's own shared-memory region (stride 1), so that a system too
+// large for 32 lanes of shared memory still runs from shared memory with
+// enough warps per SM.  The orders 1..p-1 are a runtime loop over per-level
+// code whose operand slots come from a table of per-operation descriptors;
+// each operation performs the same terms in the same order as the lane form
+// (Gen::emit_op), so both forms give the same bits.
+struct TeamGen {
+    Gen g;  // alias folding, histories and j*a_j needs (gpu arithmetic, no adjoint)
+    const Dec &d;
+    uint32_t p, N, NU;
+    uint32_t XS, HS, KS;  // strides of state rows, operation histories, j*a_j histories (odd)
+    std::vector<int> tslot, tkslot, tislot, level;
+    uint32_t nslot = 0, par_slot = 0;
+    int max_level = 0;
+    struct Desc {
+        int a = 0, b = 0, c = 0, ka = 0, kc = 0, inv = 0, prt = 0;
+        double num = 0;
+    };
+    std::vector<Desc> descs;
+    struct Group {
+        std::string key;
+        std::vector<uint32_t> members;  // u-variables (operations) or state indices (updates)
+        uint32_t off = 0;               // first descriptor
+    };
+    std::vector<std::vector<Group>> levels;  // [level - 1]
+    std::vector<Group> supd;                 // state updates
+    std::vector<double> alphas;              // distinct pow exponents
+    std::string err;
+    std::ostringstream o;
+
+    TeamGen(const Dec &dd, uint32_t order)
+        : g(dd, order, false, false), d(dd), p(order), N(dd.n_eq), NU(dd.n_u()) {
+        XS = (p + 1) | 1u;
+        HS = p | 1u;
+        KS = (p >= 2 ? p - 1 : 1) | 1u;
+        tslot.assign(NU, -1);
+        tkslot.assign(NU, -1);
+        tislot.assign(NU, -1);
+        level.assign(NU, 0);
+        uint32_t s = 0;
+        for (uint32_t i = 0; i < N; ++i) {
+            tslot[i] = (int)s;
+            s += XS;
+        }
+        for (uint32_t u = N; u < NU; ++u)
+            if (!g.alias[u]) {
+                tslot[u] = (int)s;
+                s += g.hist[u] ? HS : 1;
+            }
+        for (uint32_t u = 0; u < NU; ++u)
+            if (g.needka[u] && !g.alias[u]) {
+                tkslot[u] = (int)s;
+                s += KS;
+            }
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const int op = d.ops[k].op;
+            if (!g.alias[N + k] && (op == HYK_OP_DIV || op == HYK_OP_SQRT || op == HYK_OP_POW || op == HYK_OP_LOG))
+                tislot[N + k] = (int)s++;
+        }
+        par_slot = s;
+        s += d.n_pars;
+        nslot = s;
+    }
+
+    static bool isK(const Ref &r) { return r.kind == HYK_ARG_NUM || r.kind == HYK_ARG_PAR; }
+    static bool isU(const Ref &r) { return r.kind == HYK_ARG_U; }
+    static bool isT(const Ref &r) { return r.kind == HYK_ARG_TIME; }
+
+    // Whether the team form covers an operation (operand kinds per operation).
+    bool supported(uint32_t u, std::string &why) const {
+        const auto &op = d.ops[u - N];
+        const Ref A = g.res(op.a), B = g.res(op.b);
+        auto bad = [&](const char *m) {
+            why = std::string(m) + " at u" + std::to_string(u);
+            return false;
+        };
+        switch (op.op) {
+        case HYK_OP_ADD:
+        case HYK_OP_SUB:
+            if (isT(A) && isT(B)) return bad("time +- time");
+            if (A.kind == HYK_ARG_NUM && B.kind == HYK_ARG_NUM) return bad("number +- number");
+            return true;
+        case HYK_OP_MUL:
+            if (isT(A) && isT(B)) return bad("time * time");
+            if (A.kind == HYK_ARG_NUM && B.kind == HYK_ARG_NUM) return bad("number * number");
+            return true;
+        case HYK_OP_DIV:
+            if (!((isU(A) && isU(B)) || (isU(A) && isK(B)) || (isK(A) && isU(B)))) return bad("division operands");
+            return true;
+        case HYK_OP_EXP:
+        case HYK_OP_SIN:
+        case HYK_OP_COS:
+            if (!isU(A) && !isT(A)) return bad("constant argument");
+            return true;
+        case HYK_OP_SQUARE:
+        case HYK_OP_SQRT:
+        case HYK_OP_POW:
+        case HYK_OP_LOG:
+            if (!isU(A)) return bad("non-variable argument");
+            return true;
+        default:
+            return bad("operation");
+        }
+    }
+
+    std::string rkey(const Ref &r) const {
+        std::string k = std::to_string(r.kind);
+        if (isU(r)) k += std::string(r.neg ? "n" : "p") + (g.hist[r.u] ? "h" : "c");
+        return k;
+    }
+
+    bool analyse() {
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const uint32_t u = N + k;
+            if (g.alias[u]) continue;
+            if (!supported(u, err)) return false;
+            const auto &op = d.ops[k];
+            const Ref A = g.res(op.a), B = g.res(op.b);
+            int lv = 0;
+            if (isU(A)) lv = std::max(lv, level[A.u]);
+            if (isU(B)) lv = std::max(lv, level[B.u]);
+            level[u] = lv + 1;
+            max_level = std::max(max_level, lv + 1);
+        }
+        levels.assign(max_level, {});
+        std::vector<std::map<std::string, size_t>> index(max_level);
+        for (uint32_t k = 0; k < d.n_ops; ++k) {
+            const uint32_t u = N + k;
+            if (g.alias[u]) continue;
+            const auto &op = d.ops[k];
+            const Ref A = g.res(op.a), B = g.res(op.b);
+            std::string key = "op" + std::to_string(op.op) + "_" + rkey(A) + "_" + rkey(B) + "_c" +
+                              (g.hist[u] ? "h" : "c") + (g.needka[u] ? "k" : "");
+            if (op.op == HYK_OP_POW) {
+                char buf[40];
+                std::snprintf(buf, sizeof buf, "_a%a", op.b.num);
+                key += buf;
+            }
+            if (op.op == HYK_OP_SIN || op.op == HYK_OP_COS) key += (u < (uint32_t)op.aux) ? "_lead" : "_follow";
+            auto &lv = levels[level[u] - 1];
+            auto &ix = index[level[u] - 1];
+            auto it = ix.find(key);
+            if (it == ix.end()) {
+                ix[key] = lv.size();
+                lv.push_back(Group{key, {u}, 0});
+            } else {
+                lv[it->second].members.push_back(u);
+            }
+        }
+        for (auto &lv : levels)
+            std::sort(lv.begin(), lv.end(), [](const Group &x, const Group &y) { return x.key < y.key; });
+        std::map<std::string, size_t> sx;
+        for (uint32_t i = 0; i < N; ++i) {
+            const Ref R = g.res(d.rhs[i]);
+            const std::string key = "upd_" + rkey(R) + (g.needka[i] ? "k" : "");
+            auto it = sx.find(key);
+            if (it == sx.end()) {
+                sx[key] = supd.size();
+                supd.push_back(Group{key, {i}, 0});
+            } else {
+                supd[it->second].members.push_back(i);
+            }
+        }
+        std::sort(supd.begin(), supd.end(), [](const Group &x, const Group &y) { return x.key < y.key; });
+        // Descriptors, group by group.
+        auto slot_of = [&](const Ref &r) {
+            if (isU(r)) return tslot[r.u];
+            if (r.kind == HYK_ARG_PAR) return (int)par_slot + r.par;
+            return 0;
+        };
+        for (auto &lv : levels)
+            for (auto &gr : lv) {
+                gr.off = (uint32_t)descs.size();
+                for (uint32_t u : gr.members) {
+                    const auto &op = d.ops[u - N];
+                    const Ref A = g.res(op.a), B = g.res(op.b);
+                    Desc D;
+                    D.a = slot_of(A);
+                    D.b = slot_of(B);
+                    D.c = tslot[u];
+                    D.ka = isU(A) ? tkslot[A.u] : 0;
+                    D.kc = tkslot[u];
+                    D.inv = tislot[u];
+                    if (op.op == HYK_OP_SIN || op.op == HYK_OP_COS) D.prt = tslot[op.aux];
+                    if (A.kind == HYK_ARG_NUM) D.num = A.num;
+                    if (B.kind == HYK_ARG_NUM && op.op != HYK_OP_POW) D.num = B.num;
+                    descs.push_back(D);
+                }
+                if (d.ops[gr.members[0] - N].op == HYK_OP_POW) {
+                    const double al = d.ops[gr.members[0] - N].b.num;
+                    bool seen = false;
+                    for (double x : alphas) seen = seen || std::memcmp(&x, &al, sizeof al) == 0;
+                    if (!seen) alphas.push_back(al);
+                }
+            }
+        for (auto &gr : supd) {
+            gr.off = (uint32_t)descs.size();
+            for (uint32_t i : gr.members) {
+                const Ref R = g.res(d.rhs[i]);
+                Desc D;
+                D.a = slot_of(R);
+                D.c = tslot[i];
+                D.kc = tkslot[i];
+                if (R.kind == HYK_ARG_NUM) D.num = R.num;
+                descs.push_back(D);
+            }
+        }
+        return true;
+    }
+
+    // Weighted share of busy threads over all rounds of one order for a team of T threads.
+    double util(uint32_t T) const {
+        double work = 0, busy = 0;
+        auto add = [&](const Group &gr, double w) {
+            const double m = (double)gr.members.size();
+            work += m * w;
+            busy += std::ceil(m / T) * T * w;
+        };
+        for (auto &lv : levels)
+            for (auto &gr : lv) {
+                const auto &op = d.ops[gr.members[0] - N];
+                const Ref A = g.res(op.a), B = g.res(op.b);
+                bool conv = false;
+                switch (op.op) {
+                case HYK_OP_MUL: conv = isU(A) && isU(B); break;
+                case HYK_OP_DIV: conv = isU(B); break;
+                case HYK_OP_ADD: case HYK_OP_SUB: conv = false; break;
+                default: conv = true;
+                }
+                add(gr, conv ? 0.5 * p : 1.0);
+            }
+        for (auto &gr : supd) add(gr, 1.0);
+        return busy > 0 ? work / busy : 0.0;
+    }
+
+    // ---- expressions (D = the thread's descriptor, n = the order)
+    static std::string wrap(const Ref &r, const std::string &s) { return r.neg ? "(-" + s + ")" : s; }
+    // Operand coefficient at the current order n (runtime) or at order 0.
+    std::string cur(const Ref &r, char f, bool n0) const {
+        const std::string fld = std::string("D.") + f;
+        switch (r.kind) {
+        case HYK_ARG_U:
+            return wrap(r, (n0 || !g.hist[r.u]) ? "S[" + fld + "]" : "S[" + fld + " + n]");
+        case HYK_ARG_PAR:
+            return n0 ? "S[" + fld + "]" : "";
+        case HYK_ARG_NUM:
+            return n0 ? "D.num" : "";
+        case HYK_ARG_TIME:
+            return n0 ? "t0" : "";  // order n >= 2; order 1 handled by the caller
+        }
+        return "";
+    }
+    // Operand coefficient at order J (expression, a past order: needs the history).
+    std::string at(const Ref &r, char f, const std::string &J) const {
+        return wrap(r, std::string("S[D.") + f + " + " + J + "]");
+    }
+    std::string K(const Ref &r, char f) const { return r.kind == HYK_ARG_NUM ? "D.num" : std::string("S[D.") + f + "]"; }
+
+    void out(uint32_t u, bool n0, const std::string &v) {
+        o << "            const double v = " << v << ";\n";
+        o << "            S[D.c" << ((!n0 && g.hist[u]) ? " + n" : "") << "] = v;\n";
+        if (!n0 && g.needka[u]) o << "            S[D.kc + n - 1] = (double)n * v;\n";
+    }
+
+    void addsub(const std::string &a, const std::string &b, bool add, uint32_t u, bool n0) {
+        std::string v;
+        if (!a.empty() && !b.empty())
+            v = "(" + a + (add ? " + " : " - ") + b + ")";
+        else if (!a.empty())
+            v = a;
+        else if (!b.empty())
+            v = add ? b : "(-" + b + ")";
+        else
+            v = "0.0";
+        out(u, n0, v);
+    }
+
+    void emit_group_op(const Group &gr, bool n0) {
+        const uint32_t u = gr.members[0];
+        const auto &op = d.ops[u - N];
+        const Ref A = g.res(op.a), B = g.res(op.b);
+        const std::string fma_ = "__fma_rn";
+        o << "        // " << gr.key << "\n";
+        o << "#pragma unroll 1\n";
+        o << "        for (int q = r; q < " << gr.members.size() << "; q += HYK_TEAM) {\n";
+        o << "            const hyk_tdesc &D = hyk_td[" << gr.off << " + q];\n";
+        if (n0) {
+            const std::string a = cur(A, 'a', true), b = cur(B, 'b', true);
+            switch (op.op) {
+            case HYK_OP_ADD: out(u, true, "(" + a + " + " + b + ")"); break;
+            case HYK_OP_SUB: out(u, true, "(" + a + " - " + b + ")"); break;
+            case HYK_OP_MUL: out(u, true, a + " * " + b); break;
+            case HYK_OP_DIV:
+                out(u, true, "(" + a + " / " + b + ")");
+                o << "            S[D.inv] = 1.0 / " << b << ";\n";
+                break;
+            case HYK_OP_SQUARE: out(u, true, a + " * " + a); break;
+            case HYK_OP_SQRT:
+                out(u, true, "sqrt(" + a + ")");
+                o << "            S[D.inv] = 1.0 / (2.0 * v);\n";
+                break;
+            case HYK_OP_POW:
+                out(u, true, "hyk_dm_pow(" + a + ", " + lit(op.b.num) + ")");
+                o << "            S[D.inv] = 1.0 / " << a << ";\n";
+                break;
+            case HYK_OP_EXP: out(u, true, "hyk_dm_exp(" + a + ")"); break;
+            case HYK_OP_LOG:
+                out(u, true, "hyk_dm_log(" + a + ")");
+                o << "            S[D.inv] = 1.0 / " << a << ";\n";
+                break;
+            case HYK_OP_SIN:
+            case HYK_OP_COS:
+                if (u < (uint32_t)op.aux) {
+                    o << "            double sv, cv;\n";
+                    o << "            hyk_dm_sincos(" << a << ", &sv, &cv);\n";
+                    o << "            S[D.c] = " << (op.op == HYK_OP_SIN ? "sv" : "cv") << ";\n";
+                    o << "            S[D.prt] = " << (op.op == HYK_OP_SIN ? "cv" : "sv") << ";\n";
+                }
+                break;
+            }
+            o << "        }\n";
+            return;
+        }
+        switch (op.op) {
+        case HYK_OP_ADD:
+        case HYK_OP_SUB: {
+            const bool add = op.op == HYK_OP_ADD;
+            const std::string a = cur(A, 'a', false), b = cur(B, 'b', false);
+            if (isT(A) || isT(B)) {
+                o << "            if (n == 1) {\n";
+                addsub(isT(A) ? "1.0" : a, isT(B) ? "1.0" : b, add, u, false);
+                o << "            } else {\n";
+                addsub(a, b, add, u, false);
+                o << "            }\n";
+            } else {
+                addsub(a, b, add, u, false);
+            }
+            break;
+        }
+        case HYK_OP_MUL:
+            if (isU(A) && isU(B)) {
+                o << "            double acc = " << at(A, 'a', "0") << " * " << at(B, 'b', "n") << ";\n";
+                o << "#pragma unroll 1\n";
+                o << "            for (int j = 1; j <= n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
+                  << at(B, 'b', "n - j") << ", acc);\n";
+                out(u, false, "acc");
+            } else if (isU(A) && isK(B)) {
+                out(u, false, cur(A, 'a', false) + " * " + K(B, 'b'));
+            } else if (isK(A) && isU(B)) {
+                out(u, false, K(A, 'a') + " * " + cur(B, 'b', false));
+            } else if (isU(A) && isT(B)) {
+                o << "            double acc = " << at(A, 'a', "n - 1") << " * 1.0;\n";
+                o << "            acc = " << fma_ << "(" << at(A, 'a', "n") << ", t0, acc);\n";
+                out(u, false, "acc");
+            } else if (isT(A) && isU(B)) {
+                o << "            double acc = t0 * " << at(B, 'b', "n") << ";\n";
+                o << "            acc = " << fma_ << "(1.0, " << at(B, 'b', "n - 1") << ", acc);\n";
+                out(u, false, "acc");
+            } else if (isK(A) && isK(B)) {
+                out(u, false, "0.0");
+            } else if (isK(A) && isT(B)) {
+                out(u, false, "(n == 1 ? " + K(A, 'a') + " * 1.0 : 0.0)");
+            } else {  // time * constant
+                out(u, false, "(n == 1 ? 1.0 * " + K(B, 'b') + " : 0.0)");
+            }
+            break;
+        case HYK_OP_DIV:
+            if (isU(B)) {
+                o << "            double acc = " << at(B, 'b', "1") << " * S[D.c + n - 1];\n";
+                o << "#pragma unroll 1\n";
+                o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << at(B, 'b', "j")
+                  << ", S[D.c + n - j], acc);\n";
+                const std::string a = isU(A) ? cur(A, 'a', false) : "0.0";
+                out(u, false, "((" + a + " - acc) * S[D.inv])");
+            } else {
+                out(u, false, "(" + cur(A, 'a', false) + " * S[D.inv])");
+            }
+            break;
+        case HYK_OP_SQUARE:
+            o << "            double acc = " << at(A, 'a', "0") << " * " << at(A, 'a', "n") << ";\n";
+            o << "#pragma unroll 1\n";
+            o << "            for (int j = 1; 2 * j < n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
+              << at(A, 'a', "n - j") << ", acc);\n";
+            o << "            acc = acc + acc;\n";
+            o << "            if ((n & 1) == 0) acc = " << fma_ << "(" << at(A, 'a', "n / 2") << ", "
+              << at(A, 'a', "n / 2") << ", acc);\n";
+            out(u, false, "acc");
+            break;
+        case HYK_OP_SQRT:
+            o << "            double acc = 0.0;\n";
+            o << "            if (n == 2) {\n";
+            o << "                acc = S[D.c + 1] * S[D.c + 1];\n";
+            o << "            } else if (n > 2) {\n";
+            o << "                acc = S[D.c + 1] * S[D.c + n - 1];\n";
+            o << "#pragma unroll 1\n";
+            o << "                for (int j = 2; 2 * j < n; ++j) acc = " << fma_ << "(S[D.c + j], S[D.c + n - j], acc);\n";
+            o << "                acc = acc + acc;\n";
+            o << "                if ((n & 1) == 0) acc = " << fma_ << "(S[D.c + n / 2], S[D.c + n / 2], acc);\n";
+            o << "            }\n";
+            out(u, false, "(n == 1 ? (" + cur(A, 'a', false) + " * S[D.inv]) : ((" + cur(A, 'a', false) +
+                              " - acc) * S[D.inv]))");
+            break;
+        case HYK_OP_POW: {
+            size_t ai = 0;
+            for (; ai < alphas.size(); ++ai)
+                if (std::memcmp(&alphas[ai], &op.b.num, sizeof(double)) == 0) break;
+            const std::string pc = "hyk_pc" + std::to_string(ai) + "[n * (HYK_ORDER + 1)";
+            o << "            double acc = (" << pc << "] * " << at(A, 'a', "n") << ") * S[D.c];\n";
+            o << "#pragma unroll 1\n";
+            o << "            for (int j = 1; j < n; ++j) acc = " << fma_ << "(" << pc << " + j] * "
+              << at(A, 'a', "n - j") << ", S[D.c + j], acc);\n";
+            out(u, false, "((acc * hyk_invn[n]) * S[D.inv])");
+            break;
+        }
+        case HYK_OP_EXP:
+            if (isT(A)) {  // d(t)/dt = 1: the single term j = 1
+                o << "            const double acc = 1.0 * S[D.c + n - 1];\n";
+                out(u, false, "(acc * hyk_invn[n])");
+                break;
+            }
+            o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.c + n - 1];\n";
+            o << "#pragma unroll 1\n";
+            o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
+              << ", S[D.c + n - j], acc);\n";
+            out(u, false, "(acc * hyk_invn[n])");
+            break;
+        case HYK_OP_LOG:
+            o << "            double acc = 0.0;\n";
+            o << "            if (n >= 2) {\n";
+            o << "                acc = S[D.kc] * " << at(A, 'a', "n - 1") << ";\n";
+            o << "#pragma unroll 1\n";
+            o << "                for (int j = 2; j < n; ++j) acc = " << fma_ << "(S[D.kc + j - 1], " << at(A, 'a', "n - j")
+              << ", acc);\n";
+            o << "            }\n";
+            out(u, false, "(n == 1 ? (" + cur(A, 'a', false) + " * S[D.inv]) : ((" + cur(A, 'a', false) +
+                              " - (acc * hyk_invn[n])) * S[D.inv]))");
+            break;
+        case HYK_OP_SIN:
+        case HYK_OP_COS:
+            if (isT(A)) {
+                o << "            const double acc = 1.0 * S[D.prt + n - 1];\n";
+            } else {
+                o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.prt + n - 1];\n";
+                o << "#pragma unroll 1\n";
+                o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
+                  << ", S[D.prt + n - j], acc);\n";
+            }
+            out(u, false, op.op == HYK_OP_SIN ? "(acc * hyk_invn[n])" : "(-(acc * hyk_invn[n]))");
+            break;
+        }
+        o << "        }\n";
+    }
+
+    void emit_group_upd(const Group &gr, bool n0) {
+        const uint32_t i = gr.members[0];
+        const Ref R = g.res(d.rhs[i]);
+        o << "        // " << gr.key << "\n";
+        o << "#pragma unroll 1\n";
+        o << "        for (int q = r; q < " << gr.members.size() << "; q += HYK_TEAM) {\n";
+        o << "            const hyk_tdesc &D = hyk_td[" << gr.off << " + q];\n";
+        std::string f;
+        if (n0) {
+            f = cur(R, 'a', true);
+        } else if (isU(R)) {
+            f = cur(R, 'a', false);
+        } else if (isT(R)) {
+            f = "(n == 1 ? 1.0 : 0.0)";
+        }
+        const std::string nn = n0 ? "1" : "n + 1";
+        std::string v;
+        if (f.empty())
+            v = "0.0";
+        else if (isT(R) && !n0)
+            v = "(n == 1 ? (1.0 * hyk_invn[2]) : 0.0)";
+        else
+            v = "(" + f + " * hyk_invn[" + nn + "])";
+        o << "            const double v = " << v << ";\n";
+        o << "            S[D.c + " << nn << "] = v;\n";
+        if (g.needka[i]) {
+            if (n0)
+                o << "            if (1 < HYK_ORDER) S[D.kc] = 1.0 * v;\n";
+            else
+                o << "            if (n + 1 < HYK_ORDER) S[D.kc + n] = (double)(n + 1) * v;\n";
+        }
+        o << "        }\n";
+    }
+
+    void emit_order(bool n0) {
+        for (auto &lv : levels) {
+            for (auto &gr : lv) emit_group_op(gr, n0);
+            o << "        __syncwarp();\n";
+        }
+        for (auto &gr : supd) emit_group_upd(gr, n0);
+        o << "        __syncwarp();\n";
+    }
+
+    void emit() {
+        o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, pad;\n    double num;\n};\n";
+        o << "static __device__ const hyk_tdesc hyk_td[" << std::max<size_t>(descs.size(), 1) << "] = {\n";
+        for (const auto &D : descs)
+            o << "    {" << D.a << ", " << D.b << ", " << D.c << ", " << D.ka << ", " << D.kc << ", " << D.inv << ", "
+              << D.prt << ", 0, " << lit(D.num) << "},\n";
+        if (descs.empty()) o << "    {0, 0, 0, 0, 0, 0, 0, 0, 0.0},\n";
+        o << "};\n";
+        o << "static __constant__ double hyk_invn[" << (p + 2) << "] = {0.0";
+        for (uint32_t k = 1; k <= p + 1; ++k) o << ", " << lit(1.0 / (double)k);
+        o << "};\n";
+        for (size_t ai = 0; ai < alphas.size(); ++ai) {
+            const double alpha = alphas[ai];
+            o << "static __device__ const double hyk_pc" << ai << "[" << (p + 1) * (p + 1) << "] = {\n";
+            for (uint32_t n = 0; n <= p; ++n) {
+                o << "   ";
+                for (uint32_t j = 0; j <= p; ++j) {
+                    const double coef = (j < n) ? (double)n * alpha - (double)j * (alpha + 1.0) : 0.0;
+                    o << " " << lit(coef) << ",";
+                }
+                o << "\n";
+            }
+            o << "};\n";
+        }
+        o << "static __device__ __noinline__ void hyk_tjets(double *__restrict__ S, const double t0, const int r) {\n";
+        o << "    __syncwarp();\n";
+        o << "    {\n        // ---- order 0\n";
+        emit_order(true);
+        o << "    }\n";
+        o << "#pragma unroll 1\n";
+        o << "    for (int n = 1; n < HYK_ORDER; ++n) {\n";
+        emit_order(false);
+        o << "    }\n";
+        o << "}\n";
+    }
+};
+
+const char *kCommon =
+#include "kernel_common.inc"
+    ;
+
 const char *kTemplate =
 #include "kernel_template.inc"
+    ;
+
+const char *kTeam =
+#include "kernel_team.inc"
     ;
 
 // hyk_dmath.h as a string (generated at build time from the header).
@@ -942,6 +1489,7 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     }
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << kDmath << "\n";
+    h << kCommon << "\n";
     h << kTemplate << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
     g.emit_jets();
@@ -968,13 +1516,98 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
 }
 
 
-// Host translation unit of the same generated recurrences (forward jets and,
-// with the adjoint, the reverse sweep) for CPU checks of the generator: one
-// lane, HYK_BLK = 1, the CUDA intrinsics mapped to their host equivalents.
-bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err) {
+bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err) {
+    TeamGen tg(d, order);
+    if (!tg.analyse()) {
+        err = tg.err;
+        return false;
+    }
+    info.n_slot = tg.nslot | 1u;
+    for (uint32_t T = 1; T <= 32; T *= 2) info.util[__builtin_ctz(T)] = tg.util(T);
+    return true;
+}
+
+bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
+                   std::string &err) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
+    }
+    if (team < 2 || team > 32 || (team & (team - 1)) || tpb % 32 || tpb == 0) {
+        err = "invalid team geometry";
+        return false;
+    }
+    TeamGen tg(d, order);
+    if (!tg.analyse()) {
+        err = tg.err;
+        return false;
+    }
+    tg.g.emit_jets();  // flop count of the same recurrences
+    const double p = (double)order;
+    const double e1 = std::exp(1.0);
+    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+    const uint32_t nt = tg.nslot | 1u;
+    std::ostringstream h;
+    h << "// Generated by libhyk (team form, " << team << " threads per trajectory): " << d.n_eq << " equations, "
+      << d.n_ops << " u-operations, order " << order << "\n";
+    h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
+      << "\n#define HYK_TPB " << tpb << "\n#define HYK_TEAM " << team << "\n#define HYK_XS " << tg.XS
+      << "\n#define HYK_NT " << nt << "\n#define HYK_NSLOT " << tg.nslot << "\n#define HYK_PAR_SLOT " << tg.par_slot
+      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
+      << lit(1.0 / (p - 1.0)) << "\n";
+    h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
+    h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
+    h << kDmath << "\n";
+    h << kCommon << "\n";
+    h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
+    tg.emit();
+    h << tg.o.str() << "\n";
+    h << kTeam << "\n";
+    out.src = h.str();
+    out.n_slot = nt;
+    out.par_slot = tg.par_slot;
+    out.flops = tg.g.flops + 2.0 * d.n_eq * order + 46.0 + 10.0;
+    return true;
+}
+
+// Host translation unit of the same generated recurrences (forward jets and,
+// with the adjoint, the reverse sweep) for CPU checks of the generator: one
+// lane, HYK_BLK = 1, the CUDA intrinsics mapped to their host equivalents.
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team) {
+    if (order < 2) {
+        err = "the Taylor order must be at least 2";
+        return false;
+    }
+    if (team) {
+        // The team form's recurrences run by a team of one thread.
+        TeamGen tg(d, order);
+        if (!tg.analyse()) {
+            err = tg.err;
+            return false;
+        }
+        std::ostringstream h;
+        h << "#include <cmath>\n#include <cstdint>\n#define __device__\n#define __constant__\n#define __noinline__\n"
+             "#define __forceinline__ inline\n#define __restrict__\n"
+             "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
+             "static inline void __syncwarp() {}\n";
+        h << kDmath << "\n";
+        h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
+          << "\n#define HYK_TEAM 1\n#define HYK_XS " << tg.XS << "\n#define HYK_NSLOT " << tg.nslot
+          << "\n#define HYK_PAR_SLOT " << tg.par_slot << "\n";
+        h << "#define HYK_SX(i, n) S[(i) * HYK_XS + (n)]\n#define HYK_PAR(k) S[HYK_PAR_SLOT + (k)]\n";
+        tg.emit();
+        h << tg.o.str();
+        h << "extern \"C\" int hyk_host_nslot(void) { return HYK_NSLOT; }\n";
+        h << "extern \"C\" void hyk_host_step(double *S, const double *x0, const double *pars, double t0, double h, double *x1) {\n"
+             "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
+             "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
+             "    hyk_tjets(S, t0, 0);\n"
+             "    for (int i = 0; i < HYK_NEQ; ++i) {\n"
+             "        double acc = HYK_SX(i, HYK_ORDER);\n"
+             "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
+             "        x1[i] = acc;\n    }\n}\n";
+        src = h.str();
+        return true;
     }
     Gen g(d, order, false, adjoint);
     const double p = (double)order;

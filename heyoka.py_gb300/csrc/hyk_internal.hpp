@@ -38,7 +38,19 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false);
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
               std::string &err, bool adjoint = false, uint64_t gmem_stride = 0);
 
-// Host (CPU) translation unit of the same recurrences, for checks of the generator.
-bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err);
+// Team form (several threads per trajectory): slot count and the share of
+// busy threads over the rounds of one order for teams of 1, 2, 4, ..., 32.
+struct TeamInfo {
+    uint32_t n_slot = 0;  // doubles per trajectory (padded)
+    double util[6] = {0, 0, 0, 0, 0, 0};
+};
+// false (with the reason) when an operation has no team-form code.
+bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err);
+bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
+                   std::string &err);
+
+// Host (CPU) translation unit of the same recurrences, for checks of the
+// generator (team: the team form's recurrences, run by a team of one).
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team = false);
 
 }  // namespace hyk

@@ -221,6 +221,7 @@ struct hyk_module {
     CUmodule mod = nullptr;
     CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
     int adj_ctas_per_sm = 0;
+    uint32_t team = 0;           // threads per trajectory (team form); 0 = lane form
     bool gmem = false;           // Taylor coefficients in a global buffer (large systems)
     uint64_t gmem_threads = 0;   // threads of the fixed grid in that mode
     CUdeviceptr jets = 0;        // the module's coefficient buffer (gmem mode)
@@ -251,14 +252,58 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const Device &dv = *m->dv;
 
     const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
-    const uint32_t nslot = hyk::count_slots(m->d, order, adjoint);
-    const size_t lane_bytes = (size_t)nslot * sizeof(double);
+    const bool pin = (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0;
+    uint32_t nslot = hyk::count_slots(m->d, order, adjoint);
+    size_t lane_bytes = (size_t)nslot * sizeof(double);
     uint32_t blk = m->cfg.block_lanes;
-    // Systems whose coefficients do not fit 32 lanes of shared memory keep
-    // them in a global buffer owned by the module: one slot stride for the
+
+    // Form.  The lane form (one thread per trajectory) needs 32 lanes of
+    // coefficients per warp in shared memory and at least 4 resident warps
+    // per SM to keep the four FP64 pipes busy.  The team form spreads one
+    // trajectory over 2..32 threads: smaller shared memory per warp, at the
+    // price of idle threads in the rounds of each dependency level.  The
+    // estimate compares busy-thread share x min(1, warps per SM / 4).
+    hyk::TeamInfo ti;
+    std::string terr;
+    const bool team_ok = !adjoint && !pin && hyk::team_layout(m->d, order, ti, terr);
+    const uint32_t want_team = m->cfg.team_size;
+    if (want_team > 32 || (want_team & (want_team - 1)))
+        return fail(HYK_ERR_INVALID, "team_size must be 0, 1 or a power of two up to 32");
+    if (want_team > 1) {
+        if (!team_ok)
+            return fail(HYK_ERR_UNSUPPORTED, std::string("the team form is not available: ") +
+                                                 (adjoint ? "adjoint module" : pin ? "pin arithmetic" : terr));
+        m->team = want_team;
+    } else if (want_team == 0 && team_ok) {
+        const size_t warp_bytes = 32 * lane_bytes;
+        double best = 0.15;  // coefficients in global memory
+        if (warp_bytes <= (size_t)dv.smem_optin) {
+            const double w = (double)((size_t)dv.smem_per_sm / (warp_bytes + 1024));
+            best = std::min(1.0, w / 4.0);
+        }
+        for (uint32_t T = 2, l = 1; T <= 32; T *= 2, ++l) {
+            const size_t cta = (size_t)(32 / T) * ti.n_slot * sizeof(double);
+            if (cta > (size_t)dv.smem_optin) continue;
+            const double w = (double)((size_t)dv.smem_per_sm / (cta + 1024));
+            const double score = ti.util[l] * std::min(1.0, w / 4.0) * 0.85;
+            if (score > best) {
+                best = score;
+                m->team = T;
+            }
+        }
+    }
+    if (m->team) {
+        if (blk == 0) blk = 32;
+        nslot = ti.n_slot;
+        lane_bytes = (size_t)nslot * sizeof(double);
+    }
+    // Lane form of a system whose coefficients do not fit 32 lanes of shared
+    // memory: a global buffer owned by the module, one slot stride for the
     // whole fixed grid, so a warp still reads 32 consecutive doubles.
-    m->gmem = lane_bytes * 32 > (size_t)dv.smem_optin;
-    if (m->gmem) {
+    m->gmem = !m->team && lane_bytes * 32 > (size_t)dv.smem_optin;
+    if (m->team) {
+        // one CTA per warp by default: finest packing of the shared memory
+    } else if (m->gmem) {
         if (blk == 0) blk = 128;
         const uint32_t ctas = m->cfg.persist_ctas ? m->cfg.persist_ctas : 1;
         m->gmem_threads = (uint64_t)dv.n_sm * ctas * blk;
@@ -289,14 +334,16 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (blk % 32 != 0 || blk > 1024) return fail(HYK_ERR_INVALID, "block_lanes must be a multiple of 32, <= 1024");
     m->blk = blk;
     m->nslot = nslot;
-    m->smem = m->gmem ? 0 : (size_t)blk * lane_bytes;
+    m->smem = m->gmem ? 0 : m->team ? (size_t)(blk / m->team) * lane_bytes : (size_t)blk * lane_bytes;
     if (m->smem > (size_t)dv.smem_optin)
         return fail(HYK_ERR_UNSUPPORTED, "shared memory per CTA (" + std::to_string(m->smem) + ") exceeds the device limit");
 
     hyk::GenOut g;
-    if (!hyk::generate(m->d, order, (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0, blk, sizeof(KParams), g, err, adjoint,
-                       m->gmem ? m->gmem_threads : 0))
+    if (m->team) {
+        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err)) return fail(HYK_ERR_INVALID, err);
+    } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0)) {
         return fail(HYK_ERR_INVALID, err);
+    }
     if (g.n_slot != nslot) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
     m->src = g.src;
     m->flops = g.flops;
@@ -391,6 +438,7 @@ int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info) {
     info->n_u = m->d.n_u();
     info->block_lanes = m->blk;
     info->smem_per_lane = m->gmem ? 0u : m->nslot * 8;
+    info->team_size = m->team ? m->team : 1;
     info->regs_per_thread = (uint32_t)m->regs;
     info->ctas_per_sm = (uint32_t)m->ctas_per_sm;
     info->n_sm = (uint32_t)m->dv->n_sm;
@@ -421,6 +469,13 @@ static void fill_lanes(KParams &k, const hyk_lanes_t *l) {
     k.t_lo = l->time_lo;
 }
 
+// Blocks covering n trajectories: blk of them per block in the lane form,
+// blk / team in the team form.
+static uint64_t lane_blocks(const hyk_module *m, uint64_t n) {
+    const uint64_t per = m->team ? m->blk / m->team : m->blk;
+    return (n + per - 1) / per;
+}
+
 static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k, void *stream) {
     if (grid == 0) return 0;
     k.jets = reinterpret_cast<double *>(m->jets);
@@ -446,7 +501,7 @@ int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t,
     k.step_oc = outcome;
     k.step_h = h;
     k.step_tc = tc;
-    return launch(m, m->f_step, (lanes->n_lanes + m->blk - 1) / m->blk, m->blk, m->smem, k, stream);
+    return launch(m, m->f_step, lane_blocks(m, lanes->n_lanes), m->blk, m->smem, k, stream);
 }
 
 static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const hyk_prop_t *p) {
@@ -543,7 +598,7 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (check_every == 0) check_every = 16;
     k.persistent = 0;
     k.iters_per_launch = 1;
-    const uint64_t grid = (lanes->n_lanes + m->blk - 1) / m->blk;
+    const uint64_t grid = lane_blocks(m, lanes->n_lanes);
     rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
     if (rc) return rc;
     uint64_t n = 0;
@@ -632,11 +687,22 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     // The same choice as the runtime: coefficients in global memory when 32
     // lanes do not fit the opt-in shared memory of an SM (227 KB), with the
     // slot stride of a 152-SM grid.
+    const uint32_t team = cfg ? cfg->team_size : 0;
+    if (team > 1 && verbose == 3) {  // host translation unit of the team form
+        std::string hs;
+        if (!hyk::generate_host(d, order, false, hs, err, true)) return fail(HYK_ERR_UNSUPPORTED, err);
+        if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
+        return 0;
+    }
     const uint32_t slots = hyk::count_slots(d, order, adjoint);
     const uint64_t gstride = (uint64_t)slots * 8 * 32 > 227u * 1024 ? 152ull * blk : 0;
     hyk::GenOut g;
-    if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride))
+    if (team > 1) {
+        if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : 32, sizeof(KParams), g, err))
+            return fail(HYK_ERR_UNSUPPORTED, err);
+    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride)) {
         return fail(HYK_ERR_INVALID, err);
+    }
     if (n_slot) *n_slot = g.n_slot;
     if (flops) *flops = g.flops;
     if (verbose == 3) {  // host translation unit (CPU checks of the generator)

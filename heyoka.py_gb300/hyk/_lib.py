@@ -40,7 +40,7 @@ class hyk_config_t(ctypes.Structure):
         ("block_lanes", c_u32),
         ("persist_ctas", c_u32),
         ("flags", c_u32),
-        ("reserved", c_u32),
+        ("team_size", c_u32),
     ]
 
 
@@ -58,6 +58,8 @@ class hyk_module_info_t(ctypes.Structure):
         ("reserved", c_u32),
         ("flops_per_step", c_d),
         ("compile_seconds", c_d),
+        ("team_size", c_u32),
+        ("reserved2", c_u32),
     ]
 
 

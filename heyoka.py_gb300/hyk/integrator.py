@@ -143,6 +143,7 @@ class taylor_adaptive_batch:
         block_lanes=0,
         pin_arith=False,
         schedule="lpt",
+        team_size=0,
         **kwargs,
     ):
         for k in list(kwargs):
@@ -225,7 +226,7 @@ class taylor_adaptive_batch:
         self._order = order_from_tol(tol)
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
-        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith)
+        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)

@@ -99,10 +99,11 @@ typedef struct hyk_decomp {
 typedef struct hyk_module hyk_module;
 
 typedef struct hyk_config {
-    uint32_t block_lanes;  /* lanes (threads) per CTA; 0 = autotune */
+    uint32_t block_lanes;  /* threads per CTA; 0 = autotune */
     uint32_t persist_ctas; /* CTAs per SM of the persistent kernel; 0 = occupancy-derived */
     uint32_t flags;        /* HYK_CFG_* */
-    uint32_t reserved;
+    uint32_t team_size;    /* threads per trajectory: 0 = chosen per system, 1 = one thread per
+                              trajectory (lane form), 2..32 (power of two) = team form */
 } hyk_config_t;
 
 #define HYK_CFG_PIN_ARITH 1u /* oracle "pin" arithmetic: no FMA, divide by n (slower; for cross-checks) */
@@ -120,6 +121,8 @@ typedef struct hyk_module_info {
     uint32_t reserved;
     double flops_per_step;       /* algorithmic FP64 flops of one Taylor step of one lane */
     double compile_seconds;
+    uint32_t team_size;          /* threads per trajectory (1 = lane form) */
+    uint32_t reserved2;
 } hyk_module_info_t;
 
 /* Decompose-compile-load.  Replaces the construction of

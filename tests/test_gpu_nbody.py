@@ -22,11 +22,24 @@ def _case(n, t_scale, seed=21):
     return st, grid
 
 
-def test_oss_uses_global_jets(libhyk):
+def test_oss_form_choice(libhyk):
+    # Automatic choice: the team form (one trajectory per team of threads,
+    # coefficients in shared memory).  The lane form of this system keeps its
+    # coefficients in global memory.
     ta = hyk.taylor_adaptive_batch(W.oss_sys(), W.oss_ics(8)[0], tol=1e-15)
     info = ta.module_info
-    assert info["n_eq"] == 36
-    assert info["smem_per_lane"] == 0
+    assert info["n_eq"] == 36 and info["team_size"] > 1 and info["smem_per_lane"] > 0
+    lane = hyk.taylor_adaptive_batch(W.oss_sys(), W.oss_ics(8)[0], tol=1e-15, team_size=1)
+    assert lane.module_info["team_size"] == 1 and lane.module_info["smem_per_lane"] == 0
+
+
+def test_oss_global_jets_lane_form_bitwise(oracle):
+    st, grid = _case(24, 0.05, seed=24)
+    ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=1)
+    _, out = ta.propagate_grid(grid)
+    o = oracle.Oracle(W.oss_sys(), st, order=ta.order, mode=1)
+    r = o.propagate_grid(grid)
+    assert np.array_equal(out, r["grid"])
 
 
 @pytest.mark.parametrize("mode", ["persistent", "plain"])
