@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
+    ap.add_argument("--members", type=int, default=65536, help="oss: ensemble members")
     ap.add_argument("--team-size", type=int, default=0,
                     help="threads per trajectory (0: chosen per system, 1: lane form, 2..32: team form)")
     return ap.parse_args()
@@ -378,8 +379,11 @@ def run_cr3bp_adjoint(args):
 def run_oss(args):
     """Outer-solar-system 6-body ensemble: 65536 members, tol 1e-15 (order
     19), end times log-uniform in [1e3, 1e5] days, propagate_grid over 100
-    points per member.  The system is too large for shared memory, so its
-    Taylor coefficients live in the module's global buffer."""
+    points per member.  value: the device-resident call (grid and state in
+    HBM, output left on the device); kernel: the propagation launch alone
+    (CUDA events on its stream); e2e: the public propagate_grid with the
+    state and grid copied in from pinned host memory and the (100, 36,
+    65536) output copied back to the host."""
     import numpy as np
     import torch
 
@@ -387,51 +391,70 @@ def run_oss(args):
     import pyoracle
     from hyk import workloads as W
 
-    n = 65536
+    n = args.members
     st, t_end = W.oss_ics(n, seed=2)
     grid = np.linspace(0.0, 1.0, 100).reshape(-1, 1) * t_end.reshape(1, -1)
     ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=args.team_size)
     gd = torch.tensor(grid, device="cuda")
     sd = torch.tensor(st, device="cuda")
-    ta.propagate_grid(gd[:, :].clone() * 1e-3)  # warm-up: compile, short run
-    times, walls = [], []
+    g_host = torch.tensor(grid).pin_memory()
+    s_host = torch.tensor(st).pin_memory()
+    for _ in range(max(3, args.warmup)):
+        ta.set_time(0.0)
+        ta.state[:] = sd
+        ta.propagate_grid_tensor(gd * 1e-2)
+    times, ktimes, e2e = [], [], []
     mon = Clocks(0)
     for _ in range(max(1, args.steps)):
         ta.set_time(0.0)
         ta.state[:] = sd
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        w0 = time.perf_counter()
+        kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ta._launch_events = kev
         e0.record()
-        ta.propagate_grid(gd)
+        out = ta.propagate_grid_tensor(gd)
         e1.record()
         torch.cuda.synchronize()
-        walls.append(time.perf_counter() - w0)
+        ta._launch_events = None
         times.append(e0.elapsed_time(e1) / 1e3)
-    clocks = mon.stop()
+        ktimes.append(kev[0].elapsed_time(kev[1]) / 1e3)
     steps = int(ta.propagate_res_tensors["n_steps"].sum().item())
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        ta.set_time(0.0)
+        ta.state[:] = s_host.to("cuda", non_blocking=True)
+        _, out_np = ta.propagate_grid(g_host.to("cuda", non_blocking=True))
+        e2e.append(time.perf_counter() - w0)
+    clocks = mon.stop()
     info = ta.module_info
-    t_dev = float(np.median(times))
+    t_dev, t_k, t_e2e = float(np.median(times)), float(np.median(ktimes)), float(np.median(e2e))
     # CPU sample: 96 members through the oracle port, reference arithmetic.
     pick = np.linspace(0, n - 1, 96).astype(np.int64)
     c0 = time.perf_counter()
     o = pyoracle.Oracle(W.oss_sys(), st[:, pick], order=ta.order, mode=0)
     r = o.propagate_grid(grid[:, pick])
     cwall = time.perf_counter() - c0
-    fl = info["flops_per_step"] * steps / t_dev
+    fl = info["flops_per_step"] * steps / t_k
     peak = hyk.fp64_peak(0, 300.0)
+    h2d = st.nbytes + grid.nbytes
     line = {
         "metric": "FP64 Taylor trajectory-steps/s, outer-solar-system 6-body ensemble (65536 members, tol 1e-15, "
                   "propagate_grid 100 points, end times log-uniform [1e3,1e5] days)",
-        "value": steps / t_dev, "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
-        "data": "synthetic (near-circular orbits, 1e-6 relative Gaussian perturbations, seed 2)",
-        "config": {"workload": "oss-6body-65536 propagate_grid", "order": ta.order,
+        "value": steps / t_dev, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic (near-circular orbits, 1e-6 relative Gaussian perturbations, seed 2)",
+        "config": {"workload": "oss-6body-{} propagate_grid".format(n), "order": ta.order,
                    "threads_per_trajectory": info["team_size"],
                    "jets": "global memory" if info["smem_per_lane"] == 0 else "shared memory",
-                   "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"]},
-        "trajectory_steps": steps, "device_s": t_dev, "wall_s": float(np.median(walls)),
+                   "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"],
+                   "l2": "inputs and the 1.9 GB output exceed L2"},
+        "trajectory_steps": steps, "device_s": t_dev, "kernel_s": t_k,
+        "e2e": {"value": steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": int(out_np.nbytes)},
         "roofline": {"bound": "fp64", "achieved": fl / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-                     "frac": fl / peak, "traffic": None},
+                     "frac": fl / peak, "traffic": None,
+                     "note": "flops_per_step x trajectory-steps / propagation-kernel time; peak = in-process FP64 FMA probe"},
         "cpu_baseline": {"value": float(r["n_steps"].sum()) / cwall, "unit": UNIT, "cores": 1, "kind": "port",
                          "sample": "96 of the 65536 members (evenly spaced), full horizons, one thread"},
         "clocks": clocks,

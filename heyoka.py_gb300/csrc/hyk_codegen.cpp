@@ -30,6 +30,7 @@
 // oracle's "pin" mode.
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -932,6 +933,9 @@ struct TeamGen {
     std::vector<double> alphas;              // distinct pow exponents
     std::string err;
     std::ostringstream o;
+    // Unrolling of the convolution loops over j (the same sequence of fused
+    // multiply-adds, with the operand loads of later terms hoisted).
+    int ju = 4;
 
     TeamGen(const Dec &dd, uint32_t order)
         : g(dd, order, false, false), d(dd), p(order), N(dd.n_eq), NU(dd.n_u()) {
@@ -1245,7 +1249,7 @@ struct TeamGen {
         case HYK_OP_MUL:
             if (isU(A) && isU(B)) {
                 o << "            double acc = " << at(A, 'a', "0") << " * " << at(B, 'b', "n") << ";\n";
-                o << "#pragma unroll 1\n";
+                o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 1; j <= n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
                   << at(B, 'b', "n - j") << ", acc);\n";
                 out(u, false, "acc");
@@ -1272,7 +1276,7 @@ struct TeamGen {
         case HYK_OP_DIV:
             if (isU(B)) {
                 o << "            double acc = " << at(B, 'b', "1") << " * S[D.c + n - 1];\n";
-                o << "#pragma unroll 1\n";
+                o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << at(B, 'b', "j")
                   << ", S[D.c + n - j], acc);\n";
                 const std::string a = isU(A) ? cur(A, 'a', false) : "0.0";
@@ -1283,7 +1287,7 @@ struct TeamGen {
             break;
         case HYK_OP_SQUARE:
             o << "            double acc = " << at(A, 'a', "0") << " * " << at(A, 'a', "n") << ";\n";
-            o << "#pragma unroll 1\n";
+            o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 1; 2 * j < n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
               << at(A, 'a', "n - j") << ", acc);\n";
             o << "            acc = acc + acc;\n";
@@ -1297,7 +1301,7 @@ struct TeamGen {
             o << "                acc = S[D.c + 1] * S[D.c + 1];\n";
             o << "            } else if (n > 2) {\n";
             o << "                acc = S[D.c + 1] * S[D.c + n - 1];\n";
-            o << "#pragma unroll 1\n";
+            o << "#pragma unroll " << ju << "\n";
             o << "                for (int j = 2; 2 * j < n; ++j) acc = " << fma_ << "(S[D.c + j], S[D.c + n - j], acc);\n";
             o << "                acc = acc + acc;\n";
             o << "                if ((n & 1) == 0) acc = " << fma_ << "(S[D.c + n / 2], S[D.c + n / 2], acc);\n";
@@ -1311,7 +1315,7 @@ struct TeamGen {
                 if (std::memcmp(&alphas[ai], &op.b.num, sizeof(double)) == 0) break;
             const std::string pc = "hyk_pc" + std::to_string(ai) + "[n * (HYK_ORDER + 1)";
             o << "            double acc = (" << pc << "] * " << at(A, 'a', "n") << ") * S[D.c];\n";
-            o << "#pragma unroll 1\n";
+            o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 1; j < n; ++j) acc = " << fma_ << "(" << pc << " + j] * "
               << at(A, 'a', "n - j") << ", S[D.c + j], acc);\n";
             out(u, false, "((acc * hyk_invn[n]) * S[D.inv])");
@@ -1324,7 +1328,7 @@ struct TeamGen {
                 break;
             }
             o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.c + n - 1];\n";
-            o << "#pragma unroll 1\n";
+            o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
               << ", S[D.c + n - j], acc);\n";
             out(u, false, "(acc * hyk_invn[n])");
@@ -1333,7 +1337,7 @@ struct TeamGen {
             o << "            double acc = 0.0;\n";
             o << "            if (n >= 2) {\n";
             o << "                acc = S[D.kc] * " << at(A, 'a', "n - 1") << ";\n";
-            o << "#pragma unroll 1\n";
+            o << "#pragma unroll " << ju << "\n";
             o << "                for (int j = 2; j < n; ++j) acc = " << fma_ << "(S[D.kc + j - 1], " << at(A, 'a', "n - j")
               << ", acc);\n";
             o << "            }\n";
@@ -1346,7 +1350,7 @@ struct TeamGen {
                 o << "            const double acc = 1.0 * S[D.prt + n - 1];\n";
             } else {
                 o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.prt + n - 1];\n";
-                o << "#pragma unroll 1\n";
+                o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
                   << ", S[D.prt + n - j], acc);\n";
             }
@@ -1542,6 +1546,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
         err = tg.err;
         return false;
     }
+    if (const char *e = std::getenv("HYK_TEAM_UNROLL")) tg.ju = std::max(1, std::min(16, std::atoi(e)));
     tg.g.emit_jets();  // flop count of the same recurrences
     const double p = (double)order;
     const double e1 = std::exp(1.0);

@@ -41,6 +41,24 @@ def _host_copy(ta):
     return new
 
 
+def _clone_host(tmpl):
+    # A fresh host copy from the host template: CPU tensor clones only (the
+    # device is read once per ensemble, not once per iteration).
+    new = object.__new__(type(tmpl))
+    for k, v in tmpl.__dict__.items():
+        new.__dict__[k] = v.clone() if isinstance(v, torch.Tensor) else v
+    return new
+
+
+def _split(t, n_iter, B):
+    """Per-iteration contiguous blocks of a lane-minor device tensor (..., n_iter * B),
+    made by one permuting copy instead of one copy per iteration."""
+    lead = t.shape[:-1]
+    v = t.reshape(*lead, n_iter, B)
+    k = len(lead)
+    return v.permute(k, *range(k), k + 1).contiguous()
+
+
 def _validate(tp, arg, n_iter, kwargs):
     if not isinstance(n_iter, int):
         raise TypeError(
@@ -96,7 +114,8 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     if n_iter == 0:
         return []
     B = ta.batch_size
-    copies = [gen(_host_copy(ta), i) for i in range(n_iter)]
+    tmpl = _host_copy(ta)
+    copies = [gen(_clone_host(tmpl), i) for i in range(n_iter)]
     for c in copies:
         if not isinstance(c, taylor_adaptive_batch) or c.batch_size != B or c._dec is not ta._dec:
             raise TypeError("the ensemble generator must return the integrator it was given")
@@ -105,7 +124,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     big = object.__new__(type(ta))
     big.__dict__.update(ta.__dict__)
     big._B = n_iter * B
-    cat = lambda name: torch.cat([getattr(c, name).to(dev) for c in copies], dim=-1).contiguous()  # noqa: E731
+    cat = lambda name: torch.cat([getattr(c, name).cpu() for c in copies], dim=-1).to(dev).contiguous()  # noqa: E731
     big._state = cat("_state")
     big._pars = cat("_pars")
     big._thi = cat("_thi")
@@ -139,25 +158,26 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
         res = big._run(tf_hi, tf_lo, ms, md, write_tc=bool(kwargs.get("write_tc", False)),
                        c_output=bool(kwargs.get("c_output", False)), group=B)
     big._refresh_final_tc()
+    parts = {name: _split(getattr(big, name), n_iter, B) for name in ("_state", "_pars", "_thi", "_tlo", "_last_h", "_tc", "_d_out")}
+    prop = {k: (None if v is None else _split(v, n_iter, B)) for k, v in big._prop.items()}
+    grid_np = None
+    if tp == "grid":
+        g = res["grid_out"].cpu().numpy()
+        grid_np = g.reshape(g.shape[0], g.shape[1], n_iter, B)
     out = []
     for i, c in enumerate(copies):
         sl = slice(i * B, (i + 1) * B)
         ti = object.__new__(type(ta))
         ti.__dict__.update(c.__dict__)
         ti._tdev = dev
-        ti._state = big._state[:, sl].contiguous()
-        ti._pars = big._pars[:, sl].contiguous()
-        ti._thi = big._thi[sl].contiguous()
-        ti._tlo = big._tlo[sl].contiguous()
-        ti._last_h = big._last_h[sl].contiguous()
-        ti._tc = big._tc[:, :, sl].contiguous()
-        ti._d_out = big._d_out[:, sl].contiguous()
-        ti._prop = {k: (None if v is None else v[sl].contiguous()) for k, v in big._prop.items()}
+        for name, v in parts.items():
+            ti.__dict__[name] = v[i]
+        ti._prop = {k: (None if v is None else v[i]) for k, v in prop.items()}
         ti._step_res = None
         ti._final_tc_mask = None
         ti._launch_events = None
         if tp == "grid":
-            out.append((ti, None, res["grid_out"][:, :, sl].cpu().numpy()))
+            out.append((ti, None, np.ascontiguousarray(grid_np[:, :, i, :])))
         else:
             c_out = None
             if "c_output" in res:

@@ -708,6 +708,11 @@ class taylor_adaptive_batch:
         """Propagate over a per-lane time grid of shape ``(n, batch_size)``;
         returns ``(None, out)`` with ``out`` of shape ``(n, dim, batch_size)``
         (reference: heyoka/expose_batch_integrators.cpp:315-392)."""
+        return (None, self.propagate_grid_tensor(grid, max_steps, max_delta_t, callback).cpu().numpy())
+
+    def propagate_grid_tensor(self, grid, max_steps=0, max_delta_t=[], callback=None):  # noqa: B006
+        """``propagate_grid`` with the output left on the device: a float64
+        CUDA tensor of shape ``(n, dim, batch_size)``."""
         md = self._check_prop_args(max_delta_t, callback)
         g = np.asarray(grid) if not isinstance(grid, torch.Tensor) else grid
         if g.ndim != 2:
@@ -741,7 +746,7 @@ class taylor_adaptive_batch:
                 raise ValueError("A non-monotonic time grid was passed to propagate_grid()")
         tf = gd[-1].contiguous()
         r = self._run(tf, None, max_steps, md, grid=gd)
-        return (None, r["grid_out"].cpu().numpy())
+        return r["grid_out"]
 
     # ------------------------------------------------------------------ copies
     def __copy__(self):
