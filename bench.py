@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="kepler", choices=["kepler", "serve", "pendulum", "cr3bp-adjoint", "oss"],
+    ap.add_argument("--workload", default="kepler", choices=["kepler", "serve", "pendulum", "cr3bp-adjoint", "oss", "forms"],
                     help="kepler: the headline metric; serve: the Poisson request stream (p50/p99 latency); "
                          "pendulum: 4096 trajectories through ensemble_propagate_until; "
                          "cr3bp-adjoint: 65536 trajectories forward plus discrete adjoint")
@@ -462,6 +462,47 @@ def run_oss(args):
     print(json.dumps(line), flush=True)
 
 
+def run_forms(args):
+    """Lane form against team form (threads per trajectory) on three systems:
+    propagate_until of 65536 outer-solar-system members to t = 2e4 days,
+    65536 CR3BP trajectories to t = 50 and 262144 Kepler orbits to t = 50;
+    one JSON line per (system, form), best of two timed calls."""
+    import numpy as np
+    import torch
+
+    import hyk
+    from hyk import workloads as W
+
+    peak = hyk.fp64_peak(0, 300.0)
+    n = 65536
+    cases = [
+        ("oss", W.oss_sys(), W.oss_ics(n, seed=2)[0], None, 2e4, [0, 1, 4, 8, 16, 32]),
+        ("cr3bp", W.cr3bp_sys()) + W.cr3bp_ics(n, seed=3) + (50.0, [0, 1, 2, 4, 8]),
+        ("kepler", W.kepler_sys(), W.kepler_ics(4 * n, seed=1), None, 50.0, [0, 1, 2, 4]),
+    ]
+    for name, sys_, st, pars, tf, teams in cases:
+        s0 = torch.tensor(st, device="cuda")
+        for T in teams:
+            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=1e-15, team_size=T)
+            info = ta.module_info
+            ta.propagate_until(tf * 0.01)
+            best = 1e30
+            for _ in range(2):
+                ta.set_time(0.0)
+                ta.state[:] = s0
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                ta.propagate_until(tf)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            steps = int(ta.propagate_res_tensors["n_steps"].sum().item())
+            fl = info["flops_per_step"] * steps / best
+            print(json.dumps({"system": name, "requested_team_size": T, "team_size": info["team_size"],
+                              "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"],
+                              "regs": info["regs_per_thread"], "s": best, "trajectory_steps_per_s": steps / best,
+                              "fp64_frac_of_measured": fl / peak}), flush=True)
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -470,7 +511,8 @@ def main():
         return
     if args.workload != "kepler":
         if rank == 0:
-            {"serve": run_serve, "pendulum": run_pendulum, "cr3bp-adjoint": run_cr3bp_adjoint, "oss": run_oss}[args.workload](args)
+            {"serve": run_serve, "pendulum": run_pendulum, "cr3bp-adjoint": run_cr3bp_adjoint, "oss": run_oss,
+             "forms": run_forms}[args.workload](args)
         return
     import numpy as np
     import torch
