@@ -40,6 +40,20 @@
 
 #include "hyk_internal.hpp"
 
+// hyk_ev_btab (the Bernstein conversion table printed into event kernels)
+#define HYK_DM_FN static inline
+#define HYK_DM_FMA(a, b, c) std::fma((a), (b), (c))
+#define HYK_DM_BITS(x) hyk_host_bits_(x)
+static inline unsigned long long hyk_host_bits_(double x) {
+    unsigned long long u;
+    std::memcpy(&u, &x, sizeof u);
+    return u;
+}
+#include "hyk_events.h"
+#undef HYK_DM_FN
+#undef HYK_DM_FMA
+#undef HYK_DM_BITS
+
 namespace hyk {
 
 bool load_dec(const hyk_decomp_t *d, Dec &out, std::string &err) {
@@ -111,6 +125,20 @@ bool load_dec(const hyk_decomp_t *d, Dec &out, std::string &err) {
             err = "invalid right-hand side";
             return false;
         }
+    out.ev.clear();
+    if (d->n_ev > 0) {
+        if (!d->ev) {
+            err = "invalid decomposition: null events";
+            return false;
+        }
+        out.ev.assign(d->ev, d->ev + d->n_ev);
+        for (const auto &e : out.ev)
+            if (!chk(e.g, nu) || e.g.kind == HYK_ARG_NONE || (e.terminal != 0 && e.terminal != 1) || e.direction < -1 ||
+                e.direction > 1 || !(e.cooldown == e.cooldown)) {
+                err = "invalid event";
+                return false;
+            }
+    }
     return true;
 }
 
@@ -157,9 +185,17 @@ struct Gen {
     bool split = false;
     std::vector<int> islot;
 
+    // Events: every order's coefficient of each event function in its own
+    // slots (evslot + k (p+1) + n), the histories kept up to order p-1 (as
+    // for the adjoint), and an extra order-p pass over the operations the
+    // event functions depend on.
+    bool evx = false;
+    uint32_t evslot = 0;
+    std::vector<char> cone;
+
     Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false)
         : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint),
-          split((uint64_t)dd.n_ops * order > 3000) {
+          split((uint64_t)dd.n_ops * order > 3000), evx(!dd.ev.empty()) {
         base.resize(NU);
         negf.assign(NU, 0);
         alias.assign(NU, 0);
@@ -274,7 +310,8 @@ struct Gen {
             s += p + 1;
         }
         // The adjoint module keeps every history up to order p-1.
-        const uint32_t hl = adj ? p : (p >= 2 ? p - 1 : 1), kl = adj ? p - 1 : (p >= 3 ? p - 2 : 0);
+        const bool ext = adj || evx;
+        const uint32_t hl = ext ? p : (p >= 2 ? p - 1 : 1), kl = ext ? p - 1 : (p >= 3 ? p - 2 : 0);
         for (uint32_t u = N; u < NU; ++u)
             if (hist[u] && !alias[u]) {
                 slot[u] = (int)s;
@@ -294,6 +331,25 @@ struct Gen {
             }
         par_slot = s;
         s += d.n_pars;
+        if (evx) {
+            evslot = s;
+            s += (uint32_t)d.ev.size() * (p + 1);
+            // The operations the event functions depend on (through u-variable
+            // arguments, aliases resolved), for the order-p pass.
+            cone.assign(NU, 0);
+            std::vector<uint32_t> stack;
+            for (const auto &e : d.ev)
+                if (e.g.kind == HYK_ARG_U) stack.push_back((uint32_t)base[e.g.idx]);
+            while (!stack.empty()) {
+                const uint32_t u = stack.back();
+                stack.pop_back();
+                if (u < N || cone[u]) continue;
+                cone[u] = 1;
+                const auto &op = d.ops[u - N];
+                for (const hyk_arg_t *a : {&op.a, &op.b})
+                    if (a->kind == HYK_ARG_U) stack.push_back((uint32_t)base[a->idx]);
+            }
+        }
         if (adj) {
             // Adjoint accumulators: orders 0..p of every history, of every j*a_j.
             abase = s;
@@ -419,7 +475,7 @@ struct Gen {
     void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
 
     void store_hist(uint32_t u, uint32_t n) {
-        const uint32_t lim = adj ? p : p - 1;  // stored orders: 0..lim-1
+        const uint32_t lim = (adj || evx) ? p : p - 1;  // stored orders: 0..lim-1
         if (u >= N && hist[u] && n + 1 <= lim) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
         if (needka[u] && n >= 1) {
             o << "    const double " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
@@ -620,7 +676,8 @@ struct Gen {
             o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
             for (uint32_t i = 0; i < N; ++i) o << "    const double " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
         }
-        for (uint32_t n = 0; n < p; ++n) {
+        const uint32_t last = evx ? p : p - 1;  // order p: the event functions' cone only
+        for (uint32_t n = 0; n <= last; ++n) {
             if (split) {
                 o << "static __device__ __noinline__ void hyk_jets_o" << n
                   << "(double *__restrict__ S, const double t0) {\n";
@@ -637,9 +694,18 @@ struct Gen {
             }
             o << "    // ---- order " << n << "\n";
             for (uint32_t k = 0; k < d.n_ops; ++k) {
-                emit_op(k, n);
                 const uint32_t u = N + k;
+                if (n == p && !cone[u]) continue;
+                emit_op(k, n);
                 if (!alias[u]) store_hist(u, n);
+            }
+            for (size_t k = 0; k < d.ev.size(); ++k) {
+                const std::string f = cf(res(d.ev[k].g), n, n);
+                o << "    " << smem(evslot + (uint32_t)k * (p + 1) + n) << " = " << (f.empty() ? "0.0" : f) << ";\n";
+            }
+            if (n == p) {
+                if (split) o << "}\n";
+                continue;
             }
             for (uint32_t i = 0; i < N; ++i) {
                 const Ref r = res(d.rhs[i]);
@@ -650,7 +716,7 @@ struct Gen {
                     o << "    const double " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
                       << vname(i, n + 1) << ";\n";
                     flops += 1;
-                    if (kslot[i] >= 0 && n + 1 + (adj ? 1u : 2u) <= p)
+                    if (kslot[i] >= 0 && n + 1 + ((adj || evx) ? 1u : 2u) <= p)
                         o << "    " << smem((uint32_t)kslot[i] + n) << " = " << kname(i, n + 1) << ";\n";
                 }
             }
@@ -661,9 +727,36 @@ struct Gen {
         }
         if (split) {
             o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
-            for (uint32_t n = 0; n < p; ++n) o << "    hyk_jets_o" << n << "(S, t0);\n";
+            for (uint32_t n = 0; n <= last; ++n) o << "    hyk_jets_o" << n << "(S, t0);\n";
         }
         o << "}\n";
+    }
+
+    // Constants of the events for the kernel template.
+    void emit_events(std::ostream &h) const {
+        const size_t m = d.ev.size();
+        uint32_t nt = 0;
+        for (const auto &e : d.ev) nt += e.terminal ? 1u : 0u;
+        h << "#define HYK_NEV " << m << "\n#define HYK_NTEV " << nt << "\n#define HYK_EV_SLOT " << evslot << "\n";
+        if (!m) return;
+        h << "#define HYK_EVC(k, n) S[(HYK_EV_SLOT + (k) * (HYK_ORDER + 1) + (n)) * HYK_STRIDE]\n";
+        std::vector<int> idx(m);
+        uint32_t it = 0, in = 0;
+        for (size_t k = 0; k < m; ++k) idx[k] = d.ev[k].terminal ? (int)it++ : (int)in++;
+        auto arr = [&](const char *type, const char *name, auto f) {
+            h << "static __constant__ " << type << " " << name << "[" << m << "] = {";
+            for (size_t k = 0; k < m; ++k) h << (k ? ", " : "") << f(k);
+            h << "};\n";
+        };
+        arr("int", "hyk_ev_term", [&](size_t k) { return std::to_string(d.ev[k].terminal); });
+        arr("int", "hyk_ev_dir", [&](size_t k) { return std::to_string(d.ev[k].direction); });
+        arr("int", "hyk_ev_idx", [&](size_t k) { return std::to_string(idx[k]); });
+        arr("double", "hyk_ev_cool", [&](size_t k) { return lit(d.ev[k].cooldown); });
+        std::vector<double> bt((size_t)(p + 1) * (p + 1));
+        hyk_ev_btab((int)p, bt.data());
+        h << "static __constant__ double hyk_ev_bt[" << bt.size() << "] = {";
+        for (size_t k = 0; k < bt.size(); ++k) h << (k ? ", " : "") << lit(bt[k]);
+        h << "};\n";
     }
 
     // ------------------------------------------------------------------
@@ -1019,6 +1112,10 @@ struct TeamGen {
     }
 
     bool analyse() {
+        if (!d.ev.empty()) {
+            err = "events are handled by the lane form";
+            return false;
+        }
         for (uint32_t k = 0; k < d.n_ops; ++k) {
             const uint32_t u = N + k;
             if (g.alias[u]) continue;
@@ -1452,9 +1549,13 @@ const char *kTeam =
 #include "kernel_team.inc"
     ;
 
-// hyk_dmath.h as a string (generated at build time from the header).
+// hyk_dmath.h and hyk_events.h as strings (generated at build time from the headers).
 const char *kDmath =
 #include "hyk_dmath.inc"
+    ;
+
+const char *kEvents =
+#include "hyk_events.inc"
     ;
 
 }  // namespace
@@ -1493,6 +1594,8 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     }
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << kDmath << "\n";
+    g.emit_events(h);
+    if (!d.ev.empty()) h << kEvents << "\n";
     h << kCommon << "\n";
     h << kTemplate << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
@@ -1562,6 +1665,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
       << lit(1.0 / (p - 1.0)) << "\n";
     h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
     h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
+    h << "#define HYK_NEV 0\n#define HYK_NTEV 0\n";
     h << kDmath << "\n";
     h << kCommon << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
@@ -1611,6 +1715,12 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
              "        double acc = HYK_SX(i, HYK_ORDER);\n"
              "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
              "        x1[i] = acc;\n    }\n}\n";
+        h << "extern \"C\" void hyk_host_tc(double *S, const double *x0, const double *pars, double t0, double *tc) {\n"
+             "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
+             "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
+             "    hyk_tjets(S, t0, 0);\n"
+             "    for (int i = 0; i < HYK_NEQ; ++i)\n"
+             "        for (int n = 0; n <= HYK_ORDER; ++n) tc[i * (HYK_ORDER + 1) + n] = HYK_SX(i, n);\n}\n";
         src = h.str();
         return true;
     }
@@ -1642,6 +1752,12 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
          "        double acc = HYK_SX(i, HYK_ORDER);\n"
          "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
          "        x1[i] = acc;\n    }\n}\n";
+    h << "extern \"C\" void hyk_host_tc(double *S, const double *x0, const double *pars, double t0, double *tc) {\n"
+         "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
+         "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
+         "    hyk_jets(S, t0);\n"
+         "    for (int i = 0; i < HYK_NEQ; ++i)\n"
+         "        for (int n = 0; n <= HYK_ORDER; ++n) tc[i * (HYK_ORDER + 1) + n] = HYK_SX(i, n);\n}\n";
     if (adjoint)
         h << "extern \"C\" void hyk_host_adjoint(double *S, const double *x0, const double *pars, double t0, double h, "
              "double *lam, double *pb) {\n"

@@ -14,6 +14,7 @@ struct Dec {
     uint32_t n_eq = 0, n_ops = 0, n_pars = 0;
     std::vector<hyk_uop_t> ops;
     std::vector<hyk_arg_t> rhs;
+    std::vector<hyk_event_t> ev;  // events: non-terminal and terminal, in one list
     uint32_t n_u() const { return n_eq + n_ops; }
 };
 

@@ -130,6 +130,12 @@ struct KParams {
     const int64_t *adj_steps;
     double *adj_lambda, *adj_pbar;
     double *jets;
+    double *ev_thi, *ev_tlo;
+    int32_t *ev_info;
+    uint64_t *ev_cnt;
+    uint64_t ev_cap;
+    double *ev_last;
+    int32_t *ev_sign;
     int persistent;
 };
 
@@ -304,8 +310,11 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (m->team) {
         // one CTA per warp by default: finest packing of the shared memory
     } else if (m->gmem) {
+        // Two CTAs of 128 threads per SM by default: at most 255 registers a
+        // thread, so both fit the register file, and eight warps hide the
+        // latency of the global-memory coefficients better than four.
         if (blk == 0) blk = 128;
-        const uint32_t ctas = m->cfg.persist_ctas ? m->cfg.persist_ctas : 1;
+        const uint32_t ctas = m->cfg.persist_ctas ? m->cfg.persist_ctas : (blk <= 128 ? 2 : 1);
         m->gmem_threads = (uint64_t)dv.n_sm * ctas * blk;
     } else if (blk == 0) {
         // Pick the block size maximising resident lanes per SM under the
@@ -487,8 +496,24 @@ static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size
     return 0;
 }
 
+// Event buffers of a module with events (all of them are required then).
+static int fill_events(const hyk_module *m, KParams &k, const hyk_prop_t *p) {
+    if (m->d.ev.empty()) return 0;
+    if (!p || !p->ev_t_hi || !p->ev_t_lo || !p->ev_info || !p->ev_count || !p->ev_last || !p->ev_sign)
+        return fail(HYK_ERR_INVALID, "a module with events needs the event buffers (ev_t_hi, ev_t_lo, ev_info, "
+                                     "ev_count, ev_last, ev_sign)");
+    k.ev_thi = p->ev_t_hi;
+    k.ev_tlo = p->ev_t_lo;
+    k.ev_info = p->ev_info;
+    k.ev_cnt = p->ev_count;
+    k.ev_cap = p->ev_capacity;
+    k.ev_last = p->ev_last;
+    k.ev_sign = p->ev_sign;
+    return 0;
+}
+
 int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t, int backward, int64_t *outcome,
-             double *h, double *tc, void *stream) {
+             double *h, double *tc, const struct hyk_prop *ev, void *stream) {
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (!outcome || !h) return fail(HYK_ERR_INVALID, "null outcome or h pointer");
@@ -496,6 +521,8 @@ int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t,
     HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
     KParams k;
     fill_lanes(k, lanes);
+    rc = fill_events(m, k, ev);
+    if (rc) return rc;
     k.step_lim = max_delta_t;
     k.step_default_lim = backward ? -INFINITY : INFINITY;
     k.step_oc = outcome;
@@ -543,8 +570,7 @@ static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const 
     k.ck_h = p->ck_h;
     k.ck_cap = p->ck_capacity;
     if (p->ck_x && (!p->ck_t || !p->ck_h)) return fail(HYK_ERR_INVALID, "the checkpoint tape needs ck_x, ck_t and ck_h");
-    (void)m;
-    return 0;
+    return fill_events(m, k, p);
 }
 
 int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, void *stream) {

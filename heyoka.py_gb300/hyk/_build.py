@@ -26,7 +26,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["hyk_generic.cu", "hyk_noalloc.cu", "hyk_runtime.cpp", "hyk_codegen.cpp"]
-DEPS = SOURCES + ["kernel_template.inc", "hyk_internal.hpp", "hyk_dmath.h"]
+DEPS = SOURCES + ["kernel_template.inc", "kernel_common.inc", "kernel_team.inc", "hyk_internal.hpp", "hyk_dmath.h",
+                  "hyk_events.h"]
 
 
 def _stale() -> bool:
@@ -49,6 +50,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         dm = f.read()
     with open(os.path.join(obj_dir, "hyk_dmath.inc"), "w") as f:
         f.write('R"HYKDM(' + dm + ')HYKDM"\n')
+    with open(os.path.join(CSRC, "hyk_events.h")) as f:
+        ev = f.read()
+    with open(os.path.join(obj_dir, "hyk_events.inc"), "w") as f:
+        f.write('R"HYKEV(' + ev + ')HYKEV"\n')
     # --fmad=false: device arithmetic exactly as written (no contraction), so
     # the shared math gives the same bits as the host build of the oracle.
     # -ffp-contract=off: the code generator's host arithmetic (the literals it

@@ -32,7 +32,8 @@ HYK_MODE_PERSISTENT = 1
 HYK_CFG_PIN_ARITH = 1
 HYK_CFG_ADJOINT = 2
 
-LANE_DONE, LANE_STOPPED, LANE_CAPACITY = 1, 2, 4
+LANE_DONE, LANE_STOPPED, LANE_CAPACITY, LANE_EVENT = 1, 2, 4, 8
+OC_EV_OVERFLOW = -4294967310
 
 
 class hyk_config_t(ctypes.Structure):
@@ -105,6 +106,13 @@ class hyk_prop_t(ctypes.Structure):
         ("ck_h", c_vp),
         ("ck_capacity", c_u64),
         ("slice_iters", c_u64),
+        ("ev_t_hi", c_vp),
+        ("ev_t_lo", c_vp),
+        ("ev_info", c_vp),
+        ("ev_count", c_vp),
+        ("ev_capacity", c_u64),
+        ("ev_last", c_vp),
+        ("ev_sign", c_vp),
     ]
 
 
@@ -114,7 +122,7 @@ SIGNATURES = {
     "hyk_module_destroy": (c_int, [c_vp]),
     "hyk_module_get_info": (c_int, [c_vp, P(hyk_module_info_t)]),
     "hyk_module_source": (ctypes.c_char_p, [c_vp]),
-    "hyk_step": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "hyk_step": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_int, c_vp, c_vp, c_vp, P(hyk_prop_t), c_vp]),
     "hyk_prop_init": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_vp]),
     "hyk_propagate_workspace_size": (ctypes.c_size_t, [c_vp, c_u64, c_int]),
     "hyk_propagate": (

@@ -71,14 +71,24 @@ class hyk_uop_t(ctypes.Structure):
     ]
 
 
+class hyk_event_t(ctypes.Structure):
+    _fields_ = [
+        ("g", hyk_arg_t),
+        ("terminal", ctypes.c_int32),
+        ("direction", ctypes.c_int32),
+        ("cooldown", ctypes.c_double),
+    ]
+
+
 class hyk_decomp_t(ctypes.Structure):
     _fields_ = [
         ("n_eq", ctypes.c_uint32),
         ("n_ops", ctypes.c_uint32),
         ("n_pars", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("n_ev", ctypes.c_uint32),
         ("ops", ctypes.POINTER(hyk_uop_t)),
         ("rhs", ctypes.POINTER(hyk_arg_t)),
+        ("ev", ctypes.POINTER(hyk_event_t)),
     ]
 
 
@@ -100,6 +110,8 @@ class Decomposition:
     ops: list = field(default_factory=list)
     rhs: list = field(default_factory=list)
     sys: list = field(default_factory=list)
+    # events: (arg, terminal, direction, cooldown), non-terminal and terminal in one list
+    ev: list = field(default_factory=list)
 
     @property
     def n_ops(self):
@@ -119,6 +131,8 @@ class Decomposition:
                 h.update(struct.pack("<iid", k, i, v))
         for k, i, v in self.rhs:
             h.update(struct.pack("<iid", k, i, v))
+        for (k, i, v), term, dirn, cool in self.ev:
+            h.update(struct.pack("<iidiid", k, i, v, int(term), int(dirn), float(cool)))
         return h.hexdigest()
 
     def as_c(self):
@@ -132,11 +146,16 @@ class Decomposition:
         rhs = (hyk_arg_t * max(self.n_eq, 1))()
         for i, (k, j, v) in enumerate(self.rhs):
             rhs[i].kind, rhs[i].idx, rhs[i].num = k, j, v
+        ev = (hyk_event_t * max(len(self.ev), 1))()
+        for j, ((k, i, v), term, dirn, cool) in enumerate(self.ev):
+            ev[j].g.kind, ev[j].g.idx, ev[j].g.num = k, i, v
+            ev[j].terminal, ev[j].direction, ev[j].cooldown = int(term), int(dirn), float(cool)
         d = hyk_decomp_t()
-        d.n_eq, d.n_ops, d.n_pars, d.reserved = self.n_eq, n, self.n_pars, 0
+        d.n_eq, d.n_ops, d.n_pars, d.n_ev = self.n_eq, n, self.n_pars, len(self.ev)
         d.ops = ctypes.cast(ops, ctypes.POINTER(hyk_uop_t))
         d.rhs = ctypes.cast(rhs, ctypes.POINTER(hyk_arg_t))
-        return d, (ops, rhs)
+        d.ev = ctypes.cast(ev, ctypes.POINTER(hyk_event_t)) if self.ev else None
+        return d, (ops, rhs, ev)
 
     # Pretty form mirroring the reference's ``decomposition`` property.
     def as_list(self):
@@ -175,8 +194,12 @@ def _op_str(op, a, b, d):
 _NONE: Arg = (ARG_NONE, 0, 0.0)
 
 
-def taylor_decompose(sys) -> Decomposition:
-    """Decompose ``sys = [(x0, rhs0), (x1, rhs1), ...]`` into u-variables."""
+def taylor_decompose(sys, events=()) -> Decomposition:
+    """Decompose ``sys = [(x0, rhs0), (x1, rhs1), ...]`` into u-variables.
+
+    ``events``: ``(expression, terminal, direction, cooldown)`` tuples; the
+    event functions are decomposed together with the system (shared
+    subexpressions are computed once), like the reference's event equations."""
     try:
         pairs = [(_e._ex(l), _e._ex(r)) for l, r in sys]
     except (TypeError, ValueError) as exc:
@@ -257,7 +280,16 @@ def taylor_decompose(sys) -> Decomposition:
         return ret
 
     rhs = [visit(r) for _, r in pairs]
-    return Decomposition(n_eq=n_eq, n_pars=n_pars, state_names=names, ops=ops, rhs=rhs, sys=pairs)
+    ev = []
+    for ex, term, dirn, cool in events:
+        ex = _e._ex(ex)
+        for name in _e.get_variables(ex):
+            if name not in index:
+                raise ValueError(
+                    "The event expression '{}' contains the variable '{}', which is not a state variable".format(ex, name)
+                )
+        ev.append((visit(ex), bool(term), int(dirn), float(cool)))
+    return Decomposition(n_eq=n_eq, n_pars=n_pars, state_names=names, ops=ops, rhs=rhs, sys=pairs, ev=ev)
 
 
 def order_from_tol(tol: float) -> int:

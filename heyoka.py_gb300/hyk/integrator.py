@@ -51,6 +51,16 @@ class taylor_outcome(enum.IntEnum):
     err_nf_state = -4294967300
     cb_stop = -4294967301
 
+    @classmethod
+    def _missing_(cls, value):
+        # A terminal event stops a lane with the event's index (>= 0) as outcome.
+        if isinstance(value, int) and value >= 0:
+            pseudo = int.__new__(cls, value)
+            pseudo._name_ = "terminal_event_{}".format(value)
+            pseudo._value_ = value
+            return cls._value2member_map_.setdefault(value, pseudo)
+        return None
+
 
 _LLVM_KWARGS = ("opt_level", "force_avx512", "slp_vectorize", "fast_math", "code_model", "parjit")
 
@@ -144,6 +154,7 @@ class taylor_adaptive_batch:
         pin_arith=False,
         schedule="lpt",
         team_size=0,
+        persist_ctas=0,
         **kwargs,
     ):
         for k in list(kwargs):
@@ -158,8 +169,17 @@ class taylor_adaptive_batch:
             raise NotImplementedError("the GPU batch integrator supports double precision (fp_type=float) only")
         if high_accuracy:
             raise NotImplementedError("high_accuracy mode is not supported by the GPU batch integrator")
-        if len(t_events) or len(nt_events):
-            raise NotImplementedError("event detection is not supported by the GPU batch integrator")
+        from .events import nt_event_batch, t_event_batch
+
+        t_events, nt_events = list(t_events), list(nt_events)
+        for e in t_events:
+            if not isinstance(e, t_event_batch):
+                raise TypeError("the t_events argument must be a list of t_event_batch objects")
+        for e in nt_events:
+            if not isinstance(e, nt_event_batch):
+                raise TypeError("the nt_events argument must be a list of nt_event_batch objects")
+        self._t_events = _copy.deepcopy(t_events)
+        self._nt_events = _copy.deepcopy(nt_events)
         if prop_mode not in ("persistent", "plain"):
             raise ValueError("prop_mode must be 'persistent' or 'plain'")
         if schedule not in ("lpt", "fifo"):
@@ -177,7 +197,9 @@ class taylor_adaptive_batch:
                 "the expected number of dimensions is 2, but the input array has a dimension of {}".format(st.ndim)
             )
         B = st.shape[1]
-        self._dec = taylor_decompose(sys)
+        evs = [(e.expression, True, int(e.direction), e.cooldown) for e in self._t_events]
+        evs += [(e.expression, False, int(e.direction), -1.0) for e in self._nt_events]
+        self._dec = taylor_decompose(sys, events=evs)
         if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
             # the variational part starts from the identity (state arguments) and zero (parameters)
             st = np.concatenate([st, self._vsys.initial_variational_state(B)])
@@ -226,7 +248,7 @@ class taylor_adaptive_batch:
         self._order = order_from_tol(tol)
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
-        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size)
+        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size, persist_ctas)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)
@@ -243,6 +265,7 @@ class taylor_adaptive_batch:
         self._prop = None  # dict of device arrays of the last propagation
         self._final_tc_mask = None  # lanes whose tc must be the final-state jets
         self._launch_events = None
+        self._ev = self._ev_alloc(16) if (self._t_events or self._nt_events) else None
 
     # ------------------------------------------------------------------ properties
     @property
@@ -385,6 +408,114 @@ class taylor_adaptive_batch:
         return [(taylor_outcome(int(a)), float(b), float(c), int(d)) for a, b, c, d in zip(oc, mn, mx, ns)]
 
     @property
+    def t_events(self):
+        from .events import _BoundEvent
+
+        return [_BoundEvent(self, e) for e in self._t_events]
+
+    @property
+    def nt_events(self):
+        from .events import _BoundEvent
+
+        return [_BoundEvent(self, e) for e in self._nt_events]
+
+    # ------------------------------------------------------------------ events
+    def _ev_alloc(self, cap):
+        B, f = self._B, dict(device=self._tdev)
+        nt = max(len(self._t_events), 1)
+        return {
+            "cap": cap,
+            "t_hi": torch.empty((cap, B), dtype=torch.float64, **f),
+            "t_lo": torch.empty((cap, B), dtype=torch.float64, **f),
+            "info": torch.empty((cap, B), dtype=torch.int32, **f),
+            "count": torch.zeros(B, dtype=torch.int64, **f),
+            "last": torch.full((nt, B), math.nan, dtype=torch.float64, **f),
+            "sign": torch.zeros(B, dtype=torch.int32, **f),
+        }
+
+    def _ev_grow(self):
+        old = self._ev
+        new = self._ev_alloc(2 * old["cap"])
+        c = old["cap"]
+        for k in ("t_hi", "t_lo", "info"):
+            new[k][:c] = old[k]
+        for k in ("count", "last", "sign"):
+            new[k] = old[k]
+        self._ev = new
+
+    def _ev_scratch(self):
+        """Throw-away event buffers for the internal steps that are not taken
+        (estimates): their roots must not reach the integrator's records."""
+        if self._ev is None:
+            return None
+        saved = self._ev
+        self._ev = self._ev_alloc(1)
+        self._ev["last"] = saved["last"].clone()
+        d = self._ev_fill(_lib.hyk_prop_t())
+        self._ev_keep = self._ev  # alive until the next internal step
+        self._ev = saved
+        return d
+
+    def _ev_fill(self, d):
+        """Point the event fields of a hyk_prop_t at the integrator's buffers."""
+        ev = self._ev
+        if ev is None:
+            return d
+        d.ev_t_hi, d.ev_t_lo, d.ev_info = ev["t_hi"].data_ptr(), ev["t_lo"].data_ptr(), ev["info"].data_ptr()
+        d.ev_count, d.ev_capacity = ev["count"].data_ptr(), ev["cap"]
+        d.ev_last, d.ev_sign = ev["last"].data_ptr(), ev["sign"].data_ptr()
+        return d
+
+    def _ev_dispatch_nt(self):
+        """Run the non-terminal callbacks for the recorded roots, in
+        chronological order per lane, then empty the records."""
+        from .events import callback_error
+
+        ev = self._ev
+        cnt = ev["count"].cpu().numpy()
+        if not cnt.any():
+            return
+        K = int(cnt.max())
+        hi = ev["t_hi"][:K].cpu().numpy()
+        lo = ev["t_lo"][:K].cpu().numpy()
+        info = ev["info"][:K].cpu().numpy()
+        ev["count"].zero_()
+        for b in np.nonzero(cnt)[0]:
+            n = int(cnt[b])
+            th, tl, inf = hi[:n, b], lo[:n, b], info[:n, b]
+            fwd = n < 2 or (th[-1] + tl[-1]) >= (th[0] + tl[0])
+            order = np.lexsort((tl, th)) if fwd else np.lexsort((-tl, -th))
+            for r in order:
+                k, sg = int(inf[r]) >> 2, (int(inf[r]) & 3) - 1
+                cb = self._nt_events[k].callback
+                try:
+                    cb(self, float(th[r]), sg, int(b))
+                except Exception as exc:  # noqa: BLE001 - re-raised as the reference does
+                    raise callback_error(exc) from exc
+
+    def _ev_terminal(self, lanes_oc):
+        """Terminal callbacks for the lanes a terminal event stopped
+        (lanes_oc: {lane: event index}); returns the lanes whose callback
+        asked to continue."""
+        from .events import callback_error, check_bool_retval
+
+        if not lanes_oc:
+            return []
+        sg = self._ev["sign"].cpu().numpy()
+        resume = []
+        for b, k in sorted(lanes_oc.items()):
+            cb = self._t_events[k].callback
+            if cb is None:
+                continue
+            try:
+                ret = cb(self, int(sg[b]), int(b))
+            except Exception as exc:  # noqa: BLE001
+                raise callback_error(exc) from exc
+            if check_bool_retval(ret):
+                resume.append(b)
+        return resume
+
+    @property
     def propagate_res_tensors(self):
         """Device tensors of the last propagation: outcome, min_h, max_h, n_steps, n_iter."""
         if self._prop is None:
@@ -433,11 +564,17 @@ class taylor_adaptive_batch:
             if torch.isnan(md).any():
                 raise ValueError("A NaN max_delta_t was passed to the step() function of an adaptive Taylor integrator")
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
+        evd = None
+        if self._ev is not None:
+            while self._ev["cap"] < 64:  # room for the roots of one step (records are emptied after each call)
+                self._ev_grow()
+            evd = self._ev_fill(_lib.hyk_prop_t())
         with torch.cuda.device(self._dev):
             _lib.check(
                 L.hyk_step(
                     self._mod.handle, lanes, None if md is None else md.data_ptr(), int(backward),
-                    oc.data_ptr(), h.data_ptr(), self._tc.data_ptr() if write_tc else None, stream_handle(self._dev),
+                    oc.data_ptr(), h.data_ptr(), self._tc.data_ptr() if write_tc else None, evd,
+                    stream_handle(self._dev),
                 ),
                 "hyk_step",
             )
@@ -445,6 +582,12 @@ class taylor_adaptive_batch:
         self._last_h = h.clone()
         if write_tc:
             self._final_tc_mask = None
+        if self._ev is not None:
+            ocn = oc.cpu().numpy()
+            if (ocn == _lib.OC_EV_OVERFLOW).any():
+                raise RuntimeError("a step found more event roots than the event buffers hold")
+            self._ev_dispatch_nt()
+            self._ev_terminal({int(b): int(o) for b, o in enumerate(ocn) if o >= 0})
 
     def step(self, max_delta_t=None, write_tc=False):
         """One step on every lane (optionally clamped by a per-lane ``max_delta_t``)."""
@@ -497,7 +640,7 @@ class taylor_adaptive_batch:
             _lib.check(
                 L.hyk_step(
                     self._mod.handle, lanes_struct(st, self._pars, th, tl), zero.data_ptr(), 0, oc.data_ptr(),
-                    h.data_ptr(), tc.data_ptr(), stream_handle(self._dev),
+                    h.data_ptr(), tc.data_ptr(), self._ev_scratch(), stream_handle(self._dev),
                 ),
                 "hyk_step",
             )
@@ -557,7 +700,7 @@ class taylor_adaptive_batch:
         t0h, t0l = self._thi.clone(), self._tlo.clone()
 
         def desc():
-            return _lib.hyk_prop_t(
+            return self._ev_fill(_lib.hyk_prop_t(
                 tf_hi.data_ptr(), None if tf_lo is None else tf_lo.data_ptr(), None if md is None else md.data_ptr(),
                 int(max_steps),
                 None if grid is None else grid.data_ptr(), 0 if grid is None else grid.shape[0],
@@ -570,7 +713,7 @@ class taylor_adaptive_batch:
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
                 0 if lane_order is None else lane_order.numel(), None, None, None, 0, 0,
-            )
+            ))
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
         mode = _lib.HYK_MODE_PERSISTENT if self._prop_mode == "persistent" else _lib.HYK_MODE_PLAIN
@@ -590,21 +733,40 @@ class taylor_adaptive_batch:
                 )
                 if ev is not None:
                     ev[1].record(torch.cuda.current_stream(self._dev))
-                if not c_output:
+                if not c_output and self._ev is None:
                     break
                 full = (p["status"] & _lib.LANE_CAPACITY) != 0
-                if not bool(full.any()):
+                grow = bool(full.any())
+                resume = []
+                if self._ev is not None:
+                    self._ev_dispatch_nt()
+                    evl = (p["status"] & _lib.LANE_EVENT) != 0
+                    if bool(evl.any()):
+                        idx = torch.nonzero(evl).flatten().cpu().numpy()
+                        ks = p["outcome"][evl].cpu().numpy()
+                        resume = self._ev_terminal({int(b): int(k) for b, k in zip(idx, ks)})
+                if not grow and not resume:
                     break
-                # Grow the coefficient store and resume the lanes that filled it.
-                ncap = cap * 2
-                ntcs = torch.empty((ncap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
-                nthi = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
-                ntlo = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
-                ntcs[:cap] = tcs
-                nthi[:cap] = thi
-                ntlo[:cap] = tlo
-                tcs, thi, tlo, cap = ntcs, nthi, ntlo, ncap
-                p["status"] &= ~(_lib.LANE_CAPACITY | _lib.LANE_STOPPED)
+                if grow and c_output and bool((p["n_iter"] >= cap).any()):
+                    # Grow the coefficient store.
+                    ncap = cap * 2
+                    ntcs = torch.empty((ncap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
+                    nthi = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
+                    ntlo = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
+                    ntcs[:cap] = tcs
+                    nthi[:cap] = thi
+                    ntlo[:cap] = tlo
+                    tcs, thi, tlo, cap = ntcs, nthi, ntlo, ncap
+                if grow and self._ev is not None:
+                    self._ev_grow()
+                # Resume the lanes that filled a store or whose terminal callback said so.
+                clear = full
+                if resume:
+                    r = torch.zeros(B, dtype=torch.bool, device=self._tdev)
+                    r[torch.tensor(resume, device=self._tdev)] = True
+                    clear = clear | r
+                keep = torch.tensor(~(_lib.LANE_CAPACITY | _lib.LANE_STOPPED | _lib.LANE_EVENT), dtype=torch.int32)
+                p["status"] = torch.where(clear, p["status"] & keep.to(self._tdev), p["status"])
                 d = desc()
         self._finish_prop(p, group, last_tc)
         res = {"grid_out": grid_out}
@@ -624,7 +786,7 @@ class taylor_adaptive_batch:
         with torch.cuda.device(self._dev):
             _lib.check(
                 L.hyk_step(self._mod.handle, lanes_struct(st, self._pars, th, tl), None, 0, oc.data_ptr(),
-                           h.data_ptr(), None, stream_handle(self._dev)),
+                           h.data_ptr(), None, self._ev_scratch(), stream_handle(self._dev)),
                 "hyk_step",
             )
         rem = (tf_hi - self._thi).abs()
@@ -766,6 +928,13 @@ class taylor_adaptive_batch:
                 new.__dict__[k] = None if v is None else {a: (None if b is None else b.clone()) for a, b in v.items()}
             elif k == "_step_res":
                 new.__dict__[k] = None if v is None else (v[0].clone(), v[1].clone())
+            elif k == "_ev":
+                new.__dict__[k] = None if v is None else {a: (b.clone() if isinstance(b, torch.Tensor) else b)
+                                                          for a, b in v.items()}
+            elif k in ("_t_events", "_nt_events"):
+                # a copy of the integrator copies its events (the reference's
+                # deep copy gives new callback objects)
+                new.__dict__[k] = _copy.deepcopy(v, memo) if deep else list(v)
             elif deep and not k.startswith("_"):
                 new.__dict__[k] = _copy.deepcopy(v, memo)
             else:
@@ -783,6 +952,10 @@ class taylor_adaptive_batch:
                 d[k] = None if v is None else {a: (None if b is None else b.cpu()) for a, b in v.items()}
             elif k == "_step_res":
                 d[k] = None if v is None else (v[0].cpu(), v[1].cpu())
+            elif k == "_ev":
+                d[k] = None if v is None else {a: (b.cpu() if isinstance(b, torch.Tensor) else b) for a, b in v.items()}
+            elif k == "_ev_keep":
+                continue
             else:
                 d[k] = v
         return d
@@ -799,6 +972,11 @@ class taylor_adaptive_batch:
             self._prop = {a: (None if b is None else b.to(dev)) for a, b in self._prop.items()}
         if self._step_res is not None:
             self._step_res = (self._step_res[0].to(dev), self._step_res[1].to(dev))
+        if self.__dict__.get("_ev") is not None:
+            self._ev = {a: (b.to(dev) if isinstance(b, torch.Tensor) else b) for a, b in self._ev.items()}
+        self.__dict__.setdefault("_ev", None)
+        self.__dict__.setdefault("_t_events", [])
+        self.__dict__.setdefault("_nt_events", [])
         self._tdev = dev
         self._mod = get_module(self._dec, self._order, self._dev)
 

@@ -73,10 +73,26 @@ typedef struct hyk_decomp {
     uint32_t n_eq;
     uint32_t n_ops;
     uint32_t n_pars;
-    uint32_t reserved;
+    uint32_t n_ev;              /* number of events (0: none) */
     const hyk_uop_t *ops;
     const hyk_arg_t *rhs;
+    const struct hyk_event *ev; /* (n_ev) event functions, or NULL */
 } hyk_decomp_t;
+
+/* An event of the batch integrator (heyoka's t_event_batch / nt_event_batch,
+ * heyoka/taylor_expose_events.cpp:202-311): the event function g (an
+ * argument of the decomposition, normally the u-variable of the event
+ * expression, decomposed together with the system) and how its roots act.
+ * Every step the Taylor polynomial of g over the step is searched for roots;
+ * a terminal event ends the step at its first root (outcome = the event's
+ * index among the terminal events), a non-terminal event's roots are
+ * recorded (time, direction) for the host to report. */
+typedef struct hyk_event {
+    hyk_arg_t g;
+    int32_t terminal;  /* 1: terminal, 0: non-terminal */
+    int32_t direction; /* -1: only roots where g decreases, +1: increases, 0: any */
+    double cooldown;   /* terminal: after a trigger the event is ignored for this time; < 0: automatic */
+} hyk_event_t;
 
 /* ---- taylor_outcome (values of heyoka/core.cpp:324-329, as printed in
  *      doc/notebooks/Batch mode overview.ipynb) ---- */
@@ -154,9 +170,14 @@ typedef struct hyk_lanes {
  *                pass `backward` = 1 with NULL for step_backward (-inf).
  *   outcome:     (n_lanes) int64 taylor_outcome per lane (out)
  *   h:           (n_lanes) step taken per lane (out)
- *   tc:          (n_eq, order+1, n_lanes) Taylor coefficients of the step, or NULL */
+ *   tc:          (n_eq, order+1, n_lanes) Taylor coefficients of the step, or NULL
+ *   ev:          event buffers (the ev_* fields of a hyk_prop_t; the other
+ *                fields are ignored), or NULL; needed when the module has
+ *                events.  A terminal event ends the step at its root: the
+ *                outcome is the event's index and ev_sign the root's direction. */
+struct hyk_prop;
 int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t, int backward,
-             int64_t *outcome, double *h, double *tc, void *stream);
+             int64_t *outcome, double *h, double *tc, const struct hyk_prop *ev, void *stream);
 
 /* Propagation of every lane to its own final time.  Replaces
  * taylor_adaptive_batch::propagate_until / propagate_for / propagate_grid
@@ -214,11 +235,27 @@ typedef struct hyk_prop {
      * next call continues it; used to time-slice a continuously refilled
      * batch (serving). */
     uint64_t slice_iters;
+    /* events (modules with n_ev > 0): roots of non-terminal events are
+     * recorded per lane, ev_t_hi/lo (ev_capacity, ld) = time of the root
+     * (double-length), ev_info (ev_capacity, ld) = 4 * event index +
+     * (direction + 1); ev_count (ld) = records so far (in/out).  A step whose
+     * roots do not fit is not taken: the lane stops with HYK_LANE_CAPACITY.
+     * ev_last (n_terminal, ld) = time of each terminal event's last trigger
+     * (NaN: none; in/out, for the cooldown); ev_sign (ld) = direction of the
+     * root of the terminal event that stopped a lane. */
+    double *ev_t_hi;
+    double *ev_t_lo;
+    int32_t *ev_info;
+    uint64_t *ev_count;
+    uint64_t ev_capacity;
+    double *ev_last;
+    int32_t *ev_sign;
 } hyk_prop_t;
 
 #define HYK_LANE_DONE 1u     /* reached the final time */
-#define HYK_LANE_STOPPED 2u  /* stopped early: error, step limit or capacity */
-#define HYK_LANE_CAPACITY 4u /* stopped because tc_capacity was reached (resumable) */
+#define HYK_LANE_STOPPED 2u  /* stopped early: error, step limit, capacity or terminal event */
+#define HYK_LANE_CAPACITY 4u /* stopped because tc_capacity, ck_capacity or ev_capacity was reached (resumable) */
+#define HYK_LANE_EVENT 8u    /* stopped by a terminal event (outcome = its index) */
 
 /* Initialise the bookkeeping arrays of `p` for a propagation to tf. */
 int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, void *stream);

@@ -33,6 +33,11 @@
 //    (heyoka/expose_batch_integrators.cpp:315-392).
 //  * continuous output: per-iteration Taylor coefficients and end times
 //    (heyoka/taylor_expose_c_output.cpp:259-523).
+//  * events (t_event_batch / nt_event_batch, heyoka/taylor_expose_events.cpp:202-311):
+//    the event functions' Taylor coefficients up to order p, roots of their
+//    step polynomials by hyk_events.h, a terminal event ending its lane's
+//    step at the first root, non-terminal roots recorded in order
+//    (hyko_propagate_ev, gpu arithmetic, per-lane stopping like the kernels).
 //
 // Two arithmetic modes:
 //  mode 0 ("pin"): sums of products with separate multiply and add, division
@@ -54,7 +59,8 @@
 // Build: oracle/build.py (g++ -O3 -fopenmp -ffp-contract=off, no -march flags).
 
 #include "hyk.h"
-#include "hyk_dmath.h"  // the deterministic elementary functions of the CUDA kernels
+#include "hyk_dmath.h"   // the deterministic elementary functions of the CUDA kernels
+#include "hyk_events.h"  // the event root finder of the CUDA kernels
 
 #include <algorithm>
 #include <cmath>
@@ -193,6 +199,7 @@ struct Dec {
     uint32_t n_eq = 0, n_ops = 0, n_pars = 0;
     std::vector<hyk_uop_t> ops;
     std::vector<hyk_arg_t> rhs;
+    std::vector<hyk_event_t> ev;
     uint32_t n_u() const { return n_eq + n_ops; }
 };
 
@@ -236,6 +243,12 @@ bool load_dec(const hyk_decomp_t *d, Dec &out) {
     for (const auto &r : out.rhs)
         if (!chk(r, nu) || r.kind == HYK_ARG_NONE) {
             g_err = "invalid right-hand side";
+            return false;
+        }
+    if (d->n_ev > 0 && d->ev) out.ev.assign(d->ev, d->ev + d->n_ev);
+    for (const auto &e : out.ev)
+        if (!chk(e.g, nu) || e.g.kind == HYK_ARG_NONE) {
+            g_err = "invalid event";
             return false;
         }
     return true;
@@ -569,6 +582,20 @@ template <typename T> struct Batch {
             for (uint32_t k = 0; k < d.n_ops; ++k) op_coef(k, n);
             state_next(n);
         }
+        // Event functions need every order up to p.
+        if (!d.ev.empty())
+            for (uint32_t k = 0; k < d.n_ops; ++k) op_coef(k, p);
+    }
+
+    // Order-n coefficient of an argument (event functions), lane l.
+    T arg_coef(const hyk_arg_t &a, uint32_t n, uint32_t l) {
+        switch (a.kind) {
+        case HYK_ARG_U: return jr((uint32_t)a.idx, n)[l];
+        case HYK_ARG_NUM: return n == 0 ? T(a.num) : T(0);
+        case HYK_ARG_PAR: return n == 0 ? pars[(size_t)a.idx * B + l] : T(0);
+        case HYK_ARG_TIME: return n == 0 ? thi[l] : (n == 1 ? T(1) : T(0));
+        }
+        return T(0);
     }
 
     // Step size per lane from the jets (unclamped, positive).
@@ -819,11 +846,193 @@ int step_one(const Dec &d, uint32_t p, int mode, uint32_t B, double *state, cons
     return 0;
 }
 
+// Per-lane propagation with events, gpu arithmetic (double): every lane is
+// its own batch of one, stepped exactly as the kernels step it (events after
+// the step size, a terminal event ending the lane at its root).
+struct EvRec {
+    std::vector<double> t_hi, t_lo;
+    std::vector<int32_t> info;
+    std::vector<uint32_t> lane;
+};
+
+int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const double *pars, double *t_hi,
+                 double *t_lo, const double *tf_hi, uint64_t max_steps, int64_t *outcome, uint64_t *n_steps,
+                 uint32_t *status, double *ev_last, int32_t *ev_sign, EvRec &rec) {
+    const uint32_t ne = d.n_eq, np = d.n_pars;
+    std::vector<double> bt((size_t)(p + 1) * (p + 1)), work(3 * (p + 1)), g(p + 1);
+    hyk_ev_btab((int)p, bt.data());
+    uint32_t n_term = 0;
+    std::vector<int> idx(d.ev.size());
+    {
+        uint32_t nn = 0;
+        for (size_t k = 0; k < d.ev.size(); ++k) idx[k] = d.ev[k].terminal ? (int)n_term++ : (int)nn++;
+    }
+    for (uint32_t l = 0; l < B; ++l) {
+        Batch<double> bq(d, p, 1, 1);
+        for (uint32_t i = 0; i < ne; ++i) bq.state[i] = state[(size_t)i * B + l];
+        for (uint32_t i = 0; i < np; ++i) bq.pars[i] = pars ? pars[(size_t)i * B + l] : 0.0;
+        bq.thi[0] = t_hi[l];
+        bq.tlo[0] = t_lo ? t_lo[l] : 0.0;
+        dfl<double> rem = dsub(dnorm(tf_hi[l], 0.0), dfl<double>{bq.thi[0], bq.tlo[0]});
+        const bool dir = dge(rem, dfl<double>{0.0, 0.0});
+        uint64_t nit = 0, nst = 0;
+        int64_t oc = HYK_OUTCOME_TIME_LIMIT;
+        uint32_t st = (rem.hi == 0.0 && rem.lo == 0.0) ? HYK_LANE_DONE : 0u;
+        std::vector<double> h(1);
+        while (!st) {
+            const double lim = dir ? std::min(HUGE_VAL, rem.hi) : std::max(-HUGE_VAL, rem.hi);
+            bq.jets();
+            bq.step_size(h);
+            double hh = lim < 0.0 ? -h[0] : h[0];
+            if (std::fabs(lim) < std::fabs(hh)) hh = lim;
+            int64_t soc = (hh == lim) ? HYK_OUTCOME_TIME_LIMIT : HYK_OUTCOME_SUCCESS;
+            // events of the step
+            const double th = bq.thi[0], tl = bq.tlo[0];
+            int kt = -1, sgt = 0;
+            double stt = 2.0;
+            size_t rec0 = rec.t_hi.size();
+            if (hh != 0.0) {
+                const double ah = std::fabs(hh);
+                for (size_t k = 0; k < d.ev.size(); ++k) {
+                    if (!d.ev[k].terminal) continue;
+                    const int j = idx[k];
+                    double slo = 0.0;
+                    const double last = ev_last[(size_t)j * B + l];
+                    if (last == last) {
+                        const double cd = d.ev[k].cooldown >= 0.0 ? d.ev[k].cooldown
+                                                                  : 1e-12 * (std::fabs(last) > 1.0 ? std::fabs(last) : 1.0);
+                        const double r = cd - std::fabs(th - last);
+                        if (r > 0.0) slo = r / ah;
+                    }
+                    if (slo >= 1.0) continue;
+                    for (uint32_t n = 0; n <= p; ++n) g[n] = bq.arg_coef(d.ev[k].g, n, 0);
+                    double rs = 0.0;
+                    int rsg = 0;
+                    const int nf = hyk_ev_find(g.data(), 1, (int)p, hh, bt.data(), slo, 1.0, d.ev[k].direction, 1, &rs,
+                                               &rsg, 1, 1, work.data());
+                    if (nf > 0 && rs < stt) {
+                        stt = rs;
+                        kt = j;
+                        sgt = rsg;
+                    }
+                }
+                const double shi = kt >= 0 ? stt : 1.0;
+                for (size_t k = 0; k < d.ev.size(); ++k) {
+                    if (d.ev[k].terminal) continue;
+                    for (uint32_t n = 0; n <= p; ++n) g[n] = bq.arg_coef(d.ev[k].g, n, 0);
+                    std::vector<double> rs(4096);
+                    std::vector<int> rsg(4096);
+                    const int nf = hyk_ev_find(g.data(), 1, (int)p, hh, bt.data(), 0.0, shi, d.ev[k].direction, 0,
+                                               rs.data(), rsg.data(), 1, 4096, work.data());
+                    for (int r = 0; r < std::min(nf, 4096); ++r) {
+                        const dfl<double> t = dadd(dfl<double>{th, tl}, dfl<double>{rs[r] * hh, 0.0});
+                        rec.t_hi.push_back(t.hi);
+                        rec.t_lo.push_back(t.lo);
+                        rec.info.push_back(4 * idx[k] + rsg[r] + 1);
+                        rec.lane.push_back(l);
+                    }
+                }
+                if (kt >= 0) {
+                    hh = stt * hh;
+                    soc = kt;
+                }
+            }
+            std::vector<double> ns(ne);
+            bq.horner(&hh, ns.data());
+            const dfl<double> t = dadd(dfl<double>{th, tl}, dfl<double>{hh, 0.0});
+            bool fin = std::isfinite(t.hi);
+            for (uint32_t i = 0; i < ne; ++i) fin = fin && std::isfinite(ns[i]);
+            bq.state.assign(ns.begin(), ns.end());
+            bq.thi[0] = t.hi;
+            bq.tlo[0] = t.lo;
+            ++nit;
+            if (!fin) {
+                rec.t_hi.resize(rec0);
+                rec.t_lo.resize(rec0);
+                rec.info.resize(rec0);
+                rec.lane.resize(rec0);
+                oc = HYK_OUTCOME_ERR_NF_STATE;
+                st = HYK_LANE_STOPPED;
+                break;
+            }
+            nst += hh != 0.0;
+            rem = (hh == rem.hi) ? dfl<double>{0.0, 0.0} : dsub(rem, dfl<double>{hh, 0.0});
+            oc = soc;
+            if (kt >= 0) {
+                ev_last[(size_t)kt * B + l] = t.hi;
+                ev_sign[l] = sgt;
+                st = HYK_LANE_STOPPED | HYK_LANE_EVENT;
+                break;
+            }
+            if (rem.hi == 0.0 && rem.lo == 0.0) {
+                oc = HYK_OUTCOME_TIME_LIMIT;
+                st = HYK_LANE_DONE;
+                break;
+            }
+            if (max_steps != 0 && nit >= max_steps) {
+                oc = HYK_OUTCOME_STEP_LIMIT;
+                st = HYK_LANE_STOPPED;
+                break;
+            }
+        }
+        for (uint32_t i = 0; i < ne; ++i) state[(size_t)i * B + l] = bq.state[i];
+        t_hi[l] = bq.thi[0];
+        if (t_lo) t_lo[l] = bq.tlo[0];
+        outcome[l] = oc;
+        n_steps[l] = nst;
+        status[l] = st;
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
 
 const char *hyko_last_error(void) { return g_err.c_str(); }
+
+// Per-lane propagation to tf_hi with events (gpu arithmetic, double).  The
+// non-terminal roots come back in malloc'ed arrays (free with hyko_free) in
+// the order the kernels record them per lane: (time hi, time lo, info =
+// 4 * event index + direction + 1, lane).  ev_last (n_terminal, B) and ev_sign
+// (B) are in/out like the kernels' buffers.
+int hyko_propagate_ev(const hyk_decomp_t *dd, uint32_t order, uint32_t B, double *state, const double *pars,
+                      double *t_hi, double *t_lo, const double *tf_hi, uint64_t max_steps, int64_t *outcome,
+                      uint64_t *n_steps, uint32_t *status, double *ev_last, int32_t *ev_sign, uint64_t *n_rec,
+                      double **rec_t_hi, double **rec_t_lo, int32_t **rec_info, uint32_t **rec_lane) {
+    Dec d;
+    if (!load_dec(dd, d)) return HYK_ERR_INVALID;
+    if (order < 2 || B == 0) {
+        g_err = "invalid order or batch size";
+        return HYK_ERR_INVALID;
+    }
+    EvRec rec;
+    const int r = propagate_ev(d, order, B, state, pars, t_hi, t_lo, tf_hi, max_steps, outcome, n_steps, status,
+                               ev_last, ev_sign, rec);
+    auto dup = [](const void *src, size_t bytes) {
+        void *q = std::malloc(std::max<size_t>(bytes, 8));
+        if (bytes) std::memcpy(q, src, bytes);
+        return q;
+    };
+    *n_rec = rec.t_hi.size();
+    *rec_t_hi = (double *)dup(rec.t_hi.data(), rec.t_hi.size() * sizeof(double));
+    *rec_t_lo = (double *)dup(rec.t_lo.data(), rec.t_lo.size() * sizeof(double));
+    *rec_info = (int32_t *)dup(rec.info.data(), rec.info.size() * sizeof(int32_t));
+    *rec_lane = (uint32_t *)dup(rec.lane.data(), rec.lane.size() * sizeof(uint32_t));
+    return r;
+}
+
+// The kernels' root finder on one polynomial (tests of hyk_events.h on the host).
+int hyko_ev_find(const double *g, uint32_t p, double h, double s_lo, double s_hi, int dir, int first_only, double *rs,
+                 int32_t *rsg, int maxr) {
+    std::vector<double> bt((size_t)(p + 1) * (p + 1)), work(3 * (p + 1));
+    hyk_ev_btab((int)p, bt.data());
+    std::vector<int> sg(std::max(maxr, 1));
+    const int n = hyk_ev_find(g, 1, (int)p, h, bt.data(), s_lo, s_hi, dir, first_only, rs, sg.data(), 1, maxr,
+                              work.data());
+    for (int i = 0; i < std::min(n, maxr); ++i) rsg[i] = sg[i];
+    return n;
+}
 
 // One step of a batch of B lanes (host arrays, [var][lane]).  prec: 0 double, 1 binary128.
 int hyko_step(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, uint32_t B, double *state,

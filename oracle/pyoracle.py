@@ -57,6 +57,13 @@ def lib():
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
             pd, pd, pd, pd, pd, ctypes.c_int, pi64, pd, pd, pu64,
         ]
+        L.hyko_propagate_ev.argtypes = [
+            P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_uint32, pd, pd, pd, pd, pd, ctypes.c_uint64, pi64, pu64,
+            P(ctypes.c_uint32), pd, P(ctypes.c_int32), pu64, P(pd), P(pd), P(P(ctypes.c_int32)),
+            P(P(ctypes.c_uint32)),
+        ]
+        L.hyko_ev_find.argtypes = [pd, ctypes.c_uint32, c_d, c_d, c_d, ctypes.c_int, ctypes.c_int, pd,
+                                   P(ctypes.c_int32), ctypes.c_int]
         L.hyko_free.argtypes = [ctypes.c_void_p]
         L.hyko_max_threads.restype = ctypes.c_int
         _lib = L
@@ -205,3 +212,58 @@ def ensemble_until(sys_or_dec, state, pars, t0, tf, order, batch=8, n_threads=0,
     if rc != 0:
         raise RuntimeError(lib().hyko_last_error().decode())
     return {"state": state, "t_hi": t_hi, "t_lo": t_lo, "outcome": oc, "min_h": mn, "max_h": mx, "n_steps": ns}
+
+
+def ev_find(g, h, s_lo=0.0, s_hi=1.0, direction=0, first_only=False, maxr=256):
+    """The kernels' event root finder (hyk_events.h) on the host: roots s in
+    (s_lo, s_hi] of sum g_n (h s)^n, with their directions."""
+    g = _f64(g)
+    rs = np.zeros(maxr)
+    rsg = np.zeros(maxr, dtype=np.int32)
+    n = lib().hyko_ev_find(_p(g), len(g) - 1, h, s_lo, s_hi, int(direction), int(first_only), _p(rs),
+                           rsg.ctypes.data_as(P(ctypes.c_int32)), maxr)
+    return rs[: min(n, maxr)], rsg[: min(n, maxr)], n
+
+
+def propagate_ev(sys_, events, state, tf, pars=None, order=20, max_steps=0, time=None, ev_last=None, time_lo=None):
+    """Per-lane propagation with events in gpu arithmetic, the kernels'
+    semantics.  events: (expression, terminal, direction, cooldown) tuples in
+    the integrator's order (terminal events first).  Returns a dict with
+    state, t_hi, t_lo, outcome, n_steps, status, ev_last, ev_sign and the
+    non-terminal records (rec_t_hi, rec_t_lo, rec_info, rec_lane)."""
+    dec = taylor_decompose(sys_, events=events)
+    cdec, keep = dec.as_c()
+    st = _f64(state).copy()
+    B = st.shape[1]
+    pa = np.zeros((max(dec.n_pars, 1), B)) if pars is None else _f64(pars).reshape(-1, B).copy()
+    th = np.zeros(B) if time is None else _f64(np.broadcast_to(time, (B,))).copy()
+    tl = np.zeros(B) if time_lo is None else _f64(np.broadcast_to(time_lo, (B,))).copy()
+    tfv = _f64(np.broadcast_to(tf, (B,))).copy()
+    n_term = max(sum(1 for e in events if e[1]), 1)
+    last = np.full((n_term, B), np.nan) if ev_last is None else _f64(ev_last).copy()
+    sign = np.zeros(B, dtype=np.int32)
+    oc = np.zeros(B, dtype=np.int64)
+    ns = np.zeros(B, dtype=np.uint64)
+    status = np.zeros(B, dtype=np.uint32)
+    nrec = ctypes.c_uint64()
+    rh, rl = pd(), pd()
+    ri, rln = P(ctypes.c_int32)(), P(ctypes.c_uint32)()
+    L = lib()
+    rc = L.hyko_propagate_ev(ctypes.byref(cdec), order, B, _p(st), _p(pa), _p(th), _p(tl), _p(tfv), max_steps,
+                             _p(oc, pi64), _p(ns, pu64), status.ctypes.data_as(P(ctypes.c_uint32)), _p(last),
+                             sign.ctypes.data_as(P(ctypes.c_int32)), ctypes.byref(nrec), ctypes.byref(rh),
+                             ctypes.byref(rl), ctypes.byref(ri), ctypes.byref(rln))
+    if rc != 0:
+        raise RuntimeError(L.hyko_last_error().decode())
+    n = nrec.value
+    out = {
+        "state": st, "t_hi": th, "t_lo": tl, "outcome": oc, "n_steps": ns, "status": status, "ev_last": last,
+        "ev_sign": sign,
+        "rec_t_hi": np.ctypeslib.as_array(rh, (max(n, 1),))[:n].copy(),
+        "rec_t_lo": np.ctypeslib.as_array(rl, (max(n, 1),))[:n].copy(),
+        "rec_info": np.ctypeslib.as_array(ri, (max(n, 1),))[:n].copy(),
+        "rec_lane": np.ctypeslib.as_array(rln, (max(n, 1),))[:n].copy(),
+    }
+    for ptr in (rh, rl, ri, rln):
+        L.hyko_free(ptr)
+    return out

@@ -29,14 +29,35 @@ def test_python_binding_covers_header(libhyk):
     assert set(declared_symbols()) <= set(_lib.SIGNATURES)
 
 
-def test_struct_layouts():
-    from hyk import _lib
-    from hyk.decompose import hyk_arg_t, hyk_decomp_t, hyk_uop_t
+def test_struct_layouts(tmp_path):
+    """The ctypes mirrors have the sizes and field offsets of the C header
+    (a host program compiled against include/hyk.h prints them)."""
+    import subprocess
 
-    assert ctypes.sizeof(hyk_arg_t) == 16 and ctypes.sizeof(hyk_uop_t) == 40
-    assert ctypes.sizeof(hyk_decomp_t) == 32
-    assert ctypes.sizeof(_lib.hyk_lanes_t) == 48
-    assert ctypes.sizeof(_lib.hyk_prop_t) == 29 * 8
+    from hyk import _lib
+    from hyk.decompose import hyk_arg_t, hyk_decomp_t, hyk_event_t, hyk_uop_t
+
+    structs = {
+        "hyk_arg_t": hyk_arg_t, "hyk_uop_t": hyk_uop_t, "hyk_decomp_t": hyk_decomp_t, "hyk_event_t": hyk_event_t,
+        "hyk_config_t": _lib.hyk_config_t, "hyk_module_info_t": _lib.hyk_module_info_t,
+        "hyk_lanes_t": _lib.hyk_lanes_t, "hyk_prop_t": _lib.hyk_prop_t,
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "hyk.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append('printf("%s %zu\\n", "{0}", sizeof({0}));'.format(name))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %zu\\n", "{0}", "{1}", offsetof({0}, {1}));'.format(name, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                               check=True).stdout.splitlines())
+    for name, cls in structs.items():
+        assert int(out[name]) == ctypes.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(out[name + "." + f]) == getattr(cls, f).offset, (name, f)
 
 
 def test_no_device_errors(libhyk):

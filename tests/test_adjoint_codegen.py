@@ -110,3 +110,6 @@ def test_per_order_functions_bitwise_vs_oracle(libhyk, oracle):
         H.hyk_host_step(_arr(S), _arr(st[:, lane]), _arr(np.zeros(1)), ctypes.c_double(0.0), ctypes.c_double(h[lane]),
                         x1.ctypes.data_as(pd))
         assert np.array_equal(x1, o.state[:, lane])
+        tc = np.zeros(30 * 20)
+        H.hyk_host_tc(_arr(S), _arr(st[:, lane]), _arr(np.zeros(1)), ctypes.c_double(0.0), tc.ctypes.data_as(pd))
+        assert np.array_equal(tc.reshape(30, 20), o.tc[:, :, lane])

@@ -62,6 +62,7 @@ def test_team_recurrences_bitwise_vs_oracle(libhyk, oracle, name):
     o = oracle.Oracle(sys_, st, pars=pars, order=order, mode=1, time=np.full(st.shape[1], 0.25))
     _, h = o.step()
     S = np.zeros(H.hyk_host_nslot())
+    n_eq = st.shape[0]
     for lane in range(st.shape[1]):
         x0 = np.ascontiguousarray(st[:, lane], dtype=np.float64)
         p = np.ascontiguousarray(pars[:, lane] if pars is not None else np.zeros(1), dtype=np.float64)
@@ -69,6 +70,12 @@ def test_team_recurrences_bitwise_vs_oracle(libhyk, oracle, name):
         H.hyk_host_step(S.ctypes.data_as(pd), x0.ctypes.data_as(pd), p.ctypes.data_as(pd), ctypes.c_double(0.25),
                         ctypes.c_double(h[lane]), x1.ctypes.data_as(pd))
         assert np.array_equal(x1, o.state[:, lane]), (name, lane)
+        # Every Taylor coefficient, not only the stepped state (whose Horner
+        # sum can hide last-bit differences of the high orders).
+        tc = np.zeros(n_eq * (order + 1))
+        H.hyk_host_tc(S.ctypes.data_as(pd), x0.ctypes.data_as(pd), p.ctypes.data_as(pd), ctypes.c_double(0.25),
+                      tc.ctypes.data_as(pd))
+        assert np.array_equal(tc.reshape(n_eq, order + 1), o.tc[:, :, lane]), (name, lane)
 
 
 def test_team_form_rejects_unsupported_operand(libhyk):
