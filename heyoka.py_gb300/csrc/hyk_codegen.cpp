@@ -1566,7 +1566,7 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint) {
 }
 
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint, uint64_t gmem_stride) {
+              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1593,6 +1593,7 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
         h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
     }
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
+    h << "#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
     h << kDmath << "\n";
     g.emit_events(h);
     if (!d.ev.empty()) h << kEvents << "\n";
@@ -1635,7 +1636,7 @@ bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err)
 }
 
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err) {
+                   std::string &err, bool high_acc) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1665,7 +1666,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
       << lit(1.0 / (p - 1.0)) << "\n";
     h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
     h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
-    h << "#define HYK_NEV 0\n#define HYK_NTEV 0\n";
+    h << "#define HYK_NEV 0\n#define HYK_NTEV 0\n#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
     h << kDmath << "\n";
     h << kCommon << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";

@@ -348,9 +348,12 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         return fail(HYK_ERR_UNSUPPORTED, "shared memory per CTA (" + std::to_string(m->smem) + ") exceeds the device limit");
 
     hyk::GenOut g;
+    const bool high_acc = (m->cfg.flags & HYK_CFG_HIGH_ACCURACY) != 0;
     if (m->team) {
-        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err)) return fail(HYK_ERR_INVALID, err);
-    } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0)) {
+        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc))
+            return fail(HYK_ERR_INVALID, err);
+    } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
+                              high_acc)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (g.n_slot != nslot) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
@@ -723,10 +726,12 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const uint32_t slots = hyk::count_slots(d, order, adjoint);
     const uint64_t gstride = (uint64_t)slots * 8 * 32 > 227u * 1024 ? 152ull * blk : 0;
     hyk::GenOut g;
+    const bool high_acc = cfg && (cfg->flags & HYK_CFG_HIGH_ACCURACY);
     if (team > 1) {
-        if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : 32, sizeof(KParams), g, err))
+        if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : 32, sizeof(KParams), g, err,
+                                high_acc))
             return fail(HYK_ERR_UNSUPPORTED, err);
-    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride)) {
+    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (n_slot) *n_slot = g.n_slot;

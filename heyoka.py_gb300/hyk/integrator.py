@@ -11,9 +11,10 @@ follow from living on a GPU:
   reference.  ``time``, ``dtime``, ``tc``, ``last_h``, ``d_output`` are
   read-only NumPy copies, as read-only as the reference's.
 * ``batch_size`` is the number of GPU lanes: any size, not the SIMD width.
-* Step callbacks, events, ``high_accuracy``, single precision and the
-  variational API raise ``NotImplementedError``; LLVM code-generation options
-  are accepted and ignored.
+* Step callbacks and single precision raise ``NotImplementedError``; LLVM
+  code-generation options are accepted and ignored.  Events run on the
+  device; their callbacks run on the host when the step or propagation
+  returns (``hyk/events.py``).
 * ``propagate_*`` run every lane to its own final time in one persistent
   kernel launch (``prop_mode="persistent"``, the default) or with one kernel
   launch per step (``prop_mode="plain"``).  Per-lane results follow the
@@ -167,8 +168,7 @@ class taylor_adaptive_batch:
             raise TypeError("unexpected keyword argument(s): {}".format(", ".join(sorted(kwargs))))
         if fp_type not in (float, np.float64):
             raise NotImplementedError("the GPU batch integrator supports double precision (fp_type=float) only")
-        if high_accuracy:
-            raise NotImplementedError("high_accuracy mode is not supported by the GPU batch integrator")
+        self._high_accuracy = bool(high_accuracy)
         from .events import nt_event_batch, t_event_batch
 
         t_events, nt_events = list(t_events), list(nt_events)
@@ -248,7 +248,8 @@ class taylor_adaptive_batch:
         self._order = order_from_tol(tol)
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
-        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size, persist_ctas)
+        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size, persist_ctas,
+                               self._high_accuracy)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)
@@ -311,11 +312,11 @@ class taylor_adaptive_batch:
 
     @property
     def high_accuracy(self):
-        return False
+        return self._high_accuracy
 
     @property
     def with_events(self):
-        return False
+        return bool(self._t_events or self._nt_events)
 
     @property
     def decomposition(self):
@@ -978,7 +979,7 @@ class taylor_adaptive_batch:
         self.__dict__.setdefault("_t_events", [])
         self.__dict__.setdefault("_nt_events", [])
         self._tdev = dev
-        self._mod = get_module(self._dec, self._order, self._dev)
+        self._mod = get_module(self._dec, self._order, self._dev, high_accuracy=self.__dict__.get("_high_accuracy", False))
 
     def __repr__(self):
         return (

@@ -268,7 +268,11 @@ template <typename T> struct Batch {
     std::vector<T> s_acc, s_num, s_tmp, s_den;  // per-lane scratch rows
     T rhofac;
 
-    Batch(const Dec &dd, uint32_t order, uint32_t b, int md) : d(dd), p(order), B(b), nu(dd.n_u()), mode(md) {
+    int ha = 0;  // high accuracy: compensated summation in the state update
+
+    // md: bit 0 = gpu arithmetic, bit 1 = high accuracy.
+    Batch(const Dec &dd, uint32_t order, uint32_t b, int md)
+        : d(dd), p(order), B(b), nu(dd.n_u()), mode(md & 1), ha((md >> 1) & 1) {
         J.assign((size_t)nu * (p + 1) * B, T(0));
         KA.assign((size_t)nu * (p + 1) * B, T(0));
         I0.assign((size_t)nu * B, T(0));
@@ -621,8 +625,30 @@ template <typename T> struct Batch {
         }
     }
 
-    // Horner evaluation of the state polynomials at offsets dt (per lane).
+    // State polynomials at offsets dt (per lane): Horner's rule, or in
+    // high-accuracy mode the terms x_n dt^n (powers by repeated
+    // multiplication) summed from n = p down to 0 with Kahan's compensation.
     void horner(const T *dt, T *out /*[n_eq][B]*/) {
+        if (ha) {
+            std::vector<T> t(p + 1);
+            for (uint32_t i = 0; i < d.n_eq; ++i)
+                for (uint32_t l = 0; l < B; ++l) {
+                    T hp = T(1);
+                    for (uint32_t n = 0; n <= p; ++n) {
+                        t[n] = jr(i, n)[l] * hp;
+                        hp = hp * dt[l];
+                    }
+                    T sm = T(0), c = T(0);
+                    for (uint32_t n = p + 1; n-- > 0;) {
+                        const T y = t[n] - c;
+                        const T u = sm + y;
+                        c = (u - sm) - y;
+                        sm = u;
+                    }
+                    out[(size_t)i * B + l] = sm;
+                }
+            return;
+        }
         for (uint32_t i = 0; i < d.n_eq; ++i)
             for (uint32_t l = 0; l < B; ++l) {
                 T acc = jr(i, p)[l];

@@ -234,3 +234,18 @@ def test_quad_reference_error_kepler(oracle):
     d.propagate_until(10.0)
     q.propagate_until(10.0)
     assert np.max(traj_rel_err(d.state, q.state)) < 1e-12
+
+
+def test_high_accuracy_oracle_close_to_quad(oracle):
+    """The oracle's high-accuracy mode (compensated summation in the state
+    update) stays within 1e-12 of the binary128 restatement over 20 time
+    units of Kepler orbits, like the default mode."""
+    from hyk import workloads as W
+
+    st = W.kepler_ics(8, seed=52)
+    q = oracle.Oracle(W.kepler_sys(), st, order=38, prec=1, mode=0)
+    q.propagate_until(20.0)
+    for mode in (1, 3):
+        o = oracle.Oracle(W.kepler_sys(), st, order=19, mode=mode)
+        o.propagate_until(20.0)
+        assert np.max(np.abs(o.state - q.state)) < 1e-12
