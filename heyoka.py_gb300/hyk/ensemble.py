@@ -111,6 +111,8 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             raise TypeError("propagate_{}() got an unexpected keyword argument '{}'".format(tp, k))
     if kwargs.get("callback") is not None:
         raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
+    if ta.with_events:
+        raise NotImplementedError("ensemble propagations of integrators with events are not supported on the GPU")
     if n_iter == 0:
         return []
     B = ta.batch_size

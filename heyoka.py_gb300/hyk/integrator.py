@@ -54,16 +54,44 @@ class taylor_outcome(enum.IntEnum):
 
     @classmethod
     def _missing_(cls, value):
-        # A terminal event stops a lane with the event's index (>= 0) as outcome.
-        if isinstance(value, int) and value >= 0:
+        # Terminal events: a step reports the event's index k >= 0, a
+        # propagation stopped by it reports -k - 1.
+        if isinstance(value, int) and value > cls.success:
             pseudo = int.__new__(cls, value)
-            pseudo._name_ = "terminal_event_{}".format(value)
+            pseudo._name_ = "terminal_event_{}".format(value if value >= 0 else -value - 1)
             pseudo._value_ = value
             return cls._value2member_map_.setdefault(value, pseudo)
         return None
 
 
 _LLVM_KWARGS = ("opt_level", "force_avx512", "slp_vectorize", "fast_math", "code_model", "parjit")
+
+
+class code_model(enum.IntEnum):
+    """LLVM code models, accepted for compatibility (heyoka/core.cpp code_model)."""
+
+    tiny = 0
+    small = 1
+    kernel = 2
+    medium = 3
+    large = 4
+
+
+class _LLVMStateInfo:
+    """What ``llvm_state`` reports for a GPU integrator: the LLVM options it
+    was constructed with (they do not affect the CUDA code), and the
+    generated CUDA source in place of the IR."""
+
+    def __init__(self, ta, opts):
+        self._ta = ta
+        self.__dict__.update(opts)
+
+    def get_ir(self):
+        return self._ta._mod.source
+
+    def __repr__(self):
+        return "GPU module (NVRTC, sm_103a); LLVM options: {}".format(
+            {k: v for k, v in self.__dict__.items() if not k.startswith("_")})
 
 
 def _to_f64_array(x, what):
@@ -158,12 +186,15 @@ class taylor_adaptive_batch:
         persist_ctas=0,
         **kwargs,
     ):
+        llvm = {"opt_level": 3, "force_avx512": False, "slp_vectorize": False, "fast_math": False,
+                "code_model": code_model.small, "parjit": False}
         for k in list(kwargs):
             if k in _LLVM_KWARGS:
-                kwargs.pop(k)
+                llvm[k] = kwargs.pop(k)
                 warnings.warn(
                     "the LLVM option '{}' has no effect on the GPU batch integrator".format(k), stacklevel=2
                 )
+        self._llvm = llvm
         if kwargs:
             raise TypeError("unexpected keyword argument(s): {}".format(", ".join(sorted(kwargs))))
         if fp_type not in (float, np.float64):
@@ -200,6 +231,8 @@ class taylor_adaptive_batch:
         evs = [(e.expression, True, int(e.direction), e.cooldown) for e in self._t_events]
         evs += [(e.expression, False, int(e.direction), -1.0) for e in self._nt_events]
         self._dec = taylor_decompose(sys, events=evs)
+        if st.shape[0] == 0:
+            st = np.zeros((self._dec.n_eq, B))  # an empty initial state means zeros (the reference's rule)
         if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
             # the variational part starts from the identity (state arguments) and zero (parameters)
             st = np.concatenate([st, self._vsys.initial_variational_state(B)])
@@ -311,6 +344,10 @@ class taylor_adaptive_batch:
         return self._compact_mode
 
     @property
+    def llvm_state(self):
+        return _LLVMStateInfo(self, self.__dict__.get("_llvm", {}))
+
+    @property
     def high_accuracy(self):
         return self._high_accuracy
 
@@ -407,6 +444,40 @@ class taylor_adaptive_batch:
         mn, mx = p["min_h"].cpu().numpy(), p["max_h"].cpu().numpy()
         ns = p["n_steps"].cpu().numpy()
         return [(taylor_outcome(int(a)), float(b), float(c), int(d)) for a, b, c, d in zip(oc, mn, mx, ns)]
+
+    @property
+    def te_cooldowns(self):
+        """Per lane, per terminal event: None, or (time of the last trigger,
+        cooldown) while the event's cooldown applies (reference:
+        heyoka/expose_batch_integrators.cpp te_cooldowns)."""
+        if self._ev is None:
+            return [[] for _ in range(self._B)]
+        last = self._ev["last"].cpu().numpy()
+        out = []
+        for b in range(self._B):
+            row = []
+            for j, e in enumerate(self._t_events):
+                t = float(last[j, b])
+                if t != t:
+                    row.append(None)
+                else:
+                    cd = e.cooldown if e.cooldown >= 0 else 1e-12 * max(1.0, abs(t))
+                    row.append((t, cd))
+            out.append(row)
+        return out
+
+    def reset_cooldowns(self, i=None):
+        """Forget the terminal events' cooldowns, of lane ``i`` or of every lane."""
+        if self._ev is None:
+            return
+        if i is None:
+            self._ev["last"].fill_(math.nan)
+        else:
+            i = int(i)
+            if not 0 <= i < self._B:
+                raise ValueError("Cannot reset the cooldowns at batch index {}: the batch size is only {}".format(
+                    i, self._B))
+            self._ev["last"][:, i] = math.nan
 
     @property
     def t_events(self):
@@ -745,7 +816,7 @@ class taylor_adaptive_batch:
                     if bool(evl.any()):
                         idx = torch.nonzero(evl).flatten().cpu().numpy()
                         ks = p["outcome"][evl].cpu().numpy()
-                        resume = self._ev_terminal({int(b): int(k) for b, k in zip(idx, ks)})
+                        resume = self._ev_terminal({int(b): -int(k) - 1 for b, k in zip(idx, ks)})
                 if not grow and not resume:
                     break
                 if grow and c_output and bool((p["n_iter"] >= cap).any()):

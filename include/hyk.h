@@ -256,7 +256,8 @@ typedef struct hyk_prop {
 #define HYK_LANE_DONE 1u     /* reached the final time */
 #define HYK_LANE_STOPPED 2u  /* stopped early: error, step limit, capacity or terminal event */
 #define HYK_LANE_CAPACITY 4u /* stopped because tc_capacity, ck_capacity or ev_capacity was reached (resumable) */
-#define HYK_LANE_EVENT 8u    /* stopped by a terminal event (outcome = its index) */
+#define HYK_LANE_EVENT 8u    /* stopped by a terminal event (propagation outcome = -(its index) - 1;
+                                hyk_step reports the index itself) */
 
 /* Initialise the bookkeeping arrays of `p` for a propagation to tf. */
 int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, void *stream);

@@ -987,6 +987,7 @@ int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const doub
             if (kt >= 0) {
                 ev_last[(size_t)kt * B + l] = t.hi;
                 ev_sign[l] = sgt;
+                oc = -(int64_t)kt - 1;
                 st = HYK_LANE_STOPPED | HYK_LANE_EVENT;
                 break;
             }

@@ -140,7 +140,7 @@ def test_oracle_events_harmonic_oscillator(oracle):
         assert np.allclose(np.sort(tv), want, atol=1e-13)
     # terminal: stops at the first root, direction and cooldown respected
     r = oracle.propagate_ev(sys_, [(x, True, 1, -1.0)], st, 20.0, order=20)
-    assert list(r["outcome"]) == [0, 0, 0]
+    assert list(r["outcome"]) == [-1, -1, -1]  # a propagation stopped by terminal event k reports -k - 1
     assert np.allclose(r["t_hi"], [1.5 * math.pi, 1.5 * math.pi, 0.5 * math.pi], atol=1e-13)
     assert list(r["ev_sign"]) == [1, 1, 1]
     r2 = oracle.propagate_ev(sys_, [(x, True, 1, -1.0)], r["state"], 20.0, order=20, time=r["t_hi"],

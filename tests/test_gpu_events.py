@@ -185,3 +185,64 @@ def test_terminal_events_bitwise_vs_oracle(oracle):
     assert np.array_equal(ta.time, r2["t_hi"])
     assert np.array_equal(np.asarray(ta.state), r2["state"])
     assert np.all(ta.time > r["t_hi"])
+
+
+def test_reference_propagate_outcome_and_cooldowns():
+    """heyoka/_test_batch_integrator.py:560-600: a terminal event without
+    callback stops propagate_until with outcome -1; te_cooldowns and
+    reset_cooldowns per lane."""
+    x, v, sys_ = pend()
+
+    def cb0(ta, t, d_sgn, bidx):
+        pass
+
+    ta = hyk.taylor_adaptive_batch(sys_, np.array([[0.0, 0.001], [0.25, 0.2501]]),
+                                   nt_events=[nt_event_batch(v * v - 1e-6, cb0)], t_events=[t_event_batch(v)])
+    assert ta.with_events and len(ta.t_events) == 1 and len(ta.nt_events) == 1
+    ta.propagate_until([1e9, 1e9])
+    assert all(int(r[0]) == -1 for r in ta.propagate_res)
+    assert ta.te_cooldowns[0][0] is not None and ta.te_cooldowns[1][0] is not None
+    ta.reset_cooldowns(0)
+    assert ta.te_cooldowns[0][0] is None and ta.te_cooldowns[1][0] is not None
+    ta.reset_cooldowns()
+    assert ta.te_cooldowns[0][0] is None and ta.te_cooldowns[1][0] is None
+
+
+def test_reference_event_pickling():
+    """heyoka/_test_batch_integrator.py:605-690: integrators with events
+    survive pickling, stateful callbacks included."""
+    import pickle
+
+    pytest.importorskip("cloudpickle")
+    x, v, sys_ = pend()
+
+    def cb0(ta, t, d_sgn, bidx):
+        pass
+
+    ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]]),
+                                   nt_events=[nt_event_batch(v * v - 1e-6, cb0)])
+    for _ in range(4):
+        ta.step()
+    ta2 = pickle.loads(pickle.dumps(ta))
+    assert np.all(np.asarray(ta.state) == np.asarray(ta2.state)) and np.all(ta.time == ta2.time)
+    assert len(ta.nt_events) == len(ta2.nt_events)
+    ta.step()
+    ta2.step()
+    assert np.all(np.asarray(ta.state) == np.asarray(ta2.state))
+
+    class cb1:
+        def __init__(self):
+            self.n = 0
+
+        def __call__(self, ta, d_sgn, bidx):
+            self.n += 1
+            return True
+
+    clb = cb1()
+    ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]]),
+                                   t_events=[t_event_batch(v, callback=clb)])
+    assert id(clb) != id(ta.t_events[0].callback) and ta.t_events[0].callback.n == 0
+    ta.propagate_until([100.0, 100.0])
+    assert ta.t_events[0].callback.n > 0
+    ta2 = pickle.loads(pickle.dumps(ta))
+    assert ta.t_events[0].callback.n == ta2.t_events[0].callback.n
