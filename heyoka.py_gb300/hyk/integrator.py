@@ -389,6 +389,70 @@ class taylor_adaptive_batch:
             raise ValueError("The integrator is not variational")
         return self._vsys.mindex(i)
 
+    def _tstate_buf(self):
+        buf = self.__dict__.get("_tstate")
+        if buf is None:
+            buf = np.zeros((self.n_orig_sv, self._B))
+            self._tstate = buf
+        return buf
+
+    @property
+    def tstate(self):
+        """The result of the last ``eval_taylor_map`` (read-only, shape (n_orig_sv, batch_size))."""
+        if self._vsys is None:
+            raise ValueError("The integrator is not variational")
+        v = self._tstate_buf().view()
+        v.flags.writeable = False
+        return v
+
+    def eval_taylor_map(self, inputs):
+        """Evaluate the Taylor map of the variational state at the argument
+        displacements ``inputs`` (shape (n_vargs, batch_size)): for every
+        original state variable, sum over the multi-indices alpha of
+        X_alpha delta^alpha / alpha! (reference:
+        heyoka/expose_batch_integrators.cpp:549-649).  Returns ``tstate``."""
+        if self._vsys is None:
+            raise ValueError("The integrator is not variational")
+        m, B = len(self._vsys.vargs), self._B
+        if isinstance(inputs, torch.Tensor):
+            if inputs.device.type == "cuda" and inputs.untyped_storage().data_ptr() == \
+                    self._state.untyped_storage().data_ptr():
+                raise ValueError("The array of inputs provided for the evaluation of a Taylor map may overlap "
+                                 "with the internal state of the integrator")
+            inputs = inputs.detach().cpu().numpy()
+        arr = np.asarray(inputs)
+        if arr.dtype != np.float64:
+            if np.issubdtype(arr.dtype, np.integer) and isinstance(inputs, np.ndarray):
+                raise TypeError("Invalid dtype detected for the inputs of a Taylor map evaluation: the expected "
+                                "dtype is float64, but the dtype is {} instead".format(arr.dtype))
+            arr = arr.astype(np.float64)
+        if isinstance(inputs, np.ndarray) and not inputs.flags.c_contiguous:
+            raise ValueError("Invalid inputs array detected in a Taylor map evaluation: the array is not C-style "
+                             "contiguous, please consider using numpy.ascontiguousarray() to turn it into one")
+        if arr.ndim != 2:
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map has {} dimension(s), "
+                             "but it must have 2 dimensions instead".format(arr.ndim))
+        if arr.shape[0] != m:
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map has {} row(s), but it "
+                             "must have {} row(s) instead".format(arr.shape[0], m))
+        if arr.shape[1] != B:
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map has {} column(s), but "
+                             "it must have {} column(s) instead".format(arr.shape[1], B))
+        buf = self._tstate_buf()
+        if np.shares_memory(arr, buf):
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map may overlap with "
+                             "the internal state of the integrator")
+        st = self._state.cpu().numpy()
+        out = np.zeros((self.n_orig_sv, B))
+        for row, comp, a, inv_fact in self._vsys.taylor_map_terms():
+            term = st[row] * inv_fact
+            for j, e in enumerate(a):
+                if e:
+                    term = term * arr[j] ** e
+            out[comp] += term
+        buf[...] = out
+        return self.tstate
+
     @property
     def device(self):
         return self._tdev

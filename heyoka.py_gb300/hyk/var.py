@@ -1,23 +1,31 @@
-"""First-order variational equations: ``var_ode_sys(sys, args, order=1)``.
+"""Variational equations: ``var_ode_sys(sys, args, order)``.
 
 Restates the reference's variational ODE construction
 (heyoka/expose_var_ode_sys.cpp:29-59, batch variational API
-heyoka/expose_batch_integrators.cpp:549-649) at order 1: the system is
-augmented with the sensitivities dx_i/d(arg_j) of every state variable with
-respect to the chosen arguments (initial values of state variables and/or
-runtime parameters),
+heyoka/expose_batch_integrators.cpp:549-649): the system is augmented with
+the partial derivatives of every state variable with respect to the chosen
+arguments (initial values of state variables and/or runtime parameters) up to
+the given order.  With X_{i,alpha} = d^|alpha| x_i / d a^alpha for a
+multi-index alpha over the m arguments,
 
-    d/dt (dx_i/da_j) = sum_k (df_i/dx_k) (dx_k/da_j) + df_i/da_j,
+    d/dt X_{i,e_j} = D_j f_i,   d/dt X_{i,alpha} = D_k (d/dt X_{i,alpha - e_k}),
 
-with the layout the reference's tests pin (heyoka/_test_var_integrator.py:
-190-201): the original state first, then for each component i and each
-argument j in order, dx_i/da_j.  Initial values: the identity for state
-arguments, zero for parameters.
+where k is the last argument with alpha_k > 0 and D_k is the total
+derivative along argument k: D_k g = sum over the variables v of g of
+(dg/dv) (dv/da_k) + dg/da_k (a_k a parameter), with dx_l/da_k = X_{l,e_k} and
+dX_{l,beta}/da_k = X_{l,beta + e_k}.
+
+Layout (heyoka/_test_var_integrator.py:54-65 pins it up to order 1): the
+original state, then for each order 1, 2, ... and each component i, the
+multi-indices of that order in decreasing lexicographic order ((1,0) before
+(0,1); (2,0), (1,1), (0,2) at order 2).  Initial values: the identity for
+state arguments at order 1, zero otherwise.
 """
 
 from __future__ import annotations
 
 import enum
+import math
 
 from . import expr as _e
 
@@ -29,10 +37,28 @@ class var_args(enum.IntFlag):
     all = 7
 
 
+def _multi_indices(m, r):
+    """The multi-indices of total order r over m arguments, decreasing lexicographic."""
+    out = []
+
+    def rec(prefix, left, k):
+        if k == m - 1:
+            out.append(prefix + [left])
+            return
+        for a in range(left, -1, -1):
+            rec(prefix + [a], left - a, k + 1)
+
+    if m == 0:
+        return [] if r else [[]]
+    rec([], r, 0)
+    return out
+
+
 class var_ode_sys:
     def __init__(self, sys, args=var_args.vars, order=1):
-        if order != 1:
-            raise NotImplementedError("only first-order variational equations are supported")
+        order = int(order)
+        if order < 1:
+            raise ValueError("The order of a variational ODE system must be at least 1")
         pairs = [(_e._ex(l), _e._ex(r)) for l, r in sys]
         xs = [l for l, _ in pairs]
         if isinstance(args, var_args):
@@ -56,48 +82,111 @@ class var_ode_sys:
                 if not (a.kind == _e.PAR or (a.kind == _e.VAR and a in xs)):
                     raise ValueError("variational arguments must be state variables or parameters")
         n, m = len(pairs), len(vargs)
-        dvars = [[_e.make_vars("d_{}_{}".format(i, j)) for j in range(m)] for i in range(n)]
-        jac = [[_e.diff(f, x) for x in xs] for _, f in pairs]
-        out = list(pairs)
-        for i, (_, f) in enumerate(pairs):
-            for j, a in enumerate(vargs):
-                terms = [jac[i][k] * dvars[k][j] for k in range(n)]
-                if a.kind == _e.PAR:
-                    terms.append(_e.diff(f, a))
-                out.append((dvars[i][j], _e.sum(terms)))
-        self.sys = out
-        self.vargs = vargs
         self.n_orig_sv = n
-        self.order = 1
+        self.vargs = vargs
+        self.order = order
+        # multi-indices per order, and the variable of each (component, multi-index)
+        self._mi = {r: _multi_indices(m, r) for r in range(1, order + 1)}
+        var_of = {}
+        for r in range(1, order + 1):
+            for i in range(n):
+                for a in self._mi[r]:
+                    var_of[(i, tuple(a))] = _e.make_vars("d_{}_{}".format(i, "_".join(map(str, a))))
+        self._var_of = var_of
+        # d(variable)/d(a_k) for the variables of the augmented state
+        xidx = {x.value: i for i, x in enumerate(xs)}
+        vidx = {v.value: key for key, v in var_of.items()}
+
+        def dvar(v, k):
+            e = [0] * m
+            e[k] = 1
+            if v.value in xidx:
+                return var_of[(xidx[v.value], tuple(e))]
+            i, a = vidx[v.value]
+            b = tuple(x + y for x, y in zip(a, e))
+            return var_of.get((i, b))  # None beyond the order (never needed)
+
+        def total(g, k):
+            terms = []
+            for name in _e.get_variables(g):
+                v = _e.expression(name)
+                dg = _e.diff(g, v)
+                if dg.kind == _e.NUM and dg.value == 0.0:
+                    continue
+                terms.append(dg * dvar(v, k))
+            a = vargs[k]
+            if a.kind == _e.PAR:
+                terms.append(_e.diff(g, a))
+            return _e.sum(terms)
+
+        rhs = {}
+        out = list(pairs)
+        for r in range(1, order + 1):
+            for i in range(n):
+                for a in self._mi[r]:
+                    k = max(j for j in range(m) if a[j] > 0)
+                    if r == 1:
+                        g = total(pairs[i][1], k)
+                    else:
+                        b = list(a)
+                        b[k] -= 1
+                        g = total(rhs[(i, tuple(b))], k)
+                    rhs[(i, tuple(a))] = g
+                    out.append((var_of[(i, tuple(a))], g))
+        self.sys = out
 
     def initial_variational_state(self, B):
-        """The (n * m, B) initial values of the sensitivities."""
+        """The initial values of the derivatives, shape (n_derivatives, B)."""
         import numpy as np
 
         n, m = self.n_orig_sv, len(self.vargs)
-        out = np.zeros((n * m, B))
-        for i in range(n):
-            for j, a in enumerate(self.vargs):
-                if a.kind == _e.VAR and a == self.sys[i][0]:
-                    out[i * m + j] = 1.0
-        return out
+        rows = []
+        for r in range(1, self.order + 1):
+            for i in range(n):
+                for a in self._mi[r]:
+                    one = r == 1 and self.vargs[a.index(1)].kind == _e.VAR and self.vargs[a.index(1)] == self.sys[i][0]
+                    rows.append(np.full(B, 1.0 if one else 0.0))
+        return np.stack(rows) if rows else np.zeros((0, B))
+
+    def _count(self, r):
+        return len(self._mi[r]) if r >= 1 else 1
 
     def vslice(self, order, component=None):
-        n, m = self.n_orig_sv, len(self.vargs)
+        n = self.n_orig_sv
+        if order < 0 or order > self.order:
+            raise ValueError("invalid variational order")
         if order == 0:
             return slice(0, n) if component is None else slice(component, component + 1)
-        if order == 1:
-            if component is None:
-                return slice(n, n + n * m)
-            return slice(n + component * m, n + (component + 1) * m)
-        raise ValueError("invalid variational order")
+        start = n + sum(n * self._count(r) for r in range(1, order))
+        c = self._count(order)
+        if component is None:
+            return slice(start, start + n * c)
+        if not 0 <= component < n:
+            raise ValueError("invalid component")
+        return slice(start + component * c, start + (component + 1) * c)
 
     def mindex(self, i):
         n, m = self.n_orig_sv, len(self.vargs)
         if i < n:
             return [i] + [0] * m
         k = i - n
-        comp, arg = divmod(k, m)
-        out = [comp] + [0] * m
-        out[1 + arg] = 1
+        for r in range(1, self.order + 1):
+            c = self._count(r)
+            if k < n * c:
+                comp, j = divmod(k, c)
+                return [comp] + list(self._mi[r][j])
+            k -= n * c
+        raise ValueError("index out of range")
+
+    def taylor_map_terms(self):
+        """(state row, component, multi-index, 1/alpha!) for every term of the Taylor map."""
+        out = []
+        total = self.n_orig_sv + sum(self.n_orig_sv * self._count(r) for r in range(1, self.order + 1))
+        for row in range(total):
+            mi = self.mindex(row)
+            a = mi[1:]
+            fact = 1.0
+            for x in a:
+                fact *= math.factorial(x)
+            out.append((row, mi[0], a, 1.0 / fact))
         return out

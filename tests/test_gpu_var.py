@@ -1,0 +1,73 @@
+"""The batch variational API on the GPU (heyoka/_test_var_integrator.py:144-258):
+an order-2 variational system, its properties, ``tstate`` and
+``eval_taylor_map``, and bit-for-bit parity of the augmented state with the
+oracle."""
+
+from sys import getrefcount
+
+import numpy as np
+import pytest
+
+import hyk
+from hyk import var
+
+pytestmark = pytest.mark.gpu
+
+
+def forced():
+    x, v = hyk.make_vars("x", "v")
+    return x, v, [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
+
+
+def test_reference_batch_variational(oracle):
+    x, v, orig = forced()
+    vsys = var.var_ode_sys(orig, var.var_args.vars, order=2)
+    ta = hyk.taylor_adaptive_batch(vsys, [[0.2, 0.21], [0.3, 0.31]], pars=[[0.4, 0.41]], time=[0.5, 0.51],
+                                   compact_mode=True)
+    assert ta.dim > 2 and ta.n_orig_sv == 2 and ta.is_variational and ta.vorder == 2 and ta.vargs == [x, v]
+    rc = getrefcount(ta)
+    ts = ta.tstate
+    assert ts.shape == (2, 2) and np.all(ts == 0.0)
+    with pytest.raises(ValueError):
+        ta.tstate[0] = 0.5
+    assert ta.get_vslice(order=1) == slice(2, 6) and ta.get_vslice(order=1, component=1) == slice(4, 6)
+    assert ta.get_mindex(4) == [1, 1, 0] and ta.get_mindex(i=5) == [1, 0, 1]
+    ta.propagate_until(3.0)
+    ts2 = ta.eval_taylor_map([[0.0, 0.0], [0.0, 0.0]])
+    assert np.shares_memory(ts, ts2)
+    assert np.all(ts2 == np.asarray(ta.state)[:2])
+    ts2 = ta.eval_taylor_map(np.array([[0.0, 0.0], [0.0, 0.0]]))
+    assert np.all(ts2 == np.asarray(ta.state)[:2])
+    with pytest.raises(TypeError, match="Invalid dtype detected for the inputs of a Taylor map evaluation:"):
+        ta.eval_taylor_map(np.array([[0, 0], [0, 0]], dtype=np.int32))
+    with pytest.raises(ValueError, match="the array is not C-style contiguous, please "):
+        ta.eval_taylor_map(np.zeros((2, 4))[:, ::2])
+    with pytest.raises(ValueError, match="has 1 dimension"):
+        ta.eval_taylor_map(np.array([0.0, 0.0]))
+    with pytest.raises(ValueError, match="has 1 row\\(s\\), but it must have 2 row\\(s\\) instead"):
+        ta.eval_taylor_map(np.array([[0.0, 0.0]]))
+    with pytest.raises(ValueError, match="has 1 column\\(s\\), but it must have 2 column\\(s\\) instead"):
+        ta.eval_taylor_map(np.array([[0.0], [0.0]]))
+    with pytest.raises(ValueError, match="may overlap"):
+        ta.eval_taylor_map(ta.state[:2])
+    with pytest.raises(ValueError, match="may overlap"):
+        ta.eval_taylor_map(ta.tstate)
+    # the augmented state equals the oracle's, bit for bit
+    full = np.concatenate([np.array([[0.2, 0.21], [0.3, 0.31]]), vsys.initial_variational_state(2)])
+    o = oracle.Oracle(vsys.sys, full, pars=[[0.4, 0.41]], time=[0.5, 0.51], order=ta.order, mode=1)
+    o.propagate_until(3.0)
+    assert np.array_equal(np.asarray(ta.state), o.state)
+
+
+def test_taylor_map_predicts_perturbed_flow():
+    x, v, orig = forced()
+    vsys = var.var_ode_sys(orig, var.var_args.vars | var.var_args.params, order=2)
+    st = np.array([[0.2, 0.25, 0.3], [0.3, 0.2, 0.1]])
+    ta = hyk.taylor_adaptive_batch(vsys, st, pars=[[0.4, 0.4, 0.4]])
+    ta.propagate_until(2.0)
+    d = np.array([[1e-3, -2e-3, 0.0], [0.0, 1e-3, -1e-3], [5e-4, 0.0, 1e-3]])
+    pred = ta.eval_taylor_map(d).copy()
+    ref = hyk.taylor_adaptive_batch(orig, st + d[:2], pars=[[0.4, 0.4, 0.4]] + d[2:3])
+    ref.propagate_until(2.0)
+    err = np.max(np.abs(pred - np.asarray(ref.state)))
+    assert err < 1e-7  # third-order remainder of displacements ~1e-3

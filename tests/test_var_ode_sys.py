@@ -82,3 +82,51 @@ def test_sensitivities_vs_finite_differences(oracle):
         b.propagate_until(3.0)
         fd = (a.state - b.state) / (2 * eps)
         assert np.max(np.abs(fd - sens[:, j, :])) < 1e-7
+
+
+def test_order2_layout():
+    vs = var.var_ode_sys(forced(), var.var_args.vars, order=2)
+    # the reference's pinned part (heyoka/_test_var_integrator.py:54-65)
+    assert vs.vslice(0) == slice(0, 2) and vs.vslice(1) == slice(2, 6) and vs.vslice(1, 1) == slice(4, 6)
+    assert [vs.mindex(i) for i in range(6)] == [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, 0, 1]]
+    # order 2: per component the multi-indices (2,0), (1,1), (0,2)
+    assert vs.vslice(2) == slice(6, 12) and vs.vslice(2, 1) == slice(9, 12)
+    assert [vs.mindex(i) for i in range(6, 12)] == [[0, 2, 0], [0, 1, 1], [0, 0, 2], [1, 2, 0], [1, 1, 1], [1, 0, 2]]
+    assert len(vs.sys) == 12 and vs.order == 2
+    init = vs.initial_variational_state(3)
+    assert init.shape == (10, 3) and np.array_equal(init[:4, 0], [1.0, 0.0, 0.0, 1.0]) and not init[4:].any()
+
+
+def test_order2_sensitivities_vs_finite_differences(oracle):
+    """Second derivatives of the flow (state and parameter arguments) against
+    central differences of the first-order sensitivities."""
+    vs2 = var.var_ode_sys(forced(), var.var_args.vars | var.var_args.params, order=2)
+    vs1 = var.var_ode_sys(forced(), var.var_args.vars | var.var_args.params, order=1)
+    st0 = np.array([[0.2, 0.21], [0.3, 0.31]])
+    pars = np.array([[0.4, 0.41]])
+    o = oracle.Oracle(vs2.sys, np.concatenate([st0, vs2.initial_variational_state(2)]), pars=pars, order=20, mode=1)
+    o.propagate_until(3.0)
+    m = 3
+    mi2 = [vs2.mindex(i) for i in range(vs2.vslice(2).start, vs2.vslice(2).stop)]
+    eps = 1e-5
+    for j in range(m):
+        plus, minus = st0.copy(), st0.copy()
+        pp, pm = pars.copy(), pars.copy()
+        if j < 2:
+            plus[j] += eps
+            minus[j] -= eps
+        else:
+            pp[0] += eps
+            pm[0] -= eps
+        a = oracle.Oracle(vs1.sys, np.concatenate([plus, vs1.initial_variational_state(2)]), pars=pp, order=20, mode=1)
+        b = oracle.Oracle(vs1.sys, np.concatenate([minus, vs1.initial_variational_state(2)]), pars=pm, order=20,
+                          mode=1)
+        a.propagate_until(3.0)
+        b.propagate_until(3.0)
+        d1 = (a.state[2:] - b.state[2:]).reshape(2, m, 2) / (2 * eps)  # d/da_j of dx_i/da_k
+        for row, mi in zip(range(vs2.vslice(2).start, vs2.vslice(2).stop), mi2):
+            comp, alpha = mi[0], mi[1:]
+            if alpha[j] == 0:
+                continue
+            k = [q for q in range(m) if alpha[q] - (1 if q == j else 0) > 0][0]
+            assert np.max(np.abs(o.state[row] - d1[comp, k])) < 1e-6, (row, mi, j)
