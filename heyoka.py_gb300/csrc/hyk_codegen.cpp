@@ -193,12 +193,20 @@ struct Gen {
     uint32_t evslot = 0;
     std::vector<char> cone;
 
+    // Operations whose arguments are all time-constant (numbers, parameters,
+    // other such operations) are constant in time: only their order-0 value
+    // exists (one slot, like a parameter) and their higher orders are known
+    // zeros, so products with them are single terms.  Gpu arithmetic only;
+    // the pinned arithmetic and the adjoint keep the full recurrences.
+    std::vector<char> cst;
+
     Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false)
         : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint),
           split((uint64_t)dd.n_ops * order > 3000), evx(!dd.ev.empty()) {
         base.resize(NU);
         negf.assign(NU, 0);
         alias.assign(NU, 0);
+        cst.assign(NU, 0);
         for (uint32_t u = 0; u < NU; ++u) base[u] = (int)u;
         for (uint32_t k = 0; k < d.n_ops; ++k) {
             const auto &op = d.ops[k];
@@ -207,6 +215,13 @@ struct Gen {
                 alias[u] = 1;
                 base[u] = base[op.a.idx];
                 negf[u] = !negf[op.a.idx];
+            }
+            if (!pin && !adj) {
+                auto kconst = [&](const hyk_arg_t &a) {
+                    return a.kind == HYK_ARG_NONE || a.kind == HYK_ARG_NUM || a.kind == HYK_ARG_PAR ||
+                           (a.kind == HYK_ARG_U && cst[base[a.idx]]);
+                };
+                cst[u] = kconst(op.a) && kconst(op.b);
             }
         }
         analyse();
@@ -225,7 +240,7 @@ struct Gen {
         }
         return r;
     }
-    static bool varying(const Ref &r) { return r.kind == HYK_ARG_U || r.kind == HYK_ARG_TIME; }
+    bool varying(const Ref &r) const { return (r.kind == HYK_ARG_U && !cst[r.u]) || r.kind == HYK_ARG_TIME; }
 
     void analyse() {
         hist.assign(NU, 0);
@@ -240,7 +255,7 @@ struct Gen {
                 if (r.kind == HYK_ARG_U) hist[r.u] = 1;
             };
             auto K = [&](const Ref &r) {
-                if (r.kind == HYK_ARG_U) needka[r.u] = 1;
+                if (r.kind == HYK_ARG_U && !cst[r.u]) needka[r.u] = 1;
             };
             switch (op.op) {
             case HYK_OP_MUL:
@@ -313,7 +328,12 @@ struct Gen {
         const bool ext = adj || evx;
         const uint32_t hl = ext ? p : (p >= 2 ? p - 1 : 1), kl = ext ? p - 1 : (p >= 3 ? p - 2 : 0);
         for (uint32_t u = N; u < NU; ++u)
-            if (hist[u] && !alias[u]) {
+            if (!alias[u] && cst[u]) {
+                hist[u] = 1;  // the order-0 value, read at every order
+                needka[u] = 0;
+                slot[u] = (int)s;
+                s += 1;
+            } else if (hist[u] && !alias[u]) {
                 slot[u] = (int)s;
                 s += hl;
             }
@@ -386,6 +406,7 @@ struct Gen {
     std::string cf(const Ref &r, uint32_t j, uint32_t n) const {
         switch (r.kind) {
         case HYK_ARG_U: {
+            if (cst[r.u] && j >= 1) return "";
             const std::string s = ucoef((uint32_t)r.u, j, n);
             return r.neg ? "(-" + s + ")" : s;
         }
@@ -402,6 +423,7 @@ struct Gen {
     std::string kcf(const Ref &r, uint32_t j, uint32_t n) const {
         switch (r.kind) {
         case HYK_ARG_U: {
+            if (cst[r.u]) return "";
             const uint32_t u = (uint32_t)r.u;
             std::string s;
             if (j == n)
@@ -425,10 +447,10 @@ struct Gen {
     // Whether the order-j coefficient (or j * a_j) of an argument can be
     // non-zero; checked before building an expression, so that no history is
     // requested for a term that vanishes.
-    static bool nz(const Ref &r, uint32_t j) {
+    bool nz(const Ref &r, uint32_t j) const {
         switch (r.kind) {
         case HYK_ARG_U:
-            return true;
+            return !cst[r.u] || j == 0;
         case HYK_ARG_TIME:
             return j <= 1;
         case HYK_ARG_NUM:
@@ -437,8 +459,8 @@ struct Gen {
         }
         return false;
     }
-    static bool knz(const Ref &r, uint32_t j) {
-        return (r.kind == HYK_ARG_U && j >= 1) || (r.kind == HYK_ARG_TIME && j == 1);
+    bool knz(const Ref &r, uint32_t j) const {
+        return (r.kind == HYK_ARG_U && !cst[r.u] && j >= 1) || (r.kind == HYK_ARG_TIME && j == 1);
     }
 
     std::string fma(const std::string &x, const std::string &y, const std::string &c) const {
@@ -475,6 +497,10 @@ struct Gen {
     void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
 
     void store_hist(uint32_t u, uint32_t n) {
+        if (u >= N && cst[u]) {
+            if (n == 0) o << "    " << smem((uint32_t)slot[u]) << " = " << vname(u, 0) << ";\n";
+            return;
+        }
         const uint32_t lim = (adj || evx) ? p : p - 1;  // stored orders: 0..lim-1
         if (u >= N && hist[u] && n + 1 <= lim) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
         if (needka[u] && n >= 1) {
@@ -488,6 +514,7 @@ struct Gen {
         const auto &op = d.ops[k];
         const uint32_t u = N + k;
         if (alias[u]) return;
+        if (cst[u] && n >= 1) return;  // known zero
         const Ref A = res(op.a), B = res(op.b);
         const std::string acc = "a" + std::to_string(u) + "_" + std::to_string(n);
         const std::string z = "0.0";
@@ -1047,7 +1074,7 @@ struct TeamGen {
         for (uint32_t u = N; u < NU; ++u)
             if (!g.alias[u]) {
                 tslot[u] = (int)s;
-                s += g.hist[u] ? HS : 1;
+                s += (g.hist[u] && !g.cst[u]) ? HS : 1;
             }
         for (uint32_t u = 0; u < NU; ++u)
             if (g.needka[u] && !g.alias[u]) {
@@ -1064,8 +1091,12 @@ struct TeamGen {
         nslot = s;
     }
 
-    static bool isK(const Ref &r) { return r.kind == HYK_ARG_NUM || r.kind == HYK_ARG_PAR; }
-    static bool isU(const Ref &r) { return r.kind == HYK_ARG_U; }
+    // A time-constant operation (Gen::cst) reads like a parameter: its value in
+    // its slot at order 0, zero above.
+    bool isK(const Ref &r) const {
+        return r.kind == HYK_ARG_NUM || r.kind == HYK_ARG_PAR || (r.kind == HYK_ARG_U && g.cst[r.u]);
+    }
+    bool isU(const Ref &r) const { return r.kind == HYK_ARG_U && !g.cst[r.u]; }
     static bool isT(const Ref &r) { return r.kind == HYK_ARG_TIME; }
 
     // Whether the team form covers an operation (operand kinds per operation).
@@ -1076,6 +1107,7 @@ struct TeamGen {
             why = std::string(m) + " at u" + std::to_string(u);
             return false;
         };
+        if (g.cst[u]) return true;  // order 0 only
         switch (op.op) {
         case HYK_OP_ADD:
         case HYK_OP_SUB:
@@ -1106,6 +1138,7 @@ struct TeamGen {
     }
 
     std::string rkey(const Ref &r) const {
+        if (r.kind == HYK_ARG_U && g.cst[r.u]) return std::string("3") + (r.neg ? "n" : "p");
         std::string k = std::to_string(r.kind);
         if (isU(r)) k += std::string(r.neg ? "n" : "p") + (g.hist[r.u] ? "h" : "c");
         return k;
@@ -1122,9 +1155,9 @@ struct TeamGen {
             if (!supported(u, err)) return false;
             const auto &op = d.ops[k];
             const Ref A = g.res(op.a), B = g.res(op.b);
-            int lv = 0;
-            if (isU(A)) lv = std::max(lv, level[A.u]);
-            if (isU(B)) lv = std::max(lv, level[B.u]);
+            int lv = 0;  // after every u-variable argument (time-constant ones included: order 0 reads them)
+            if (A.kind == HYK_ARG_U) lv = std::max(lv, level[A.u]);
+            if (B.kind == HYK_ARG_U) lv = std::max(lv, level[B.u]);
             level[u] = lv + 1;
             max_level = std::max(max_level, lv + 1);
         }
@@ -1136,7 +1169,7 @@ struct TeamGen {
             const auto &op = d.ops[k];
             const Ref A = g.res(op.a), B = g.res(op.b);
             std::string key = "op" + std::to_string(op.op) + "_" + rkey(A) + "_" + rkey(B) + "_c" +
-                              (g.hist[u] ? "h" : "c") + (g.needka[u] ? "k" : "");
+                              (g.cst[u] ? "K" : (g.hist[u] ? "h" : "c")) + (g.needka[u] ? "k" : "");
             if (op.op == HYK_OP_POW) {
                 char buf[40];
                 std::snprintf(buf, sizeof buf, "_a%a", op.b.num);
@@ -1170,7 +1203,7 @@ struct TeamGen {
         std::sort(supd.begin(), supd.end(), [](const Group &x, const Group &y) { return x.key < y.key; });
         // Descriptors, group by group.
         auto slot_of = [&](const Ref &r) {
-            if (isU(r)) return tslot[r.u];
+            if (r.kind == HYK_ARG_U) return tslot[r.u];
             if (r.kind == HYK_ARG_PAR) return (int)par_slot + r.par;
             return 0;
         };
@@ -1246,6 +1279,7 @@ struct TeamGen {
         const std::string fld = std::string("D.") + f;
         switch (r.kind) {
         case HYK_ARG_U:
+            if (g.cst[r.u]) return n0 ? wrap(r, "S[" + fld + "]") : "";
             return wrap(r, (n0 || !g.hist[r.u]) ? "S[" + fld + "]" : "S[" + fld + " + n]");
         case HYK_ARG_PAR:
             return n0 ? "S[" + fld + "]" : "";
@@ -1260,7 +1294,9 @@ struct TeamGen {
     std::string at(const Ref &r, char f, const std::string &J) const {
         return wrap(r, std::string("S[D.") + f + " + " + J + "]");
     }
-    std::string K(const Ref &r, char f) const { return r.kind == HYK_ARG_NUM ? "D.num" : std::string("S[D.") + f + "]"; }
+    std::string K(const Ref &r, char f) const {
+        return r.kind == HYK_ARG_NUM ? "D.num" : wrap(r, std::string("S[D.") + f + "]");
+    }
 
     void out(uint32_t u, bool n0, const std::string &v) {
         o << "            const double v = " << v << ";\n";
@@ -1283,6 +1319,7 @@ struct TeamGen {
 
     void emit_group_op(const Group &gr, bool n0) {
         const uint32_t u = gr.members[0];
+        if (!n0 && g.cst[u]) return;  // time-constant: order 0 only
         const auto &op = d.ops[u - N];
         const Ref A = g.res(op.a), B = g.res(op.b);
         const std::string fma_ = "__fma_rn";
@@ -1560,8 +1597,8 @@ const char *kEvents =
 
 }  // namespace
 
-uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint) {
-    Gen g(d, order, false, adjoint);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin) {
+    Gen g(d, order, pin, adjoint);
     return g.nslot;
 }
 

@@ -30,7 +30,7 @@ struct GenOut {
 
 // Shared-memory slots per lane for a decomposition at a given order (the
 // block size does not change it).
-uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pin = false);
 
 // adjoint: also emit the reverse sweep hyk_jets_bw() and the adjoint kernel
 // (and keep every history up to order p-1 for it).

@@ -259,7 +259,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
 
     const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
     const bool pin = (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0;
-    uint32_t nslot = hyk::count_slots(m->d, order, adjoint);
+    uint32_t nslot = hyk::count_slots(m->d, order, adjoint, pin);
     size_t lane_bytes = (size_t)nslot * sizeof(double);
     uint32_t blk = m->cfg.block_lanes;
 
@@ -723,7 +723,7 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
         return 0;
     }
-    const uint32_t slots = hyk::count_slots(d, order, adjoint);
+    const uint32_t slots = hyk::count_slots(d, order, adjoint, pin);
     const uint64_t gstride = (uint64_t)slots * 8 * 32 > 227u * 1024 ? 152ull * blk : 0;
     hyk::GenOut g;
     const bool high_acc = cfg && (cfg->flags & HYK_CFG_HIGH_ACCURACY);

@@ -269,6 +269,10 @@ template <typename T> struct Batch {
     T rhofac;
 
     int ha = 0;  // high accuracy: compensated summation in the state update
+    // gpu arithmetic: time-constant operations (every argument a number, a
+    // parameter or such an operation) have only an order-0 value, their
+    // higher orders are known zeros (the kernels' code generator does the same).
+    std::vector<char> cst;
 
     // md: bit 0 = gpu arithmetic, bit 1 = high accuracy.
     Batch(const Dec &dd, uint32_t order, uint32_t b, int md)
@@ -307,6 +311,16 @@ template <typename T> struct Batch {
         }
         for (uint32_t i = 0; i < d.n_eq; ++i)
             if (d.rhs[i].kind == HYK_ARG_NUM) rhs_numrow[i] = add_row(d.rhs[i].num);
+        cst.assign(nu, 0);
+        if (mode == 1)
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                const auto &o = d.ops[k];
+                auto kc = [&](const hyk_arg_t &a) {
+                    return a.kind == HYK_ARG_NONE || a.kind == HYK_ARG_NUM || a.kind == HYK_ARG_PAR ||
+                           (a.kind == HYK_ARG_U && cst[a.idx]);
+                };
+                cst[d.n_eq + k] = kc(o.a) && kc(o.b);
+            }
         // rho factor exp(-2) * exp(-0.7/(p-1)), written as 1/(e*e) * exp((-7/10)/(p-1)).
         const T e1 = M<T>::exp(T(1));
         rhofac = T(1) / (e1 * e1) * M<T>::exp((T(-7) / T(10)) / T(p - 1));
@@ -319,7 +333,7 @@ template <typename T> struct Batch {
     const T *row(const hyk_arg_t &a, int64_t nr, uint32_t j) {
         switch (a.kind) {
         case HYK_ARG_U:
-            return jr(a.idx, j);
+            return (cst[a.idx] && j >= 1) ? nullptr : jr(a.idx, j);
         case HYK_ARG_NUM:
             return j == 0 ? &numrows[(size_t)nr * B] : nullptr;
         case HYK_ARG_PAR:
@@ -333,7 +347,7 @@ template <typename T> struct Batch {
     const T *karow(const hyk_arg_t &a, uint32_t j) {
         switch (a.kind) {
         case HYK_ARG_U:
-            return kr(a.idx, j);
+            return cst[a.idx] ? nullptr : kr(a.idx, j);
         case HYK_ARG_TIME:
             return j == 1 ? ones.data() : nullptr;
         default:
@@ -385,6 +399,7 @@ template <typename T> struct Batch {
     void op_coef(uint32_t k, uint32_t n) {
         const hyk_uop_t &o = d.ops[k];
         const uint32_t u = d.n_eq + k;
+        if (cst[u] && n >= 1) return;  // known zero
         T *c = jr(u, n);
         const int64_t ra = numrow_of[2 * k], rb = numrow_of[2 * k + 1];
         std::vector<T> &acc = s_acc;

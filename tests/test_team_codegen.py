@@ -22,9 +22,9 @@ from hyk.decompose import taylor_decompose
 pd = ctypes.POINTER(ctypes.c_double)
 
 
-def _team_host(libhyk, sys_, order):
+def _team_host(libhyk, sys_, order, team=2):
     d, keep = taylor_decompose(sys_).as_c()
-    cfg = _lib.hyk_config_t(0, 0, 0, 2)
+    cfg = _lib.hyk_config_t(0, 0, 0, team)
     buf = ctypes.create_string_buffer(1 << 24)
     rc = libhyk.hyk_codegen_check(ctypes.byref(d), order, ctypes.byref(cfg), 3, buf, len(buf), None, None)
     assert rc == 0, libhyk.hyk_last_error()
@@ -46,19 +46,34 @@ def _mixed():
     ]
 
 
+def _consts():
+    # time-constant operations (only an order-0 value) feeding every kind of operation
+    x, y = hyk.make_vars("x", "y")
+    p = hyk.par
+    c1, c2 = 1.0 - p[0], hyk.exp(p[1])
+    return [
+        (x, c1 * y + c2 * hyk.sin(x) + hyk.sqrt(p[0] + 2.0) - (p[0] * 3.0) / (x + 4.0) + y / (p[1] + 1.0)),
+        (y, -x * hyk.sin(p[1]) + hyk.cos(p[0] * x) + (c1 - y) ** 2.0 + hyk.log(c2 + x * x) - c1),
+    ]
+
+
 CASES = {
     "pendulum": lambda: (W.pendulum_sys(), W.pendulum_ics(3, seed=1), None, 20),
     "kepler": lambda: (W.kepler_sys(), W.kepler_ics(3, seed=2), None, 19),
     "cr3bp": lambda: (W.cr3bp_sys(),) + W.cr3bp_ics(3, seed=3) + (19,),
     "oss": lambda: (W.oss_sys(), W.oss_ics(3, seed=4)[0], None, 19),
     "mixed": lambda: (_mixed(), np.array([[1.1, 0.9, 1.3], [0.8, 0.7, 1.2]]), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), 12),
+    "consts": lambda: (_consts(), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), 15),
 }
 
 
+@pytest.mark.parametrize("form", ["team", "lane"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_team_recurrences_bitwise_vs_oracle(libhyk, oracle, name):
+def test_team_recurrences_bitwise_vs_oracle(libhyk, oracle, name, form):
+    """Both forms' generated recurrences (lane form: the host build of the
+    per-lane code; team form: a team of one) against the oracle."""
     sys_, st, pars, order = CASES[name]()
-    H = _team_host(libhyk, sys_, order)
+    H = _team_host(libhyk, sys_, order, team=2 if form == "team" else 1)
     o = oracle.Oracle(sys_, st, pars=pars, order=order, mode=1, time=np.full(st.shape[1], 0.25))
     _, h = o.step()
     S = np.zeros(H.hyk_host_nslot())
