@@ -477,13 +477,14 @@ def run_forms(args):
     n = 65536
     cases = [
         ("oss", W.oss_sys(), W.oss_ics(n, seed=2)[0], None, 2e4, [0, 1, 4, 8, 16, 32]),
-        ("cr3bp", W.cr3bp_sys()) + W.cr3bp_ics(n, seed=3) + (50.0, [0, 1, 2, 4, 8]),
-        ("kepler", W.kepler_sys(), W.kepler_ics(4 * n, seed=1), None, 50.0, [0, 1, 2, 4]),
+        ("cr3bp", W.cr3bp_sys()) + W.cr3bp_ics(n, seed=3) + (50.0, [0, 1, 2, 4, 8, "global"]),
+        ("kepler", W.kepler_sys(), W.kepler_ics(4 * n, seed=1), None, 50.0, [0, 1, 2, 4, "global"]),
     ]
     for name, sys_, st, pars, tf, teams in cases:
         s0 = torch.tensor(st, device="cuda")
         for T in teams:
-            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=1e-15, team_size=T)
+            gj = T == "global"  # one thread per trajectory, coefficients in global memory
+            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=1e-15, team_size=1 if gj else T, global_jets=gj)
             info = ta.module_info
             ta.propagate_until(tf * 0.01)
             best = 1e30
@@ -498,6 +499,7 @@ def run_forms(args):
             steps = int(ta.propagate_res_tensors["n_steps"].sum().item())
             fl = info["flops_per_step"] * steps / best
             print(json.dumps({"system": name, "requested_team_size": T, "team_size": info["team_size"],
+                              "jets": "global" if info["smem_per_lane"] == 0 else "shared",
                               "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"],
                               "regs": info["regs_per_thread"], "s": best, "trajectory_steps_per_s": steps / best,
                               "fp64_frac_of_measured": fl / peak}), flush=True)

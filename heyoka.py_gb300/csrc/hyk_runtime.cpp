@@ -306,7 +306,13 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     // Lane form of a system whose coefficients do not fit 32 lanes of shared
     // memory: a global buffer owned by the module, one slot stride for the
     // whole fixed grid, so a warp still reads 32 consecutive doubles.
-    m->gmem = !m->team && lane_bytes * 32 > (size_t)dv.smem_optin;
+    //
+    // Also when shared memory would hold fewer than two warps per SM (or the
+    // caller asks for it): the global-memory form runs eight warps per SM,
+    // and the FP64 pipes need at least one ready warp per sub-partition.
+    const size_t smem_warps = (size_t)dv.smem_per_sm / (lane_bytes * 32 + 1024);
+    m->gmem = !m->team && (lane_bytes * 32 > (size_t)dv.smem_optin || smem_warps < 2 ||
+                           (m->cfg.flags & HYK_CFG_GLOBAL_JETS) != 0);
     if (m->team) {
         // one CTA per warp by default: finest packing of the shared memory
     } else if (m->gmem) {

@@ -32,6 +32,7 @@ HYK_MODE_PERSISTENT = 1
 HYK_CFG_PIN_ARITH = 1
 HYK_CFG_ADJOINT = 2
 HYK_CFG_HIGH_ACCURACY = 4
+HYK_CFG_GLOBAL_JETS = 8
 
 LANE_DONE, LANE_STOPPED, LANE_CAPACITY, LANE_EVENT = 1, 2, 4, 8
 OC_EV_OVERFLOW = -4294967310

@@ -184,6 +184,7 @@ class taylor_adaptive_batch:
         schedule="lpt",
         team_size=0,
         persist_ctas=0,
+        global_jets=False,
         **kwargs,
     ):
         llvm = {"opt_level": 3, "force_avx512": False, "slp_vectorize": False, "fast_math": False,
@@ -282,7 +283,7 @@ class taylor_adaptive_batch:
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
         self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size, persist_ctas,
-                               self._high_accuracy)
+                               self._high_accuracy, global_jets)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)

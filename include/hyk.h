@@ -125,6 +125,9 @@ typedef struct hyk_config {
 #define HYK_CFG_PIN_ARITH 1u /* oracle "pin" arithmetic: no FMA, divide by n (slower; for cross-checks) */
 #define HYK_CFG_ADJOINT 2u   /* also generate the adjoint (reverse-mode) kernel for hyk_adjoint() */
 #define HYK_CFG_HIGH_ACCURACY 4u /* state update by compensated summation (the reference's high_accuracy) */
+#define HYK_CFG_GLOBAL_JETS 8u   /* one thread per trajectory with the Taylor coefficients in global memory
+                                    (chosen automatically for systems that leave fewer than two warps
+                                    per SM in shared memory) */
 
 typedef struct hyk_module_info {
     uint32_t n_eq, n_pars, order, n_u;
