@@ -1332,6 +1332,7 @@ struct TeamGen {
             switch (op.op) {
             case HYK_OP_ADD: out(u, true, "(" + a + " + " + b + ")"); break;
             case HYK_OP_SUB: out(u, true, "(" + a + " - " + b + ")"); break;
+            case HYK_OP_NEG: out(u, true, "(-" + a + ")"); break;  // of a constant (a NEG of a u-variable is folded)
             case HYK_OP_MUL: out(u, true, a + " * " + b); break;
             case HYK_OP_DIV:
                 out(u, true, "(" + a + " / " + b + ")");

@@ -57,12 +57,22 @@ def _consts():
     ]
 
 
+def _var2():
+    from hyk import var
+
+    x, v = hyk.make_vars("x", "v")
+    orig = [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
+    return var.var_ode_sys(orig, var.var_args.vars | var.var_args.params, order=2)
+
+
 CASES = {
     "pendulum": lambda: (W.pendulum_sys(), W.pendulum_ics(3, seed=1), None, 20),
     "kepler": lambda: (W.kepler_sys(), W.kepler_ics(3, seed=2), None, 19),
     "cr3bp": lambda: (W.cr3bp_sys(),) + W.cr3bp_ics(3, seed=3) + (19,),
     "oss": lambda: (W.oss_sys(), W.oss_ics(3, seed=4)[0], None, 19),
     "mixed": lambda: (_mixed(), np.array([[1.1, 0.9, 1.3], [0.8, 0.7, 1.2]]), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), 12),
+    "var2": lambda: (_var2().sys, np.concatenate([np.array([[0.2, 0.21], [0.3, 0.31]]), _var2().initial_variational_state(2)]),
+                     np.array([[0.4, 0.41]]), 20),
     "consts": lambda: (_consts(), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), 15),
 }
 
