@@ -20,6 +20,7 @@ only, as in the reference.
 
 from __future__ import annotations
 
+import copy as _copy
 from collections.abc import Iterable
 
 import numpy as np
@@ -33,6 +34,9 @@ def _host_copy(ta):
     for k, v in ta.__dict__.items():
         if isinstance(v, torch.Tensor):
             new.__dict__[k] = v.detach().to("cpu", copy=True)
+        elif k == "_ev":
+            new.__dict__[k] = None if v is None else {a: (b.detach().cpu() if isinstance(b, torch.Tensor) else b)
+                                                      for a, b in v.items()}
         elif k in ("_prop", "_step_res", "_final_tc_mask", "_launch_events"):
             new.__dict__[k] = None
         else:
@@ -43,10 +47,20 @@ def _host_copy(ta):
 
 def _clone_host(tmpl):
     # A fresh host copy from the host template: CPU tensor clones only (the
-    # device is read once per ensemble, not once per iteration).
+    # device is read once per ensemble, not once per iteration).  Events are
+    # deep-copied, as the reference's per-iteration deep copy does, so every
+    # iteration has its own callback objects.
     new = object.__new__(type(tmpl))
     for k, v in tmpl.__dict__.items():
-        new.__dict__[k] = v.clone() if isinstance(v, torch.Tensor) else v
+        if isinstance(v, torch.Tensor):
+            new.__dict__[k] = v.clone()
+        elif k in ("_t_events", "_nt_events"):
+            new.__dict__[k] = _copy.deepcopy(v)
+        elif k == "_ev":
+            new.__dict__[k] = None if v is None else {a: (b.clone() if isinstance(b, torch.Tensor) else b)
+                                                      for a, b in v.items()}
+        else:
+            new.__dict__[k] = v
     return new
 
 
@@ -111,8 +125,6 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             raise TypeError("propagate_{}() got an unexpected keyword argument '{}'".format(tp, k))
     if kwargs.get("callback") is not None:
         raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
-    if ta.with_events:
-        raise NotImplementedError("ensemble propagations of integrators with events are not supported on the GPU")
     if n_iter == 0:
         return []
     B = ta.batch_size
@@ -138,6 +150,26 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     big._prop = None
     big._final_tc_mask = None
     big._launch_events = None
+    views = None
+    if ta.with_events:
+        # Event buffers for the whole batch (the cooldown state of every
+        # iteration's integrator carried over), and per-iteration integrators
+        # whose tensors are views of the batch's, for the callbacks: a
+        # callback gets its iteration's integrator and its lane within it,
+        # and what it writes (state, time) reaches the batch.
+        big._ev = big._ev_alloc(16)
+        big._ev["last"] = torch.cat([c._ev["last"] for c in copies], dim=-1).to(dev).contiguous()
+        views = []
+        for i, c in enumerate(copies):
+            sl = slice(i * B, (i + 1) * B)
+            vi = object.__new__(type(ta))
+            vi.__dict__.update(c.__dict__)
+            vi._tdev = dev
+            vi._state, vi._pars = big._state[:, sl], big._pars[:, sl]
+            vi._thi, vi._tlo = big._thi[sl], big._tlo[sl]
+            vi._ev = None
+            views.append(vi)
+        big._ev_route = (views, B)
     md = kwargs.get("max_delta_t", [])
     md = big._check_prop_args(md, None)
     ms = int(kwargs.get("max_steps", 0))
@@ -178,6 +210,12 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
         ti._step_res = None
         ti._final_tc_mask = None
         ti._launch_events = None
+        if big._ev is not None:
+            ti._ev = {a: (b[..., sl].contiguous() if isinstance(b, torch.Tensor) and a in ("last", "sign", "count")
+                          else b) for a, b in big._ev.items()}
+            for a in ("t_hi", "t_lo", "info"):
+                ti._ev[a] = big._ev[a][:, sl].contiguous()
+        ti.__dict__.pop("_ev_route", None)
         if tp == "grid":
             out.append((ti, None, np.ascontiguousarray(grid_np[:, :, i, :])))
         else:

@@ -603,6 +603,15 @@ class taylor_adaptive_batch:
         d.ev_last, d.ev_sign = ev["last"].data_ptr(), ev["sign"].data_ptr()
         return d
 
+    def _ev_target(self, b):
+        """The integrator and lane a callback for batch lane b is given: this
+        one, or in an ensemble's combined batch the lane's iteration."""
+        route = self.__dict__.get("_ev_route")
+        if route is None:
+            return self, b
+        views, B = route
+        return views[b // B], b % B
+
     def _ev_dispatch_nt(self):
         """Run the non-terminal callbacks for the recorded roots, in
         chronological order per lane, then empty the records."""
@@ -622,11 +631,12 @@ class taylor_adaptive_batch:
             th, tl, inf = hi[:n, b], lo[:n, b], info[:n, b]
             fwd = n < 2 or (th[-1] + tl[-1]) >= (th[0] + tl[0])
             order = np.lexsort((tl, th)) if fwd else np.lexsort((-tl, -th))
+            tgt, lb = self._ev_target(int(b))
             for r in order:
                 k, sg = int(inf[r]) >> 2, (int(inf[r]) & 3) - 1
-                cb = self._nt_events[k].callback
+                cb = tgt._nt_events[k].callback
                 try:
-                    cb(self, float(th[r]), sg, int(b))
+                    cb(tgt, float(th[r]), sg, lb)
                 except Exception as exc:  # noqa: BLE001 - re-raised as the reference does
                     raise callback_error(exc) from exc
 
@@ -641,11 +651,12 @@ class taylor_adaptive_batch:
         sg = self._ev["sign"].cpu().numpy()
         resume = []
         for b, k in sorted(lanes_oc.items()):
-            cb = self._t_events[k].callback
+            tgt, lb = self._ev_target(int(b))
+            cb = tgt._t_events[k].callback
             if cb is None:
                 continue
             try:
-                ret = cb(self, int(sg[b]), int(b))
+                ret = cb(tgt, int(sg[b]), lb)
             except Exception as exc:  # noqa: BLE001
                 raise callback_error(exc) from exc
             if check_bool_retval(ret):

@@ -115,3 +115,51 @@ def test_errors(setup):
     with pytest.raises(ValueError, match="parallelisation algorithm must be one of"):
         hyk.ensemble_propagate_until(ta, 20.0, 10, gen, algorithm="foo")
     assert hyk.ensemble_propagate_until(ta, 20.0, 0, gen) == []
+
+
+def test_ensemble_with_events_matches_serial():
+    """An ensemble with events runs every iteration's callbacks (deep-copied
+    per iteration) on that iteration's integrator and lane; a terminal
+    callback that changes the state (a bounce) and resumes the lane acts on
+    the combined batch.  States, times and callback records equal those of
+    the iterations run one by one."""
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, hyk.expression(-9.8))]  # a ball falling on the floor x = 0
+
+    class Rec:
+        def __init__(self):
+            self.hits = []
+
+        def __call__(self, ta, t, d_sgn, bidx):
+            self.hits.append((bidx, t, d_sgn))
+
+    class Bounce:
+        def __init__(self):
+            self.n = 0
+
+        def __call__(self, ta, d_sgn, bidx):
+            self.n += 1
+            ta.state[1, bidx] = -0.8 * float(np.asarray(ta.state)[1, bidx])
+            return True
+
+    def make():
+        return hyk.taylor_adaptive_batch(sys_, [[1.0] * 3, [0.0] * 3],
+                                         nt_events=[hyk.nt_event_batch(v, Rec())],
+                                         t_events=[hyk.t_event_batch(x, callback=Bounce(),
+                                                                     direction=hyk.event_direction.negative)])
+
+    heights = np.array([[1.0, 1.5, 2.0], [0.5, 0.7, 0.9], [1.2, 0.3, 2.5], [0.8, 1.1, 1.4]])
+
+    def gen(t, i):
+        t.set_time(0.0)
+        t.state[:] = np.stack([heights[i], np.zeros(3)])
+        return t
+
+    ret = hyk.ensemble_propagate_until(make(), 3.0, 4, gen)
+    for i, (ti, _, _) in enumerate(ret):
+        ref = gen(make(), i)
+        ref.propagate_until(3.0)
+        assert np.array_equal(np.asarray(ti.state), np.asarray(ref.state)), i
+        assert np.array_equal(ti.time, ref.time)
+        assert ti.t_events[0].callback.n == ref.t_events[0].callback.n > 0
+        assert ti.nt_events[0].callback.hits == ref.nt_events[0].callback.hits
