@@ -162,4 +162,8 @@ def test_ensemble_with_events_matches_serial():
         assert np.array_equal(np.asarray(ti.state), np.asarray(ref.state)), i
         assert np.array_equal(ti.time, ref.time)
         assert ti.t_events[0].callback.n == ref.t_events[0].callback.n > 0
-        assert ti.nt_events[0].callback.hits == ref.nt_events[0].callback.hits
+        # per lane in chronological order; the interleaving of lanes follows the kernel launches
+        assert sorted(ti.nt_events[0].callback.hits) == sorted(ref.nt_events[0].callback.hits)
+        for lane in range(3):
+            ts = [t for b, t, _ in ti.nt_events[0].callback.hits if b == lane]
+            assert ts == sorted(ts)
