@@ -281,11 +281,14 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
                                                  (adjoint ? "adjoint module" : pin ? "pin arithmetic" : terr));
         m->team = want_team;
     } else if (want_team == 0 && team_ok) {
+        // Lane form: shared memory with w warps per SM scores min(1, w / 4);
+        // global-memory coefficients (eight warps per SM) score 0.7 (measured:
+        // CR3BP 52 % of the FP64 peak against Kepler's 62 % from shared memory).
         const size_t warp_bytes = 32 * lane_bytes;
-        double best = 0.15;  // coefficients in global memory
+        double best = 0.7;
         if (warp_bytes <= (size_t)dv.smem_optin) {
             const double w = (double)((size_t)dv.smem_per_sm / (warp_bytes + 1024));
-            best = std::min(1.0, w / 4.0);
+            best = std::max(best, std::min(1.0, w / 4.0));
         }
         for (uint32_t T = 2, l = 1; T <= 32; T *= 2, ++l) {
             const size_t cta = (size_t)(32 / T) * ti.n_slot * sizeof(double);
@@ -307,11 +310,12 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     // memory: a global buffer owned by the module, one slot stride for the
     // whole fixed grid, so a warp still reads 32 consecutive doubles.
     //
-    // Also when shared memory would hold fewer than two warps per SM (or the
+    // Also when shared memory would hold fewer than four warps per SM (or the
     // caller asks for it): the global-memory form runs eight warps per SM,
-    // and the FP64 pipes need at least one ready warp per sub-partition.
+    // and each of the four FP64 pipes of an SM needs a ready warp of its own
+    // (CR3BP: 3 warps from shared memory 42 % of the FP64 peak, global 52 %).
     const size_t smem_warps = (size_t)dv.smem_per_sm / (lane_bytes * 32 + 1024);
-    m->gmem = !m->team && (lane_bytes * 32 > (size_t)dv.smem_optin || smem_warps < 2 ||
+    m->gmem = !m->team && (lane_bytes * 32 > (size_t)dv.smem_optin || smem_warps < 4 ||
                            (m->cfg.flags & HYK_CFG_GLOBAL_JETS) != 0);
     if (m->team) {
         // one CTA per warp by default: finest packing of the shared memory
