@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
-    ap.add_argument("--members", type=int, default=65536, help="oss: ensemble members")
+    ap.add_argument("--members", type=int, default=65536, help="oss, cr3bp-adjoint: trajectories")
     ap.add_argument("--team-size", type=int, default=0,
                     help="threads per trajectory (0: chosen per system, 1: lane form, 2..32: team form)")
     return ap.parse_args()
@@ -343,7 +343,7 @@ def run_cr3bp_adjoint(args):
     from hyk import adjoint
     from hyk import workloads as W
 
-    n = 65536
+    n = args.members
     st, mu = W.cr3bp_ics(n, seed=3)
     rng = np.random.default_rng(3)
     target = torch.tensor(st[:3] + rng.normal(0.0, 1e-2, (3, n)), device="cuda")
@@ -367,12 +367,12 @@ def run_cr3bp_adjoint(args):
     torch.cuda.synchronize()
     fwd, bwd = e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3
     line = {
-        "metric": "CR3BP forward + discrete adjoint, 65536 trajectories, tol 1e-15, t=0..50",
+        "metric": "CR3BP forward + discrete adjoint, {} trajectories, tol 1e-15, t=0..50".format(n),
         "value": None, "unit": "s", "n_gpus": 1, "higher_is_better": False, "dtype": "f64",
         "data": "synthetic (states near L4, seed 3)",
         "forward_s": fwd, "backward_s": bwd,
         "grad_finite": bool(torch.isfinite(x.grad).all() and torch.isfinite(p.grad).all()),
-        "config": {"workload": "cr3bp-65536 forward + adjoint"},
+        "config": {"workload": "cr3bp-{} forward + adjoint".format(n)},
     }
     line["value"] = fwd + bwd
     print(json.dumps(line), flush=True)
