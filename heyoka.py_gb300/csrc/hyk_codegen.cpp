@@ -1054,7 +1054,8 @@ struct TeamGen {
     std::string err;
     std::ostringstream o;
     // Unrolling of the convolution loops over j (the same sequence of fused
-    // multiply-adds, with the operand loads of later terms hoisted).
+    // multiply-adds, with the operand loads of later terms hoisted; 4 measured
+    // best on the 6-body problem against 1, 2 and 8).
     int ju = 4;
 
     TeamGen(const Dec &dd, uint32_t order)
@@ -1688,7 +1689,6 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
         err = tg.err;
         return false;
     }
-    if (const char *e = std::getenv("HYK_TEAM_UNROLL")) tg.ju = std::max(1, std::min(16, std::atoi(e)));
     tg.g.emit_jets();  // flop count of the same recurrences
     const double p = (double)order;
     const double e1 = std::exp(1.0);
