@@ -413,7 +413,9 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
     for (CUfunction f : {m->f_step, m->f_prop}) {
         HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
-        HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+        // Global-memory coefficients: no shared memory, the whole unified
+        // on-chip array as L1 to cache them.
+        HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, m->gmem ? 0 : 100));
     }
     HYK_CU(drv().cuFuncGetAttribute(&m->regs, CU_FUNC_ATTRIBUTE_NUM_REGS, m->f_prop));
     HYK_CU(drv().cuFuncGetAttribute(&m->local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, m->f_prop));
@@ -426,7 +428,8 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (adjoint) {
         HYK_CU(drv().cuModuleGetFunction(&m->f_adj, m->mod, "hyk_adjoint_kernel"));
         HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
-        HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100));
+        HYK_CU(drv().cuFuncSetAttribute(m->f_adj, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT,
+                                        m->gmem ? 0 : 100));
         HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->adj_ctas_per_sm, m->f_adj, (int)blk, m->smem));
         if (m->adj_ctas_per_sm < 1) return fail(HYK_ERR_UNSUPPORTED, "the adjoint kernel cannot be resident on an SM");
         if (m->gmem) {
