@@ -246,3 +246,25 @@ def test_reference_event_pickling():
     assert ta.t_events[0].callback.n > 0
     ta2 = pickle.loads(pickle.dumps(ta))
     assert ta.t_events[0].callback.n == ta2.t_events[0].callback.n
+
+
+def test_events_with_global_memory_coefficients(oracle):
+    """Events in the lane form with its coefficients in global memory (the
+    form CR3BP-sized systems get): the same roots and states as the oracle."""
+    x, v, sys_ = pend()
+    st = _ics(64, 43)
+    recs = []
+
+    def cb(ta, t, d_sgn, bidx):
+        recs.append((bidx, t, d_sgn))
+
+    ta = hyk.taylor_adaptive_batch(sys_, st, global_jets=True, nt_events=[nt_event_batch(v, cb)],
+                                   t_events=[t_event_batch(x - 0.5, direction=event_direction.positive)])
+    assert ta.module_info["smem_per_lane"] == 0
+    ta.propagate_until(6.0)
+    r = oracle.propagate_ev(sys_, [(x - 0.5, True, 1, -1.0), (v, False, 0, -1.0)], st, 6.0, order=ta.order)
+    assert np.array_equal(np.asarray(ta.state), r["state"])
+    assert np.array_equal(ta.time, r["t_hi"])
+    assert [int(o) for o, *_ in ta.propagate_res] == list(r["outcome"])
+    want = sorted((int(l), float(t), (int(i) & 3) - 1) for l, i, t in zip(r["rec_lane"], r["rec_info"], r["rec_t_hi"]))
+    assert sorted(recs) == want
