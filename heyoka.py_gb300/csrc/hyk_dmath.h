@@ -35,6 +35,10 @@
 #define HYK_DM_SQRT(x) __dsqrt_rn(x)
 #define HYK_DM_BITS(x) ((unsigned long long)__double_as_longlong(x))
 #define HYK_DM_FROM(u) __longlong_as_double((long long)(u))
+#define HYK_DM_FMAF(a, b, c) __fmaf_rn((a), (b), (c))
+#define HYK_DM_SQRTF(x) __fsqrt_rn(x)
+#define HYK_DM_FBITS(x) ((unsigned)__float_as_uint(x))
+#define HYK_DM_FFROM(u) __uint_as_float((unsigned)(u))
 #else
 #include <cmath>
 #include <cstring>
@@ -53,6 +57,20 @@ static inline double hyk_dm_from_(unsigned long long u) {
 }
 #define HYK_DM_BITS(x) hyk_dm_bits_(x)
 #define HYK_DM_FROM(u) hyk_dm_from_(u)
+static inline unsigned hyk_dm_fbits_(float x) {
+    unsigned u;
+    std::memcpy(&u, &x, sizeof u);
+    return u;
+}
+static inline float hyk_dm_ffrom_(unsigned u) {
+    float x;
+    std::memcpy(&x, &u, sizeof x);
+    return x;
+}
+#define HYK_DM_FMAF(a, b, c) std::fma((float)(a), (float)(b), (float)(c))
+#define HYK_DM_SQRTF(x) std::sqrt((float)(x))
+#define HYK_DM_FBITS(x) hyk_dm_fbits_(x)
+#define HYK_DM_FFROM(u) hyk_dm_ffrom_(u)
 #endif
 
 #define HYK_DM_NAN HYK_DM_FROM(0x7ff8000000000000ULL)
@@ -234,6 +252,151 @@ HYK_DM_FN double hyk_dm_rho(double m_p, double m_pm1, double num, double inv_p, 
     const double e2 = hyk_dm_log(m_pm1 / num) * inv_pm1;
     const double e = e2 > e1 ? e2 : e1;
     return hyk_dm_exp(-e);
+}
+
+/* ------------------------------------------------------------------ float
+ * The same methods in single precision (the float32 batch integrator), with
+ * float splits of ln 2 and pi/2 (leading parts with 12 and 9 significant bits,
+ * so their products with the reduction's integer k are exact) and series
+ * truncated for float accuracy (exp to r^7, log's atanh to s^11, sine to
+ * r^9, cosine to r^10; truncation below 0.1 ulp). */
+#define HYK_DMF_RND 12582912.0f /* 1.5 * 2^23 */
+
+HYK_DM_FN int hyk_dmf_isnan(float x) { return (HYK_DM_FBITS(x) & 0x7fffffffu) > 0x7f800000u; }
+HYK_DM_FN float hyk_dmf_pow2i(int k) { return HYK_DM_FFROM((unsigned)(k + 127) << 23); }
+
+HYK_DM_FN float hyk_dmf_exp(float x) {
+    if (hyk_dmf_isnan(x)) return x;
+    if (x > 88.72283f) return HYK_DM_FFROM(0x7f800000u);
+    if (x < -103.97208f) return 0.0f;
+    const float t = HYK_DM_FMAF(x, 1.44269502f, HYK_DMF_RND);
+    const float kf = t - HYK_DMF_RND;
+    const int k = (int)(HYK_DM_FBITS(t) & 0x7fffffu) - 0x400000; /* the mantissa holds k + 2^22 */
+    float r = HYK_DM_FMAF(-kf, 0.693115234375f, x);
+    r = HYK_DM_FMAF(-kf, 3.19461833e-05f, r);
+    float p = 1.98412698e-04f;  // 1/7!
+    p = HYK_DM_FMAF(p, r, 1.38888889e-03f);
+    p = HYK_DM_FMAF(p, r, 8.33333333e-03f);
+    p = HYK_DM_FMAF(p, r, 4.16666667e-02f);
+    p = HYK_DM_FMAF(p, r, 0.166666667f);
+    p = HYK_DM_FMAF(p, r, 0.5f);
+    p = HYK_DM_FMAF(p, r, 1.0f);
+    p = HYK_DM_FMAF(p, r, 1.0f);
+    if (k >= -126 && k <= 127) return p * hyk_dmf_pow2i(k);
+    const int k1 = k / 2, k2 = k - k1;
+    return (p * hyk_dmf_pow2i(k1)) * hyk_dmf_pow2i(k2);
+}
+
+HYK_DM_FN float hyk_dmf_log(float x) {
+    unsigned u = HYK_DM_FBITS(x);
+    if (hyk_dmf_isnan(x)) return x;
+    if (u >> 31) return (u << 1) == 0 ? -HYK_DM_FFROM(0x7f800000u) : HYK_DM_FFROM(0x7fc00000u);
+    if (u == 0) return -HYK_DM_FFROM(0x7f800000u);
+    if (u == 0x7f800000u) return x;
+    int e = 0;
+    if ((u >> 23) == 0) { /* subnormal: scale by 2^25 */
+        x = x * 33554432.0f;
+        u = HYK_DM_FBITS(x);
+        e = -25;
+    }
+    e += (int)(u >> 23) - 127;
+    float m = HYK_DM_FFROM((u & 0x007fffffu) | 0x3f800000u); /* [1, 2) */
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float f = m - 1.0f;
+    const float s = f / (2.0f + f);
+    const float t = s * s;
+    float q = 9.09090909e-02f;  // 1/11
+    q = HYK_DM_FMAF(q, t, 0.111111111f);
+    q = HYK_DM_FMAF(q, t, 0.142857143f);
+    q = HYK_DM_FMAF(q, t, 0.2f);
+    q = HYK_DM_FMAF(q, t, 0.333333333f);
+    const float a = s + s;
+    const float lm = HYK_DM_FMAF(a * t, q, a);
+    const float ef = (float)e;
+    return HYK_DM_FMAF(ef, 0.693115234375f, HYK_DM_FMAF(ef, 3.19461833e-05f, lm));
+}
+
+HYK_DM_FN void hyk_dmf_sincos(float x, float *sp, float *cp) {
+    const unsigned u = HYK_DM_FBITS(x);
+    if ((u & 0x7f800000u) == 0x7f800000u) {
+        *sp = HYK_DM_FFROM(0x7fc00000u);
+        *cp = HYK_DM_FFROM(0x7fc00000u);
+        return;
+    }
+    const float t = HYK_DM_FMAF(x, 0.636619747f, HYK_DMF_RND);
+    const float kf = t - HYK_DMF_RND;
+    const unsigned q = HYK_DM_FBITS(t) & 3u;
+    float r = HYK_DM_FMAF(-kf, 1.5703125f, x);
+    r = HYK_DM_FMAF(-kf, 4.83512878e-04f, r);
+    r = HYK_DM_FMAF(-kf, 3.13916473e-07f, r);
+    const float z = r * r;
+    float ps = 2.75573192e-06f;  // 1/9!
+    ps = HYK_DM_FMAF(ps, z, -1.98412698e-04f);
+    ps = HYK_DM_FMAF(ps, z, 8.33333333e-03f);
+    ps = HYK_DM_FMAF(ps, z, -0.166666667f);
+    const float s = HYK_DM_FMAF(r * z, ps, r);
+    float pc = -2.75573192e-07f;  // -1/10!
+    pc = HYK_DM_FMAF(pc, z, 2.48015873e-05f);
+    pc = HYK_DM_FMAF(pc, z, -1.38888889e-03f);
+    pc = HYK_DM_FMAF(pc, z, 4.16666667e-02f);
+    pc = HYK_DM_FMAF(pc, z, -0.5f);
+    const float c = HYK_DM_FMAF(z, pc, 1.0f);
+    switch (q) {
+    case 0: *sp = s; *cp = c; break;
+    case 1: *sp = c; *cp = -s; break;
+    case 2: *sp = -s; *cp = -c; break;
+    default: *sp = -c; *cp = s; break;
+    }
+}
+
+HYK_DM_FN float hyk_dmf_powi(float x, unsigned n) {
+    float r = 1.0f, b = x;
+    bool first = true;
+    while (n) {
+        if (n & 1u) {
+            r = first ? b : r * b;
+            first = false;
+        }
+        n >>= 1;
+        if (n) b = b * b;
+    }
+    return r;
+}
+
+HYK_DM_FN float hyk_dmf_pow(float x, float alpha) {
+    const float a2 = alpha + alpha;
+    const bool integral = alpha <= 64.0f && alpha >= -64.0f && alpha == (float)(int)alpha;
+    const bool half = !integral && a2 <= 129.0f && a2 >= -129.0f && a2 == (float)(int)a2;
+    if (integral) {
+        const int n = (int)alpha;
+        if (n >= 0) return hyk_dmf_powi(x, (unsigned)n);
+        return 1.0f / hyk_dmf_powi(x, (unsigned)(-n));
+    }
+    if (half) {
+        const int n2 = (int)a2;
+        const float sq = HYK_DM_SQRTF(x);
+        if (n2 > 0) {
+            const unsigned m = (unsigned)((n2 - 1) / 2);
+            return m == 0 ? sq : hyk_dmf_powi(x, m) * sq;
+        }
+        const unsigned m = (unsigned)((-n2 - 1) / 2);
+        return 1.0f / (m == 0 ? sq : hyk_dmf_powi(x, m) * sq);
+    }
+    if (x < 0.0f) return HYK_DM_FFROM(0x7fc00000u);
+    if (x == 0.0f) return alpha > 0.0f ? 0.0f : HYK_DM_FFROM(0x7f800000u);
+    /* other exponents: alpha log x loses |alpha log x| ulps in float, so
+     * through the double functions (rounded once at the end) */
+    return (float)hyk_dm_exp((double)alpha * hyk_dm_log((double)x));
+}
+
+HYK_DM_FN float hyk_dmf_rho(float m_p, float m_pm1, float num, float inv_p, float inv_pm1) {
+    const float e1 = hyk_dmf_log(m_p / num) * inv_p;
+    const float e2 = hyk_dmf_log(m_pm1 / num) * inv_pm1;
+    const float e = e2 > e1 ? e2 : e1;
+    return hyk_dmf_exp(-e);
 }
 
 #endif /* HYK_DMATH_H */

@@ -48,7 +48,20 @@ __global__ void dmath_kernel(int fn, const double *__restrict__ x, const double 
     case 2: hyk_dm_sincos(x[i], &s, &c); out[i] = s; break;
     case 3: hyk_dm_sincos(x[i], &s, &c); out[i] = c; break;
     case 4: out[i] = hyk_dm_pow(x[i], a[i]); break;
-    default: out[i] = hyk_dm_rho(x[i], a[i], 1.0, 1.0 / 20, 1.0 / 19); break;
+    case 5: out[i] = hyk_dm_rho(x[i], a[i], 1.0, 1.0 / 20, 1.0 / 19); break;
+    default: {
+        // single precision: the inputs rounded to float, the result widened
+        const float xf = (float)x[i], af = a ? (float)a[i] : 0.0f;
+        float fs, fc;
+        switch (fn) {
+        case 6: out[i] = hyk_dmf_exp(xf); break;
+        case 7: out[i] = hyk_dmf_log(xf); break;
+        case 8: hyk_dmf_sincos(xf, &fs, &fc); out[i] = fs; break;
+        case 9: hyk_dmf_sincos(xf, &fs, &fc); out[i] = fc; break;
+        case 10: out[i] = hyk_dmf_pow(xf, af); break;
+        default: out[i] = hyk_dmf_rho(xf, af, 1.0f, 1.0f / 9, 1.0f / 8); break;
+        }
+    }
     }
 }
 

@@ -770,8 +770,9 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
 }
 
 int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream) {
-    if (fn < 0 || fn > 5) return fail(HYK_ERR_INVALID, "unknown function index");
-    if (n && (!x || !out || ((fn == 4 || fn == 5) && !a))) return fail(HYK_ERR_INVALID, "null argument");
+    if (fn < 0 || fn > 11) return fail(HYK_ERR_INVALID, "unknown function index");
+    if (n && (!x || !out || ((fn == 4 || fn == 5 || fn == 10 || fn == 11) && !a)))
+        return fail(HYK_ERR_INVALID, "null argument");
     if (hyk_generic_dmath(fn, x, a, out, n, stream)) return fail(HYK_ERR_CUDA, "dmath kernel launch failed");
     return 0;
 }

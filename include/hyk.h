@@ -324,8 +324,9 @@ int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_l
 
 /* The deterministic elementary functions the kernels use, evaluated on the
  * device for validation: fn 0 exp, 1 log, 2 sin, 3 cos, 4 pow(x[i], a[i]),
- * 5 the step-size rho(m_p = x[i], m_pm1 = a[i], num = 1, order 20).
- * x, a, out are device arrays of n doubles. */
+ * 5 the step-size rho(m_p = x[i], m_pm1 = a[i], num = 1, order 20); 6..11 the
+ * same functions in single precision (inputs rounded to float, order 9 for
+ * rho), used by the float32 integrator.  x, a, out are device arrays of n doubles. */
 int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
 
 /* Device FP64 FMA throughput microbenchmark (flop/s, 2 flops per FMA), used

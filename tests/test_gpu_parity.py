@@ -59,6 +59,13 @@ def test_dmath_bitwise_gpu_vs_cpu(libhyk, oracle):
         (3, rng.uniform(-1e4, 1e4, 4096), None),
         (4, np.exp(rng.uniform(-20, 20, 4096)), rng.choice([-1.5, -0.5, 2.0, 3.0, -2.0, 0.3, 1.7], 4096)),
         (5, np.exp(rng.uniform(-80, 5, 4096)), np.exp(rng.uniform(-80, 5, 4096))),
+        # single precision (float32 integrator)
+        (6, rng.uniform(-87, 88, 4096), None),
+        (7, np.exp(rng.uniform(-80, 80, 4096)), None),
+        (8, rng.uniform(-1e3, 1e3, 4096), None),
+        (9, rng.uniform(-1e3, 1e3, 4096), None),
+        (10, np.exp(rng.uniform(-10, 10, 4096)), rng.choice([-1.5, -0.5, 2.0, 3.0, -2.0, 0.3, 1.7], 4096)),
+        (11, np.exp(rng.uniform(-30, 5, 4096)), np.exp(rng.uniform(-30, 5, 4096))),
     ]
     pd = ctypes.POINTER(ctypes.c_double)
     for fn, x, a in cases:

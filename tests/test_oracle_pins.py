@@ -249,3 +249,38 @@ def test_high_accuracy_oracle_close_to_quad(oracle):
         o = oracle.Oracle(W.kepler_sys(), st, order=19, mode=mode)
         o.propagate_until(20.0)
         assert np.max(np.abs(o.state - q.state)) < 1e-12
+
+
+def test_single_precision_functions_accuracy(oracle):
+    """The float versions of the deterministic functions (float32
+    integrator): within 2 ulp of float (pow 3, the step-size rho 4) against float64 numpy
+    on their ranges of use."""
+    import ctypes
+
+    L = oracle.lib()
+    pd = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(0)
+
+    def ev(fn, x, a=None):
+        x = np.ascontiguousarray(x, dtype=np.float32).astype(np.float64)
+        a = np.zeros_like(x) if a is None else np.ascontiguousarray(a, dtype=np.float32).astype(np.float64)
+        out = np.zeros_like(x)
+        L.hyko_dm_eval(fn, x.ctypes.data_as(pd), a.ctypes.data_as(pd), out.ctypes.data_as(pd), ctypes.c_uint64(len(x)))
+        return x, a, out
+
+    def ulps(got, ref):
+        sp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+        return np.max(np.abs(got - ref) / sp)
+
+    x, _, o = ev(6, rng.uniform(-87, 88, 20000))
+    assert ulps(o, np.exp(x)) <= 2
+    x, _, o = ev(7, np.exp(rng.uniform(-80, 80, 20000)))
+    assert ulps(o, np.log(x)) <= 2
+    x, _, o = ev(8, rng.uniform(-1e3, 1e3, 20000))
+    assert ulps(o, np.sin(x)) <= 2
+    x, _, o = ev(9, x)
+    assert ulps(o, np.cos(x)) <= 2
+    x, a, o = ev(10, np.exp(rng.uniform(-10, 10, 20000)), rng.choice([-1.5, -0.5, 2.0, 3.0, 0.3, 1.7], 20000))
+    assert ulps(o, x**a) <= 3
+    m, q, o = ev(11, np.exp(rng.uniform(-30, 5, 2000)), np.exp(rng.uniform(-30, 5, 2000)))
+    assert ulps(o, np.minimum((1 / m) ** (1 / 9), (1 / q) ** (1 / 8))) <= 4  # the step-size factor
