@@ -144,7 +144,25 @@ bool load_dec(const hyk_decomp_t *d, Dec &out, std::string &err) {
 
 namespace {
 
+// Precision of the code being generated: float for the float32 integrator.
+// Literals are then the float nearest to the value (with an f suffix), and
+// the generator's own constants (1/n, pow coefficients, the step-size
+// factor) are computed in float arithmetic, as the oracle's float mode does.
+thread_local bool g_f32 = false;
+
 std::string lit(double v) {
+    if (g_f32) {
+        const float f = (float)v;
+        if (std::isnan(f)) return "HYK_FROM_BITS(HYK_NAN_BITS)";
+        if (std::isinf(f)) return f > 0 ? "hyk_inf()" : "(-hyk_inf())";
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%.9g", (double)f);
+        std::string s(buf);
+        if (s.find_first_of(".eE") == std::string::npos) s += ".0";
+        s += "f";
+        if (f < 0 || (f == 0 && std::signbit(f))) s = "(" + s + ")";
+        return s;
+    }
     if (std::isnan(v)) return "__longlong_as_double(0x7ff8000000000000LL)";
     if (std::isinf(v)) return v > 0 ? "hyk_inf()" : "(-hyk_inf())";
     char buf[64];
@@ -153,6 +171,46 @@ std::string lit(double v) {
     if (s.find_first_of(".eE") == std::string::npos) s += ".0";
     if (v < 0 || (v == 0 && std::signbit(v))) s = "(" + s + ")";
     return s;
+}
+
+// The nearest number of the generated precision to 1/n.
+double recip(double n) { return g_f32 ? (double)(1.0f / (float)n) : 1.0 / n; }
+
+// The pow recurrence's coefficient n alpha - j (alpha + 1), in the generated precision.
+double powcoef(uint32_t n, uint32_t j, double alpha) {
+    if (g_f32) {
+        const float a = (float)alpha;
+        return (double)((float)n * a - (float)j * (a + 1.0f));
+    }
+    return (double)n * alpha - (double)j * (alpha + 1.0);
+}
+
+// The step-size safety factor exp(-2) exp(-0.7 / (p - 1)), as 1/(e e) exp((-7/10)/(p-1)).
+double rhofac_of(uint32_t p) {
+    if (g_f32) {
+        const float e1 = std::exp(1.0f);
+        return (double)(1.0f / (e1 * e1) * std::exp((-7.0f / 10.0f) / (float)(p - 1)));
+    }
+    const double e1 = std::exp(1.0);
+    return 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+}
+
+// Precision-dependent part of a generated module's header.
+std::string precision_header(bool pin) {
+    std::string h;
+    if (g_f32) {
+        h += "#define HYK_F32 1\n";
+        h += "#define HYK_FMA(a, b, c) __fmaf_rn((a), (b), (c))\n";
+        h += "#define HYK_DM_EXP hyk_dmf_exp\n#define HYK_DM_LOG hyk_dmf_log\n#define HYK_DM_SINCOS hyk_dmf_sincos\n"
+             "#define HYK_DM_POW hyk_dmf_pow\n#define HYK_DM_RHO hyk_dmf_rho\n";
+    } else {
+        h += "#define HYK_F32 0\n";
+        h += "#define HYK_FMA(a, b, c) __fma_rn((a), (b), (c))\n";
+        h += "#define HYK_DM_EXP hyk_dm_exp\n#define HYK_DM_LOG hyk_dm_log\n#define HYK_DM_SINCOS hyk_dm_sincos\n"
+             "#define HYK_DM_POW hyk_dm_pow\n#define HYK_DM_RHO hyk_dm_rho\n";
+    }
+    (void)pin;
+    return h;
 }
 
 struct Ref {
@@ -415,7 +473,7 @@ struct Gen {
         case HYK_ARG_PAR:
             return j == 0 ? "HYK_PAR(" + std::to_string(r.par) + ")" : "";
         case HYK_ARG_TIME:
-            return j == 0 ? "t0" : (j == 1 ? "1.0" : "");
+            return j == 0 ? "t0" : (j == 1 ? lit(1.0) : "");
         }
         return "";
     }
@@ -438,7 +496,7 @@ struct Gen {
             return r.neg ? "(-" + s + ")" : s;
         }
         case HYK_ARG_TIME:
-            return j == 1 ? "1.0" : "";
+            return j == 1 ? lit(1.0) : "";
         default:
             return "";
         }
@@ -465,7 +523,7 @@ struct Gen {
 
     std::string fma(const std::string &x, const std::string &y, const std::string &c) const {
         if (pin) return "(" + c + " + " + x + " * " + y + ")";
-        return "__fma_rn(" + x + ", " + y + ", " + c + ")";
+        return "HYK_FMA(" + x + ", " + y + ", " + c + ")";
     }
 
     struct Acc {
@@ -475,7 +533,7 @@ struct Gen {
     void term(Acc &a, const std::string &x, const std::string &y) {
         if (x.empty() || y.empty()) return;
         if (a.first) {
-            o << "    double " << a.name << " = " << x << " * " << y << ";\n";
+            o << "    hyk_real " << a.name << " = " << x << " * " << y << ";\n";
             a.first = false;
             flops += 1;
         } else {
@@ -486,7 +544,7 @@ struct Gen {
     std::string divn(const std::string &x, uint32_t n) {
         flops += 1;
         if (pin) return "(" + x + " / " + lit((double)n) + ")";
-        return "(" + x + " * " + lit(1.0 / (double)n) + ")";
+        return "(" + x + " * " + lit(recip((double)n)) + ")";
     }
     std::string inv0(uint32_t u) const { return "i" + std::to_string(u); }
     // After defining 1/b_0 at order 0: keep it for the later order functions.
@@ -494,7 +552,7 @@ struct Gen {
         if (split && !pin && islot[u] >= 0) o << "    " << smem((uint32_t)islot[u]) << " = " << inv0(u) << ";\n";
     }
 
-    void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const double " << vname(u, n) << " = " << expr << ";\n"; }
+    void def(uint32_t u, uint32_t n, const std::string &expr) { o << "    const hyk_real " << vname(u, n) << " = " << expr << ";\n"; }
 
     void store_hist(uint32_t u, uint32_t n) {
         if (u >= N && cst[u]) {
@@ -504,7 +562,7 @@ struct Gen {
         const uint32_t lim = (adj || evx) ? p : p - 1;  // stored orders: 0..lim-1
         if (u >= N && hist[u] && n + 1 <= lim) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
         if (needka[u] && n >= 1) {
-            o << "    const double " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
+            o << "    const hyk_real " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
             flops += 1;
             if (kslot[u] >= 0 && n + 1 <= lim) o << "    " << smem((uint32_t)kslot[u] + n - 1) << " = " << kname(u, n) << ";\n";
         }
@@ -517,7 +575,7 @@ struct Gen {
         if (cst[u] && n >= 1) return;  // known zero
         const Ref A = res(op.a), B = res(op.b);
         const std::string acc = "a" + std::to_string(u) + "_" + std::to_string(n);
-        const std::string z = "0.0";
+        const std::string z = lit(0.0);
         switch (op.op) {
         case HYK_OP_ADD:
         case HYK_OP_SUB: {
@@ -550,7 +608,7 @@ struct Gen {
             const std::string b0 = cf(B, 0, n), an = cf(A, n, n);
             if (n == 0) {
                 def(u, 0, "(" + an + " / " + b0 + ")");
-                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << b0 << ";\n";
+                if (!pin) o << "    const hyk_real " << inv0(u) << " = " << lit(1.0) << " / " << b0 << ";\n";
                 flops += 2;
                 keep_inv0(u);
                 break;
@@ -581,7 +639,7 @@ struct Gen {
             const std::string an = cf(A, n, n);
             if (n == 0) {
                 def(u, 0, "sqrt(" + an + ")");  // IEEE square root in both arithmetics
-                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / (2.0 * " << vname(u, 0) << ");\n";
+                if (!pin) o << "    const hyk_real " << inv0(u) << " = " << lit(1.0) << " / (" << lit(2.0) << " * " << vname(u, 0) << ");\n";
                 flops += 3;
                 keep_inv0(u);
                 break;
@@ -603,8 +661,8 @@ struct Gen {
             const double alpha = op.b.num;
             const std::string a0 = cf(A, 0, n);
             if (n == 0) {
-                def(u, 0, (pin ? "pow(" : "hyk_dm_pow(") + a0 + ", " + lit(alpha) + ")");
-                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
+                def(u, 0, (pin ? "pow(" : "HYK_DM_POW(") + a0 + ", " + lit(alpha) + ")");
+                if (!pin) o << "    const hyk_real " << inv0(u) << " = " << lit(1.0) << " / " << a0 << ";\n";
                 flops += 21;
                 keep_inv0(u);
                 break;
@@ -613,9 +671,9 @@ struct Gen {
             for (uint32_t j = 0; j < n; ++j) {
                 const std::string anj = cf(A, n - j, n);
                 if (anj.empty()) continue;
-                const double coef = (double)n * alpha - (double)j * (alpha + 1.0);
+                const double coef = powcoef(n, j, alpha);
                 const std::string t = "t" + std::to_string(u) + "_" + std::to_string(n) + "_" + std::to_string(j);
-                o << "    const double " << t << " = " << lit(coef) << " * " << anj << ";\n";
+                o << "    const hyk_real " << t << " = " << lit(coef) << " * " << anj << ";\n";
                 flops += 1;
                 term(s, t, ucoef(u, j, n));
             }
@@ -627,12 +685,12 @@ struct Gen {
             if (pin)
                 def(u, n, "(" + acc + " / (" + lit((double)n) + " * " + a0 + "))");
             else
-                def(u, n, "((" + acc + " * " + lit(1.0 / (double)n) + ") * " + inv0(u) + ")");
+                def(u, n, "((" + acc + " * " + lit(recip((double)n)) + ") * " + inv0(u) + ")");
             break;
         }
         case HYK_OP_EXP: {
             if (n == 0) {
-                def(u, 0, (pin ? "exp(" : "hyk_dm_exp(") + cf(A, 0, n) + ")");
+                def(u, 0, (pin ? "exp(" : "HYK_DM_EXP(") + cf(A, 0, n) + ")");
                 flops += 20;
                 break;
             }
@@ -645,8 +703,8 @@ struct Gen {
         case HYK_OP_LOG: {
             const std::string a0 = cf(A, 0, n), an = cf(A, n, n);
             if (n == 0) {
-                def(u, 0, (pin ? "log(" : "hyk_dm_log(") + a0 + ")");
-                if (!pin) o << "    const double " << inv0(u) << " = 1.0 / " << a0 << ";\n";
+                def(u, 0, (pin ? "log(" : "HYK_DM_LOG(") + a0 + ")");
+                if (!pin) o << "    const hyk_real " << inv0(u) << " = " << lit(1.0) << " / " << a0 << ";\n";
                 flops += 21;
                 keep_inv0(u);
                 break;
@@ -675,11 +733,11 @@ struct Gen {
                 // The pair is evaluated together at its first member.
                 if (u < partner) {
                     const uint32_t su = is_sin ? u : partner, cu = is_sin ? partner : u;
-                    o << "    double " << vname(su, 0) << "_m, " << vname(cu, 0) << "_m;\n";
-                    o << "    " << (pin ? "sincos(" : "hyk_dm_sincos(") << cf(A, 0, n) << ", &" << vname(su, 0) << "_m, &"
+                    o << "    hyk_real " << vname(su, 0) << "_m, " << vname(cu, 0) << "_m;\n";
+                    o << "    " << (pin ? "sincos(" : "HYK_DM_SINCOS(") << cf(A, 0, n) << ", &" << vname(su, 0) << "_m, &"
                       << vname(cu, 0) << "_m);\n";
-                    o << "    const double " << vname(su, 0) << " = " << vname(su, 0) << "_m;\n";
-                    o << "    const double " << vname(cu, 0) << " = " << vname(cu, 0) << "_m;\n";
+                    o << "    const hyk_real " << vname(su, 0) << " = " << vname(su, 0) << "_m;\n";
+                    o << "    const hyk_real " << vname(cu, 0) << " = " << vname(cu, 0) << "_m;\n";
                     flops += 40;
                 }
                 break;
@@ -700,24 +758,24 @@ struct Gen {
 
     void emit_jets() {
         if (!split) {
-            o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
-            for (uint32_t i = 0; i < N; ++i) o << "    const double " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
+            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n";
+            for (uint32_t i = 0; i < N; ++i) o << "    const hyk_real " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
         }
         const uint32_t last = evx ? p : p - 1;  // order p: the event functions' cone only
         for (uint32_t n = 0; n <= last; ++n) {
             if (split) {
                 o << "static __device__ __noinline__ void hyk_jets_o" << n
-                  << "(double *__restrict__ S, const double t0) {\n";
+                  << "(hyk_real *__restrict__ S, const hyk_real t0) {\n";
                 for (uint32_t i = 0; i < N; ++i) {
-                    o << "    const double " << vname(i, n) << " = HYK_SX(" << i << ", " << n << ");\n";
+                    o << "    const hyk_real " << vname(i, n) << " = HYK_SX(" << i << ", " << n << ");\n";
                     // The same product the previous order formed (k_i_0 is never read).
                     if (needka[i] && n >= 1)
-                        o << "    const double " << kname(i, n) << " = " << lit((double)n) << " * " << vname(i, n)
+                        o << "    const hyk_real " << kname(i, n) << " = " << lit((double)n) << " * " << vname(i, n)
                           << ";\n";
                 }
                 if (!pin && n >= 1)
                     for (uint32_t u = N; u < NU; ++u)
-                        if (islot[u] >= 0) o << "    const double " << inv0(u) << " = " << smem((uint32_t)islot[u]) << ";\n";
+                        if (islot[u] >= 0) o << "    const hyk_real " << inv0(u) << " = " << smem((uint32_t)islot[u]) << ";\n";
             }
             o << "    // ---- order " << n << "\n";
             for (uint32_t k = 0; k < d.n_ops; ++k) {
@@ -728,7 +786,7 @@ struct Gen {
             }
             for (size_t k = 0; k < d.ev.size(); ++k) {
                 const std::string f = cf(res(d.ev[k].g), n, n);
-                o << "    " << smem(evslot + (uint32_t)k * (p + 1) + n) << " = " << (f.empty() ? "0.0" : f) << ";\n";
+                o << "    " << smem(evslot + (uint32_t)k * (p + 1) + n) << " = " << (f.empty() ? lit(0.0) : f) << ";\n";
             }
             if (n == p) {
                 if (split) o << "}\n";
@@ -737,10 +795,10 @@ struct Gen {
             for (uint32_t i = 0; i < N; ++i) {
                 const Ref r = res(d.rhs[i]);
                 const std::string f = cf(r, n, n);
-                def(i, n + 1, f.empty() ? "0.0" : divn(f, n + 1));
+                def(i, n + 1, f.empty() ? lit(0.0) : divn(f, n + 1));
                 o << "    HYK_SX(" << i << ", " << (n + 1) << ") = " << vname(i, n + 1) << ";\n";
                 if (needka[i]) {
-                    o << "    const double " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
+                    o << "    const hyk_real " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
                       << vname(i, n + 1) << ";\n";
                     flops += 1;
                     if (kslot[i] >= 0 && n + 1 + ((adj || evx) ? 1u : 2u) <= p)
@@ -753,7 +811,7 @@ struct Gen {
             if (split) o << "}\n";
         }
         if (split) {
-            o << "static __device__ __noinline__ void hyk_jets(double *__restrict__ S, const double t0) {\n";
+            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n";
             for (uint32_t n = 0; n <= last; ++n) o << "    hyk_jets_o" << n << "(S, t0);\n";
         }
         o << "}\n";
@@ -1300,9 +1358,9 @@ struct TeamGen {
     }
 
     void out(uint32_t u, bool n0, const std::string &v) {
-        o << "            const double v = " << v << ";\n";
+        o << "            const hyk_real v = " << v << ";\n";
         o << "            S[D.c" << ((!n0 && g.hist[u]) ? " + n" : "") << "] = v;\n";
-        if (!n0 && g.needka[u]) o << "            S[D.kc + n - 1] = (double)n * v;\n";
+        if (!n0 && g.needka[u]) o << "            S[D.kc + n - 1] = (hyk_real)n * v;\n";
     }
 
     void addsub(const std::string &a, const std::string &b, bool add, uint32_t u, bool n0) {
@@ -1314,7 +1372,7 @@ struct TeamGen {
         else if (!b.empty())
             v = add ? b : "(-" + b + ")";
         else
-            v = "0.0";
+            v = lit(0.0);
         out(u, n0, v);
     }
 
@@ -1323,7 +1381,7 @@ struct TeamGen {
         if (!n0 && g.cst[u]) return;  // time-constant: order 0 only
         const auto &op = d.ops[u - N];
         const Ref A = g.res(op.a), B = g.res(op.b);
-        const std::string fma_ = "__fma_rn";
+        const std::string fma_ = "HYK_FMA";
         o << "        // " << gr.key << "\n";
         o << "#pragma unroll 1\n";
         o << "        for (int q = r; q < " << gr.members.size() << "; q += HYK_TEAM) {\n";
@@ -1337,27 +1395,27 @@ struct TeamGen {
             case HYK_OP_MUL: out(u, true, a + " * " + b); break;
             case HYK_OP_DIV:
                 out(u, true, "(" + a + " / " + b + ")");
-                o << "            S[D.inv] = 1.0 / " << b << ";\n";
+                o << "            S[D.inv] = " << lit(1.0) << " / " << b << ";\n";
                 break;
             case HYK_OP_SQUARE: out(u, true, a + " * " + a); break;
             case HYK_OP_SQRT:
                 out(u, true, "sqrt(" + a + ")");
-                o << "            S[D.inv] = 1.0 / (2.0 * v);\n";
+                o << "            S[D.inv] = " << lit(1.0) << " / (" << lit(2.0) << " * v);\n";
                 break;
             case HYK_OP_POW:
-                out(u, true, "hyk_dm_pow(" + a + ", " + lit(op.b.num) + ")");
-                o << "            S[D.inv] = 1.0 / " << a << ";\n";
+                out(u, true, "HYK_DM_POW(" + a + ", " + lit(op.b.num) + ")");
+                o << "            S[D.inv] = " << lit(1.0) << " / " << a << ";\n";
                 break;
-            case HYK_OP_EXP: out(u, true, "hyk_dm_exp(" + a + ")"); break;
+            case HYK_OP_EXP: out(u, true, "HYK_DM_EXP(" + a + ")"); break;
             case HYK_OP_LOG:
-                out(u, true, "hyk_dm_log(" + a + ")");
-                o << "            S[D.inv] = 1.0 / " << a << ";\n";
+                out(u, true, "HYK_DM_LOG(" + a + ")");
+                o << "            S[D.inv] = " << lit(1.0) << " / " << a << ";\n";
                 break;
             case HYK_OP_SIN:
             case HYK_OP_COS:
                 if (u < (uint32_t)op.aux) {
-                    o << "            double sv, cv;\n";
-                    o << "            hyk_dm_sincos(" << a << ", &sv, &cv);\n";
+                    o << "            hyk_real sv, cv;\n";
+                    o << "            HYK_DM_SINCOS(" << a << ", &sv, &cv);\n";
                     o << "            S[D.c] = " << (op.op == HYK_OP_SIN ? "sv" : "cv") << ";\n";
                     o << "            S[D.prt] = " << (op.op == HYK_OP_SIN ? "cv" : "sv") << ";\n";
                 }
@@ -1373,7 +1431,7 @@ struct TeamGen {
             const std::string a = cur(A, 'a', false), b = cur(B, 'b', false);
             if (isT(A) || isT(B)) {
                 o << "            if (n == 1) {\n";
-                addsub(isT(A) ? "1.0" : a, isT(B) ? "1.0" : b, add, u, false);
+                addsub(isT(A) ? lit(1.0) : a, isT(B) ? lit(1.0) : b, add, u, false);
                 o << "            } else {\n";
                 addsub(a, b, add, u, false);
                 o << "            }\n";
@@ -1384,7 +1442,7 @@ struct TeamGen {
         }
         case HYK_OP_MUL:
             if (isU(A) && isU(B)) {
-                o << "            double acc = " << at(A, 'a', "0") << " * " << at(B, 'b', "n") << ";\n";
+                o << "            hyk_real acc = " << at(A, 'a', "0") << " * " << at(B, 'b', "n") << ";\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 1; j <= n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
                   << at(B, 'b', "n - j") << ", acc);\n";
@@ -1394,35 +1452,35 @@ struct TeamGen {
             } else if (isK(A) && isU(B)) {
                 out(u, false, K(A, 'a') + " * " + cur(B, 'b', false));
             } else if (isU(A) && isT(B)) {
-                o << "            double acc = " << at(A, 'a', "n - 1") << " * 1.0;\n";
+                o << "            hyk_real acc = " << at(A, 'a', "n - 1") << " * " << lit(1.0) << ";\n";
                 o << "            acc = " << fma_ << "(" << at(A, 'a', "n") << ", t0, acc);\n";
                 out(u, false, "acc");
             } else if (isT(A) && isU(B)) {
-                o << "            double acc = t0 * " << at(B, 'b', "n") << ";\n";
-                o << "            acc = " << fma_ << "(1.0, " << at(B, 'b', "n - 1") << ", acc);\n";
+                o << "            hyk_real acc = t0 * " << at(B, 'b', "n") << ";\n";
+                o << "            acc = " << fma_ << "(" << lit(1.0) << ", " << at(B, 'b', "n - 1") << ", acc);\n";
                 out(u, false, "acc");
             } else if (isK(A) && isK(B)) {
-                out(u, false, "0.0");
+                out(u, false, lit(0.0));
             } else if (isK(A) && isT(B)) {
-                out(u, false, "(n == 1 ? " + K(A, 'a') + " * 1.0 : 0.0)");
+                out(u, false, "(n == 1 ? " + K(A, 'a') + " * " + lit(1.0) + " : " + lit(0.0) + ")");
             } else {  // time * constant
-                out(u, false, "(n == 1 ? 1.0 * " + K(B, 'b') + " : 0.0)");
+                out(u, false, "(n == 1 ? " + lit(1.0) + " * " + K(B, 'b') + " : " + lit(0.0) + ")");
             }
             break;
         case HYK_OP_DIV:
             if (isU(B)) {
-                o << "            double acc = " << at(B, 'b', "1") << " * S[D.c + n - 1];\n";
+                o << "            hyk_real acc = " << at(B, 'b', "1") << " * S[D.c + n - 1];\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << at(B, 'b', "j")
                   << ", S[D.c + n - j], acc);\n";
-                const std::string a = isU(A) ? cur(A, 'a', false) : "0.0";
+                const std::string a = isU(A) ? cur(A, 'a', false) : lit(0.0);
                 out(u, false, "((" + a + " - acc) * S[D.inv])");
             } else {
                 out(u, false, "(" + cur(A, 'a', false) + " * S[D.inv])");
             }
             break;
         case HYK_OP_SQUARE:
-            o << "            double acc = " << at(A, 'a', "0") << " * " << at(A, 'a', "n") << ";\n";
+            o << "            hyk_real acc = " << at(A, 'a', "0") << " * " << at(A, 'a', "n") << ";\n";
             o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 1; 2 * j < n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
               << at(A, 'a', "n - j") << ", acc);\n";
@@ -1432,7 +1490,7 @@ struct TeamGen {
             out(u, false, "acc");
             break;
         case HYK_OP_SQRT:
-            o << "            double acc = 0.0;\n";
+            o << "            hyk_real acc = " << lit(0.0) << ";\n";
             o << "            if (n == 2) {\n";
             o << "                acc = S[D.c + 1] * S[D.c + 1];\n";
             o << "            } else if (n > 2) {\n";
@@ -1450,7 +1508,7 @@ struct TeamGen {
             for (; ai < alphas.size(); ++ai)
                 if (std::memcmp(&alphas[ai], &op.b.num, sizeof(double)) == 0) break;
             const std::string pc = "hyk_pc" + std::to_string(ai) + "[n * (HYK_ORDER + 1)";
-            o << "            double acc = (" << pc << "] * " << at(A, 'a', "n") << ") * S[D.c];\n";
+            o << "            hyk_real acc = (" << pc << "] * " << at(A, 'a', "n") << ") * S[D.c];\n";
             o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 1; j < n; ++j) acc = " << fma_ << "(" << pc << " + j] * "
               << at(A, 'a', "n - j") << ", S[D.c + j], acc);\n";
@@ -1459,18 +1517,18 @@ struct TeamGen {
         }
         case HYK_OP_EXP:
             if (isT(A)) {  // d(t)/dt = 1: the single term j = 1
-                o << "            const double acc = 1.0 * S[D.c + n - 1];\n";
+                o << "            const hyk_real acc = " << lit(1.0) << " * S[D.c + n - 1];\n";
                 out(u, false, "(acc * hyk_invn[n])");
                 break;
             }
-            o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.c + n - 1];\n";
+            o << "            hyk_real acc = " << wrap(A, "S[D.ka]") << " * S[D.c + n - 1];\n";
             o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
               << ", S[D.c + n - j], acc);\n";
             out(u, false, "(acc * hyk_invn[n])");
             break;
         case HYK_OP_LOG:
-            o << "            double acc = 0.0;\n";
+            o << "            hyk_real acc = " << lit(0.0) << ";\n";
             o << "            if (n >= 2) {\n";
             o << "                acc = S[D.kc] * " << at(A, 'a', "n - 1") << ";\n";
             o << "#pragma unroll " << ju << "\n";
@@ -1483,9 +1541,9 @@ struct TeamGen {
         case HYK_OP_SIN:
         case HYK_OP_COS:
             if (isT(A)) {
-                o << "            const double acc = 1.0 * S[D.prt + n - 1];\n";
+                o << "            const hyk_real acc = " << lit(1.0) << " * S[D.prt + n - 1];\n";
             } else {
-                o << "            double acc = " << wrap(A, "S[D.ka]") << " * S[D.prt + n - 1];\n";
+                o << "            hyk_real acc = " << wrap(A, "S[D.ka]") << " * S[D.prt + n - 1];\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
                   << ", S[D.prt + n - j], acc);\n";
@@ -1509,23 +1567,23 @@ struct TeamGen {
         } else if (isU(R)) {
             f = cur(R, 'a', false);
         } else if (isT(R)) {
-            f = "(n == 1 ? 1.0 : 0.0)";
+            f = "(n == 1 ? " + lit(1.0) + " : " + lit(0.0) + ")";
         }
         const std::string nn = n0 ? "1" : "n + 1";
         std::string v;
         if (f.empty())
-            v = "0.0";
+            v = lit(0.0);
         else if (isT(R) && !n0)
-            v = "(n == 1 ? (1.0 * hyk_invn[2]) : 0.0)";
+            v = "(n == 1 ? (" + lit(1.0) + " * hyk_invn[2]) : " + lit(0.0) + ")";
         else
             v = "(" + f + " * hyk_invn[" + nn + "])";
-        o << "            const double v = " << v << ";\n";
+        o << "            const hyk_real v = " << v << ";\n";
         o << "            S[D.c + " << nn << "] = v;\n";
         if (g.needka[i]) {
             if (n0)
-                o << "            if (1 < HYK_ORDER) S[D.kc] = 1.0 * v;\n";
+                o << "            if (1 < HYK_ORDER) S[D.kc] = " << lit(1.0) << " * v;\n";
             else
-                o << "            if (n + 1 < HYK_ORDER) S[D.kc + n] = (double)(n + 1) * v;\n";
+                o << "            if (n + 1 < HYK_ORDER) S[D.kc + n] = (hyk_real)(n + 1) * v;\n";
         }
         o << "        }\n";
     }
@@ -1540,30 +1598,30 @@ struct TeamGen {
     }
 
     void emit() {
-        o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, pad;\n    double num;\n};\n";
+        o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, pad;\n    hyk_real num;\n};\n";
         o << "static __device__ const hyk_tdesc hyk_td[" << std::max<size_t>(descs.size(), 1) << "] = {\n";
         for (const auto &D : descs)
             o << "    {" << D.a << ", " << D.b << ", " << D.c << ", " << D.ka << ", " << D.kc << ", " << D.inv << ", "
               << D.prt << ", 0, " << lit(D.num) << "},\n";
-        if (descs.empty()) o << "    {0, 0, 0, 0, 0, 0, 0, 0, 0.0},\n";
+        if (descs.empty()) o << "    {0, 0, 0, 0, 0, 0, 0, 0, " << lit(0.0) << "},\n";
         o << "};\n";
-        o << "static __constant__ double hyk_invn[" << (p + 2) << "] = {0.0";
-        for (uint32_t k = 1; k <= p + 1; ++k) o << ", " << lit(1.0 / (double)k);
+        o << "static __constant__ hyk_real hyk_invn[" << (p + 2) << "] = {" << lit(0.0);
+        for (uint32_t k = 1; k <= p + 1; ++k) o << ", " << lit(recip((double)k));
         o << "};\n";
         for (size_t ai = 0; ai < alphas.size(); ++ai) {
             const double alpha = alphas[ai];
-            o << "static __device__ const double hyk_pc" << ai << "[" << (p + 1) * (p + 1) << "] = {\n";
+            o << "static __device__ const hyk_real hyk_pc" << ai << "[" << (p + 1) * (p + 1) << "] = {\n";
             for (uint32_t n = 0; n <= p; ++n) {
                 o << "   ";
                 for (uint32_t j = 0; j <= p; ++j) {
-                    const double coef = (j < n) ? (double)n * alpha - (double)j * (alpha + 1.0) : 0.0;
+                    const double coef = (j < n) ? powcoef(n, j, alpha) : 0.0;
                     o << " " << lit(coef) << ",";
                 }
                 o << "\n";
             }
             o << "};\n";
         }
-        o << "static __device__ __noinline__ void hyk_tjets(double *__restrict__ S, const double t0, const int r) {\n";
+        o << "static __device__ __noinline__ void hyk_tjets(hyk_real *__restrict__ S, const hyk_real t0, const int r) {\n";
         o << "    __syncwarp();\n";
         o << "    {\n        // ---- order 0\n";
         emit_order(true);
@@ -1604,16 +1662,25 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin) {
     return g.nslot;
 }
 
+struct PrecisionScope {
+    explicit PrecisionScope(bool f32) { g_f32 = f32; }
+    ~PrecisionScope() { g_f32 = false; }
+};
+
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc) {
+              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc, bool f32) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
     }
+    if (f32 && (pin_arith || adjoint || !d.ev.empty())) {
+        err = "single precision supports neither pin arithmetic, the adjoint nor events";
+        return false;
+    }
+    PrecisionScope prec(f32);
     Gen g(d, order, pin_arith, adjoint);
     const double p = (double)order;
-    const double e1 = std::exp(1.0);
-    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+    const double rhofac = rhofac_of(order);
     std::ostringstream h;
     h << "// Generated by libhyk: " << d.n_eq << " equations, " << d.n_ops << " u-operations, order " << order
       << (pin_arith ? ", pin arithmetic" : "") << "\n";
@@ -1621,15 +1688,16 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
       << "\n#define HYK_BLK " << blk << "\n#define HYK_TPB " << blk << "\n#define HYK_GMEM " << (gmem_stride ? 1 : 0)
       << "\n#define HYK_STRIDE " << (gmem_stride ? std::to_string(gmem_stride) + "ULL" : std::to_string(blk))
       << "\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
-      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
-      << lit(1.0 / (p - 1.0)) << "\n";
+      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(recip(p)) << "\n#define HYK_INV_PM1 "
+      << lit(recip(p - 1.0)) << "\n";
+    h << precision_header(pin_arith);
     if (pin_arith) {
         h << "#define HYK_FMA_ACC(a, b, c) ((a) * (b) + (c))\n";
         h << "#define HYK_RHO(mp, mq, num) (1.0 / pow((mq) / (num), HYK_INV_PM1) < 1.0 / pow((mp) / (num), HYK_INV_P) "
              "? 1.0 / pow((mq) / (num), HYK_INV_PM1) : 1.0 / pow((mp) / (num), HYK_INV_P))\n";
     } else {
-        h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
-        h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
+        h << "#define HYK_FMA_ACC(a, b, c) HYK_FMA((a), (b), (c))\n";
+        h << "#define HYK_RHO(mp, mq, num) HYK_DM_RHO((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
     }
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << "#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
@@ -1675,7 +1743,7 @@ bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err)
 }
 
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc) {
+                   std::string &err, bool high_acc, bool f32) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1684,6 +1752,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
         err = "invalid team geometry";
         return false;
     }
+    PrecisionScope prec(f32);
     TeamGen tg(d, order);
     if (!tg.analyse()) {
         err = tg.err;
@@ -1691,8 +1760,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
     }
     tg.g.emit_jets();  // flop count of the same recurrences
     const double p = (double)order;
-    const double e1 = std::exp(1.0);
-    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
+    const double rhofac = rhofac_of(order);
     const uint32_t nt = tg.nslot | 1u;
     std::ostringstream h;
     h << "// Generated by libhyk (team form, " << team << " threads per trajectory): " << d.n_eq << " equations, "
@@ -1700,10 +1768,11 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
       << "\n#define HYK_TPB " << tpb << "\n#define HYK_TEAM " << team << "\n#define HYK_XS " << tg.XS
       << "\n#define HYK_NT " << nt << "\n#define HYK_NSLOT " << tg.nslot << "\n#define HYK_PAR_SLOT " << tg.par_slot
-      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
-      << lit(1.0 / (p - 1.0)) << "\n";
-    h << "#define HYK_FMA_ACC(a, b, c) __fma_rn((a), (b), (c))\n";
-    h << "#define HYK_RHO(mp, mq, num) hyk_dm_rho((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
+      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(recip(p)) << "\n#define HYK_INV_PM1 "
+      << lit(recip(p - 1.0)) << "\n";
+    h << precision_header(false);
+    h << "#define HYK_FMA_ACC(a, b, c) HYK_FMA((a), (b), (c))\n";
+    h << "#define HYK_RHO(mp, mq, num) HYK_DM_RHO((mp), (mq), (num), HYK_INV_P, HYK_INV_PM1)\n";
     h << "#define HYK_NEV 0\n#define HYK_NTEV 0\n#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
     h << kDmath << "\n";
     h << kCommon << "\n";
@@ -1721,7 +1790,8 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
 // Host translation unit of the same generated recurrences (forward jets and,
 // with the adjoint, the reverse sweep) for CPU checks of the generator: one
 // lane, HYK_BLK = 1, the CUDA intrinsics mapped to their host equivalents.
-bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team) {
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team, bool f32) {
+    PrecisionScope ps(f32);
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1737,8 +1807,10 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
         h << "#include <cmath>\n#include <cstdint>\n#define __device__\n#define __constant__\n#define __noinline__\n"
              "#define __forceinline__ inline\n#define __restrict__\n"
              "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
+             "static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }\n"
              "static inline void __syncwarp() {}\n";
         h << kDmath << "\n";
+        h << (f32 ? "typedef float hyk_real;\n" : "typedef double hyk_real;\n") << precision_header(false);
         h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
           << "\n#define HYK_TEAM 1\n#define HYK_XS " << tg.XS << "\n#define HYK_NSLOT " << tg.nslot
           << "\n#define HYK_PAR_SLOT " << tg.par_slot << "\n";
@@ -1746,15 +1818,15 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
         tg.emit();
         h << tg.o.str();
         h << "extern \"C\" int hyk_host_nslot(void) { return HYK_NSLOT; }\n";
-        h << "extern \"C\" void hyk_host_step(double *S, const double *x0, const double *pars, double t0, double h, double *x1) {\n"
+        h << "extern \"C\" void hyk_host_step(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real h, hyk_real *x1) {\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
              "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
              "    hyk_tjets(S, t0, 0);\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) {\n"
-             "        double acc = HYK_SX(i, HYK_ORDER);\n"
-             "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
+             "        hyk_real acc = HYK_SX(i, HYK_ORDER);\n"
+             "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = HYK_FMA(acc, h, HYK_SX(i, n));\n"
              "        x1[i] = acc;\n    }\n}\n";
-        h << "extern \"C\" void hyk_host_tc(double *S, const double *x0, const double *pars, double t0, double *tc) {\n"
+        h << "extern \"C\" void hyk_host_tc(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real *tc) {\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
              "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
              "    hyk_tjets(S, t0, 0);\n"
@@ -1765,33 +1837,33 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
     }
     Gen g(d, order, false, adjoint);
     const double p = (double)order;
-    const double e1 = std::exp(1.0);
-    const double rhofac = 1.0 / (e1 * e1) * std::exp((-7.0 / 10.0) / (p - 1.0));
     std::ostringstream h;
     h << "#include <cmath>\n#include <cstdint>\n#define __device__\n#define __noinline__\n"
          "#define __forceinline__ inline\n#define __restrict__\n"
          "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
+             "static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }\n"
          "static inline void __syncwarp() {}\n";
     h << kDmath << "\n";
+    h << (f32 ? "typedef float hyk_real;\n" : "typedef double hyk_real;\n") << precision_header(false);
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
       << "\n#define HYK_BLK 1\n#define HYK_STRIDE 1\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot
-      << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(1.0 / p) << "\n#define HYK_INV_PM1 "
-      << lit(1.0 / (p - 1.0)) << "\n";
+      << "\n#define HYK_RHOFAC " << lit(rhofac_of(order)) << "\n#define HYK_INV_P " << lit(recip(p)) << "\n#define HYK_INV_PM1 "
+      << lit(recip(p - 1.0)) << "\n";
     h << "#define HYK_SX(i, n) S[((i) * (HYK_ORDER + 1) + (n)) * HYK_STRIDE]\n#define HYK_PAR(k) S[(HYK_PAR_SLOT + (k)) * HYK_STRIDE]\n";
-    h << "static inline double hyk_inf() { return HUGE_VAL; }\n";
+    h << "static inline hyk_real hyk_inf() { return (hyk_real)HUGE_VAL; }\n";
     g.emit_jets();
     if (adjoint) g.emit_bw();
     h << g.o.str();
     h << "extern \"C\" int hyk_host_nslot(void) { return HYK_NSLOT; }\n";
-    h << "extern \"C\" void hyk_host_step(double *S, const double *x0, const double *pars, double t0, double h, double *x1) {\n"
+    h << "extern \"C\" void hyk_host_step(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real h, hyk_real *x1) {\n"
          "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
          "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
          "    hyk_jets(S, t0);\n"
          "    for (int i = 0; i < HYK_NEQ; ++i) {\n"
-         "        double acc = HYK_SX(i, HYK_ORDER);\n"
-         "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = __fma_rn(acc, h, HYK_SX(i, n));\n"
+         "        hyk_real acc = HYK_SX(i, HYK_ORDER);\n"
+         "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = HYK_FMA(acc, h, HYK_SX(i, n));\n"
          "        x1[i] = acc;\n    }\n}\n";
-    h << "extern \"C\" void hyk_host_tc(double *S, const double *x0, const double *pars, double t0, double *tc) {\n"
+    h << "extern \"C\" void hyk_host_tc(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real *tc) {\n"
          "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
          "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
          "    hyk_jets(S, t0);\n"

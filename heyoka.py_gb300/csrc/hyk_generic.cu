@@ -13,16 +13,21 @@
 namespace {
 
 // out[i][l] = sum_n tc[i][n][l] dt[l]^n, Horner with fused multiply-adds (the
-// same operation sequence as the generated kernels' dense output).
-__global__ void dense_eval_kernel(const double *__restrict__ tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes,
-                                  uint64_t ld, const double *__restrict__ dt, double *__restrict__ out) {
+// same operation sequence as the generated kernels' dense output), in double
+// or in float.
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <typename R>
+__global__ void dense_eval_kernel(const R *__restrict__ tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes,
+                                  uint64_t ld, const R *__restrict__ dt, R *__restrict__ out) {
     const uint64_t lane = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (lane >= n_lanes) return;
-    const double t = dt[lane];
+    const R t = dt[lane];
     for (uint32_t i = 0; i < n_eq; ++i) {
-        const double *c = tc + (uint64_t)i * (order + 1) * ld + lane;
-        double acc = c[(uint64_t)order * ld];
-        for (int n = (int)order - 1; n >= 0; --n) acc = __fma_rn(acc, t, c[(uint64_t)n * ld]);
+        const R *c = tc + (uint64_t)i * (order + 1) * ld + lane;
+        R acc = c[(uint64_t)order * ld];
+        for (int n = (int)order - 1; n >= 0; --n) acc = fma_rn(acc, t, c[(uint64_t)n * ld]);
         out[(uint64_t)i * ld + lane] = acc;
     }
 }
@@ -90,7 +95,15 @@ extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t 
                                       const double *dt, double *out, void *stream) {
     const unsigned blk = 128;
     const uint64_t grid = (n_lanes + blk - 1) / blk;
-    dense_eval_kernel<<<(unsigned)grid, blk, 0, (cudaStream_t)stream>>>(tc, n_eq, order, n_lanes, ld, dt, out);
+    dense_eval_kernel<double><<<(unsigned)grid, blk, 0, (cudaStream_t)stream>>>(tc, n_eq, order, n_lanes, ld, dt, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int hyk_generic_dense_eval_f32(const float *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes,
+                                          uint64_t ld, const float *dt, float *out, void *stream) {
+    const unsigned blk = 128;
+    const uint64_t grid = (n_lanes + blk - 1) / blk;
+    dense_eval_kernel<float><<<(unsigned)grid, blk, 0, (cudaStream_t)stream>>>(tc, n_eq, order, n_lanes, ld, dt, out);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 

@@ -37,7 +37,8 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pi
 // gmem_stride != 0: Taylor coefficients in a global-memory buffer with that
 // slot stride (the number of threads of the fixed grid) instead of shared memory.
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint = false, uint64_t gmem_stride = 0, bool high_acc = false);
+              std::string &err, bool adjoint = false, uint64_t gmem_stride = 0, bool high_acc = false,
+              bool f32 = false);
 
 // Team form (several threads per trajectory): slot count and the share of
 // busy threads over the rounds of one order for teams of 1, 2, 4, ..., 32.
@@ -48,10 +49,11 @@ struct TeamInfo {
 // false (with the reason) when an operation has no team-form code.
 bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err);
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc = false);
+                   std::string &err, bool high_acc = false, bool f32 = false);
 
 // Host (CPU) translation unit of the same recurrences, for checks of the
 // generator (team: the team form's recurrences, run by a team of one).
-bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team = false);
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team = false,
+                   bool f32 = false);
 
 }  // namespace hyk

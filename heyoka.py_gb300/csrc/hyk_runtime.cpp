@@ -31,6 +31,8 @@
 // Generic kernels compiled by nvcc into this library (hyk_generic.cu).
 extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
                                       const double *dt, double *out, void *stream);
+extern "C" int hyk_generic_dense_eval_f32(const float *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes,
+                                          uint64_t ld, const float *dt, float *out, void *stream);
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
 extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
@@ -228,6 +230,7 @@ struct hyk_module {
     CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
     int adj_ctas_per_sm = 0;
     uint32_t team = 0;           // threads per trajectory (team form); 0 = lane form
+    bool f32 = false;            // single precision
     bool gmem = false;           // Taylor coefficients in a global buffer (large systems)
     uint64_t gmem_threads = 0;   // threads of the fixed grid in that mode
     CUdeviceptr jets = 0;        // the module's coefficient buffer (gmem mode)
@@ -253,14 +256,19 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (cfg) m->cfg = *cfg;
     m->order = order;
     m->device = device;
+    const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
+    const bool pin = (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0;
+    const bool f32 = (m->cfg.flags & HYK_CFG_FLOAT32) != 0;
+    if (f32 && (pin || adjoint || !m->d.ev.empty()))
+        return fail(HYK_ERR_UNSUPPORTED, "single precision supports neither pin arithmetic, the adjoint nor events");
+    m->f32 = f32;
     int rc = get_device(device, m->dv);
     if (rc) return rc;
     const Device &dv = *m->dv;
 
-    const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
-    const bool pin = (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0;
+    const size_t real_bytes = f32 ? sizeof(float) : sizeof(double);
     uint32_t nslot = hyk::count_slots(m->d, order, adjoint, pin);
-    size_t lane_bytes = (size_t)nslot * sizeof(double);
+    size_t lane_bytes = (size_t)nslot * real_bytes;
     uint32_t blk = m->cfg.block_lanes;
 
     // Form.  The lane form (one thread per trajectory) needs 32 lanes of
@@ -291,7 +299,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
             best = std::max(best, std::min(1.0, w / 4.0));
         }
         for (uint32_t T = 2, l = 1; T <= 32; T *= 2, ++l) {
-            const size_t cta = (size_t)(32 / T) * ti.n_slot * sizeof(double);
+            const size_t cta = (size_t)(32 / T) * ti.n_slot * real_bytes;
             if (cta > (size_t)dv.smem_optin) continue;
             const double w = (double)((size_t)dv.smem_per_sm / (cta + 1024));
             const double score = ti.util[l] * std::min(1.0, w / 4.0) * 0.85;
@@ -304,7 +312,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (m->team) {
         if (blk == 0) blk = 32;
         nslot = ti.n_slot;
-        lane_bytes = (size_t)nslot * sizeof(double);
+        lane_bytes = (size_t)nslot * real_bytes;
     }
     // Lane form of a system whose coefficients do not fit 32 lanes of shared
     // memory: a global buffer owned by the module, one slot stride for the
@@ -360,10 +368,10 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     hyk::GenOut g;
     const bool high_acc = (m->cfg.flags & HYK_CFG_HIGH_ACCURACY) != 0;
     if (m->team) {
-        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc))
+        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32))
             return fail(HYK_ERR_INVALID, err);
     } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
-                              high_acc)) {
+                              high_acc, f32)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (g.n_slot != nslot) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
@@ -462,7 +470,7 @@ int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info) {
     info->order = m->order;
     info->n_u = m->d.n_u();
     info->block_lanes = m->blk;
-    info->smem_per_lane = m->gmem ? 0u : m->nslot * 8;
+    info->smem_per_lane = m->gmem ? 0u : m->nslot * (m->f32 ? 4u : 8u);
     info->team_size = m->team ? m->team : 1;
     info->regs_per_thread = (uint32_t)m->regs;
     info->ctas_per_sm = (uint32_t)m->ctas_per_sm;
@@ -717,6 +725,15 @@ int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_l
     return 0;
 }
 
+int hyk_dense_eval_f32(const float *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld, const float *dt,
+                       float *out, void *stream) {
+    if (n_lanes == 0) return 0;
+    if (!tc || !dt || !out || ld < n_lanes || n_eq == 0) return fail(HYK_ERR_INVALID, "invalid dense-output arguments");
+    const int rc = hyk_generic_dense_eval_f32(tc, n_eq, order, n_lanes, ld, dt, out, stream);
+    if (rc) return fail(HYK_ERR_CUDA, "dense-output kernel launch failed");
+    return 0;
+}
+
 int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
                       size_t log_len, uint32_t *n_slot, double *flops) {
     hyk::Dec d;
@@ -730,28 +747,29 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     // lanes do not fit the opt-in shared memory of an SM (227 KB), with the
     // slot stride of a 152-SM grid.
     const uint32_t team = cfg ? cfg->team_size : 0;
+    const bool f32 = cfg && (cfg->flags & HYK_CFG_FLOAT32);
     if (team > 1 && verbose == 3) {  // host translation unit of the team form
         std::string hs;
-        if (!hyk::generate_host(d, order, false, hs, err, true)) return fail(HYK_ERR_UNSUPPORTED, err);
+        if (!hyk::generate_host(d, order, false, hs, err, true, f32)) return fail(HYK_ERR_UNSUPPORTED, err);
         if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
         return 0;
     }
     const uint32_t slots = hyk::count_slots(d, order, adjoint, pin);
-    const uint64_t gstride = (uint64_t)slots * 8 * 32 > 227u * 1024 ? 152ull * blk : 0;
+    const uint64_t gstride = (uint64_t)slots * (f32 ? 4 : 8) * 32 > 227u * 1024 ? 152ull * blk : 0;
     hyk::GenOut g;
     const bool high_acc = cfg && (cfg->flags & HYK_CFG_HIGH_ACCURACY);
     if (team > 1) {
         if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : 32, sizeof(KParams), g, err,
-                                high_acc))
+                                high_acc, f32))
             return fail(HYK_ERR_UNSUPPORTED, err);
-    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc)) {
+    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (n_slot) *n_slot = g.n_slot;
     if (flops) *flops = g.flops;
     if (verbose == 3) {  // host translation unit (CPU checks of the generator)
         std::string hs;
-        if (!hyk::generate_host(d, order, adjoint, hs, err)) return fail(HYK_ERR_INVALID, err);
+        if (!hyk::generate_host(d, order, adjoint, hs, err, false, f32)) return fail(HYK_ERR_INVALID, err);
         if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
         return 0;
     }

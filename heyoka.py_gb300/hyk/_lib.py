@@ -29,10 +29,17 @@ c_u32, c_u64, c_i64, c_int, c_d, c_vp = (
 
 HYK_MODE_PLAIN = 0
 HYK_MODE_PERSISTENT = 1
+HYK_ERR_INVALID = -1
+HYK_ERR_CUDA = -2
+HYK_ERR_NVRTC = -3
+HYK_ERR_UNSUPPORTED = -4
+HYK_ERR_TIMEOUT = -5
+
 HYK_CFG_PIN_ARITH = 1
 HYK_CFG_ADJOINT = 2
 HYK_CFG_HIGH_ACCURACY = 4
 HYK_CFG_GLOBAL_JETS = 8
+HYK_CFG_FLOAT32 = 16
 
 LANE_DONE, LANE_STOPPED, LANE_CAPACITY, LANE_EVENT = 1, 2, 4, 8
 OC_EV_OVERFLOW = -4294967310
@@ -134,6 +141,7 @@ SIGNATURES = {
     "hyk_propagate_noalloc": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_u32, P(c_u64), c_vp]),
     "hyk_adjoint": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_size_t, c_vp]),
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
+    "hyk_dense_eval_f32": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),
     "hyk_codegen_check": (

@@ -125,6 +125,9 @@ typedef struct hyk_config {
 #define HYK_CFG_PIN_ARITH 1u /* oracle "pin" arithmetic: no FMA, divide by n (slower; for cross-checks) */
 #define HYK_CFG_ADJOINT 2u   /* also generate the adjoint (reverse-mode) kernel for hyk_adjoint() */
 #define HYK_CFG_HIGH_ACCURACY 4u /* state update by compensated summation (the reference's high_accuracy) */
+#define HYK_CFG_FLOAT32 16u      /* single precision: every real array of the lanes and of hyk_prop_t is float
+                                    (heyoka's float32 batch integrator); not with pin arithmetic, the
+                                    adjoint or events */
 #define HYK_CFG_GLOBAL_JETS 8u   /* one thread per trajectory with the Taylor coefficients in global memory
                                     (chosen automatically for systems that leave fewer than two warps
                                     per SM in shared memory) */
@@ -157,7 +160,10 @@ int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info);
 /* The generated CUDA source of the module (valid until hyk_module_destroy). */
 const char *hyk_module_source(const hyk_module *m);
 
-/* Lane data, device pointers, row stride `ld` (>= n_lanes) for 2-D arrays. */
+/* Lane data, device pointers, row stride `ld` (>= n_lanes) for 2-D arrays.
+ * A module created with HYK_CFG_FLOAT32 (heyoka's taylor_adaptive_batch<float>)
+ * reads and writes float arrays through every real pointer of hyk_lanes_t,
+ * hyk_step and hyk_prop_t: the caller passes float buffers cast to double *. */
 typedef struct hyk_lanes {
     uint64_t n_lanes;
     uint64_t ld;
@@ -321,6 +327,10 @@ int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, con
  *  heyoka/taylor_expose_c_output.cpp:272-408). */
 int hyk_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
                    const double *dt, double *out, void *stream);
+
+/* Dense output of a single-precision module (float arrays, the same layout). */
+int hyk_dense_eval_f32(const float *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
+                       const float *dt, float *out, void *stream);
 
 /* The deterministic elementary functions the kernels use, evaluated on the
  * device for validation: fn 0 exp, 1 log, 2 sin, 3 cos, 4 pow(x[i], a[i]),

@@ -103,6 +103,19 @@ template <> struct M<double> {
     static double inf() { return std::numeric_limits<double>::infinity(); }
     static double nan() { return std::numeric_limits<double>::quiet_NaN(); }
 };
+template <> struct M<float> {
+    static float sin(float x) { return std::sin(x); }
+    static float cos(float x) { return std::cos(x); }
+    static float exp(float x) { return std::exp(x); }
+    static float log(float x) { return std::log(x); }
+    static float sqrt(float x) { return std::sqrt(x); }
+    static float pow(float x, float y) { return std::pow(x, y); }
+    static float fma(float a, float b, float c) { return std::fma(a, b, c); }
+    static float abs(float x) { return std::fabs(x); }
+    static bool isfinite(float x) { return std::isfinite(x); }
+    static float inf() { return std::numeric_limits<float>::infinity(); }
+    static float nan() { return std::numeric_limits<float>::quiet_NaN(); }
+};
 template <> struct M<qreal> {
 #if HYKO_QUADMATH
     static qreal sin(qreal x) { return sinq(x); }
@@ -157,6 +170,27 @@ template <> struct F<double> {
     static bool rho(double mp, double mq, double num, double ip, double iq, int m, double &out) {
         if (!m) return false;
         out = hyk_dm_rho(mp, mq, num, ip, iq);
+        return true;
+    }
+};
+
+// Single precision (heyoka's float integrator): "gpu" arithmetic only, with
+// the float functions of the kernels.
+template <> struct F<float> {
+    static float exp(float x, int m) { return m ? hyk_dmf_exp(x) : std::exp(x); }
+    static float log(float x, int m) { return m ? hyk_dmf_log(x) : std::log(x); }
+    static float pow(float x, float a, int m) { return m ? hyk_dmf_pow(x, a) : std::pow(x, a); }
+    static void sincos(float x, float &s, float &c, int m) {
+        if (m) {
+            hyk_dmf_sincos(x, &s, &c);
+        } else {
+            s = std::sin(x);
+            c = std::cos(x);
+        }
+    }
+    static bool rho(float mp, float mq, float num, float ip, float iq, int m, float &out) {
+        if (!m) return false;
+        out = hyk_dmf_rho(mp, mq, num, ip, iq);
         return true;
     }
 };
@@ -1076,7 +1110,8 @@ int hyko_ev_find(const double *g, uint32_t p, double h, double s_lo, double s_hi
     return n;
 }
 
-// One step of a batch of B lanes (host arrays, [var][lane]).  prec: 0 double, 1 binary128.
+// One step of a batch of B lanes (host arrays, [var][lane]).  prec: 0 double,
+// 1 binary128, 2 float (the values are converted from and to double exactly).
 int hyko_step(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, uint32_t B, double *state,
               const double *pars, double *t_hi, double *t_lo, const double *max_dt, int backward,
               int64_t *outcome, double *h, double *tc) {
@@ -1087,6 +1122,7 @@ int hyko_step(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, uint32
         return HYK_ERR_INVALID;
     }
     if (prec == 0) return step_one<double>(d, order, mode, B, state, pars, t_hi, t_lo, max_dt, backward, outcome, h, tc);
+    if (prec == 2) return step_one<float>(d, order, mode, B, state, pars, t_hi, t_lo, max_dt, backward, outcome, h, tc);
     return step_one<qreal>(d, order, mode, B, state, pars, t_hi, t_lo, max_dt, backward, outcome, h, tc);
 }
 
@@ -1108,7 +1144,9 @@ int hyko_propagate(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, u
     std::vector<double> vt, vh, vl;
     PropIO io{state,  pars,     t_hi,   t_lo,  tf_hi, tf_lo, max_steps, max_dt, grid,    n_grid,  grid_out,
               c_output, &vt, &vh, &vl, outcome, min_h, max_h, n_steps, last_h, last_tc, n_iter};
-    const int r = prec == 0 ? propagate<double>(d, order, mode, B, io) : propagate<qreal>(d, order, mode, B, io);
+    const int r = prec == 0   ? propagate<double>(d, order, mode, B, io)
+                  : prec == 2 ? propagate<float>(d, order, mode, B, io)
+                              : propagate<qreal>(d, order, mode, B, io);
     if (c_output) {
         auto dup = [](const std::vector<double> &v) {
             double *p = (double *)std::malloc(sizeof(double) * std::max<size_t>(v.size(), 1));

@@ -5,7 +5,7 @@ this module; the product path (the ``hyk`` package and libhyk.so) never does.
 See hyk_oracle.cpp for the restated algorithm and its reference citations.
 
 All arrays are float64 NumPy arrays in the reference's [var][lane] layout.
-``prec``: 0 = double, 1 = binary128.  ``mode``: 0 = "pin" arithmetic (the
+``prec``: 0 = double, 1 = binary128, 2 = float (gpu arithmetic).  ``mode``: 0 = "pin" arithmetic (the
 arithmetic pinned to the reference's notebook outputs), 1 = "gpu" arithmetic
 (fused multiply-adds and reciprocal multiplications, operation for operation
 what the CUDA kernels do).
