@@ -44,8 +44,15 @@
 #define HYK_DM_FN static inline
 #define HYK_DM_FMA(a, b, c) std::fma((a), (b), (c))
 #define HYK_DM_BITS(x) hyk_host_bits_(x)
+#define HYK_DM_FMAF(a, b, c) std::fma((a), (b), (c))
+#define HYK_DM_FBITS(x) hyk_host_fbits_(x)
 static inline unsigned long long hyk_host_bits_(double x) {
     unsigned long long u;
+    std::memcpy(&u, &x, sizeof u);
+    return u;
+}
+static inline unsigned hyk_host_fbits_(float x) {
+    unsigned u;
     std::memcpy(&u, &x, sizeof u);
     return u;
 }
@@ -53,6 +60,8 @@ static inline unsigned long long hyk_host_bits_(double x) {
 #undef HYK_DM_FN
 #undef HYK_DM_FMA
 #undef HYK_DM_BITS
+#undef HYK_DM_FMAF
+#undef HYK_DM_FBITS
 
 namespace hyk {
 
@@ -836,10 +845,10 @@ struct Gen {
         arr("int", "hyk_ev_term", [&](size_t k) { return std::to_string(d.ev[k].terminal); });
         arr("int", "hyk_ev_dir", [&](size_t k) { return std::to_string(d.ev[k].direction); });
         arr("int", "hyk_ev_idx", [&](size_t k) { return std::to_string(idx[k]); });
-        arr("double", "hyk_ev_cool", [&](size_t k) { return lit(d.ev[k].cooldown); });
+        arr("hyk_real", "hyk_ev_cool", [&](size_t k) { return lit(d.ev[k].cooldown); });
         std::vector<double> bt((size_t)(p + 1) * (p + 1));
         hyk_ev_btab((int)p, bt.data());
-        h << "static __constant__ double hyk_ev_bt[" << bt.size() << "] = {";
+        h << "static __constant__ hyk_real hyk_ev_bt[" << bt.size() << "] = {";
         for (size_t k = 0; k < bt.size(); ++k) h << (k ? ", " : "") << lit(bt[k]);
         h << "};\n";
     }
@@ -1673,8 +1682,8 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
         err = "the Taylor order must be at least 2";
         return false;
     }
-    if (f32 && (pin_arith || adjoint || !d.ev.empty())) {
-        err = "single precision supports neither pin arithmetic, the adjoint nor events";
+    if (f32 && (pin_arith || adjoint)) {
+        err = "single precision supports neither pin arithmetic nor the adjoint";
         return false;
     }
     PrecisionScope prec(f32);
@@ -1702,9 +1711,9 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << "#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
     h << kDmath << "\n";
+    h << kCommon << "\n";
     g.emit_events(h);
     if (!d.ev.empty()) h << kEvents << "\n";
-    h << kCommon << "\n";
     h << kTemplate << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
     g.emit_jets();

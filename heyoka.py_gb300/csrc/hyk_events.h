@@ -21,15 +21,23 @@
  *    ratios C(k,i)/C(p,i)) have V sign changes; V = 0 means no root, V = 1
  *    one root, V >= 2 a split into the two halves (up to HYK_EV_DEPTH levels);
  *  - an interval with V = 1 (or at the deepest level) whose end values have
- *    opposite signs is refined by bisection to adjacent doubles; a zero value
+ *    opposite signs is refined by bisection to adjacent numbers; a zero value
  *    at the right end is a root there.
  * Every operation is an IEEE add, multiply or fused multiply-add in a fixed
- * order.
+ * order, in the integrator's precision R (double, or float for the float32
+ * integrator, whose dyadic walk stops at depth 22 so that the interval ends
+ * i 2^-d stay exact).
  */
 #ifndef HYK_EVENTS_H
 #define HYK_EVENTS_H
 
 #define HYK_EV_DEPTH 40
+
+/* Automatic cooldown of a terminal event that triggered at time t:
+ * REL * max(1, |t|), about 4500 units in the last place of t in either
+ * precision (a root found again this close after the trigger is the same root). */
+#define HYK_EV_COOL_REL_D 1e-12
+#define HYK_EV_COOL_REL_F 5e-4f
 
 #if !defined(__CUDACC_RTC__)
 /* C(k, i) / C(p, i) for 0 <= i <= k <= p, row-major (p + 1) x (p + 1);
@@ -48,39 +56,43 @@ static inline void hyk_ev_btab(int p, double *bt) {
 }
 #endif
 
-HYK_DM_FN double hyk_ev_q(const double *a, int p, double s) {
-    double r = a[p];
-    for (int n = p - 1; n >= 0; --n) r = HYK_DM_FMA(r, s, a[n]);
-    return r;
-}
-
-HYK_DM_FN double hyk_ev_dq(const double *a, int p, double s) {
-    double r = (double)p * a[p];
-    for (int n = p - 1; n >= 1; --n) r = HYK_DM_FMA(r, s, (double)n * a[n]);
-    return r;
-}
-
+HYK_DM_FN double hyk_ev_fma(double a, double b, double c) { return HYK_DM_FMA(a, b, c); }
+HYK_DM_FN float hyk_ev_fma(float a, float b, float c) { return HYK_DM_FMAF(a, b, c); }
 HYK_DM_FN int hyk_ev_finite(double x) { return (HYK_DM_BITS(x) & 0x7ff0000000000000ULL) != 0x7ff0000000000000ULL; }
+HYK_DM_FN int hyk_ev_finite(float x) { return (HYK_DM_FBITS(x) & 0x7f800000u) != 0x7f800000u; }
+
+template <typename R> HYK_DM_FN R hyk_ev_q(const R *a, int p, R s) {
+    R r = a[p];
+    for (int n = p - 1; n >= 0; --n) r = hyk_ev_fma(r, s, a[n]);
+    return r;
+}
+
+template <typename R> HYK_DM_FN R hyk_ev_dq(const R *a, int p, R s) {
+    R r = (R)p * a[p];
+    for (int n = p - 1; n >= 1; --n) r = hyk_ev_fma(r, s, (R)n * a[n]);
+    return r;
+}
 
 /* Sign changes of the Bernstein coefficients of q on [lo, lo + w]
- * (c and b are work arrays of p + 1 doubles). */
-HYK_DM_FN int hyk_ev_changes(const double *a, int p, double lo, double w, const double *bt, double *c, double *b) {
+ * (c and b are work arrays of p + 1 numbers). */
+template <typename R>
+HYK_DM_FN int hyk_ev_changes(const R *a, int p, R lo, R w, const R *bt, R *c, R *b) {
     for (int k = 0; k <= p; ++k) c[k] = a[k];
     for (int k = 0; k < p; ++k)
-        for (int j = p - 1; j >= k; --j) c[j] = HYK_DM_FMA(c[j + 1], lo, c[j]);
-    double wk = 1.0;
+        for (int j = p - 1; j >= k; --j) c[j] = hyk_ev_fma(c[j + 1], lo, c[j]);
+    R wk = 1;
     for (int k = 0; k <= p; ++k) {
         c[k] = c[k] * wk;
         wk = wk * w;
     }
     for (int k = 0; k <= p; ++k) {
-        double acc = c[0] * bt[k * (p + 1)];
-        for (int i = 1; i <= k; ++i) acc = HYK_DM_FMA(bt[k * (p + 1) + i], c[i], acc);
+        R acc = c[0] * bt[k * (p + 1)];
+        for (int i = 1; i <= k; ++i) acc = hyk_ev_fma(bt[k * (p + 1) + i], c[i], acc);
         b[k] = acc;
     }
     int v = 0, last = 0;
     for (int k = 0; k <= p; ++k) {
-        const int sg = b[k] > 0.0 ? 1 : (b[k] < 0.0 ? -1 : 0);
+        const int sg = b[k] > 0 ? 1 : (b[k] < 0 ? -1 : 0);
         if (sg == 0) continue;
         if (last != 0 && sg != last) ++v;
         last = sg;
@@ -90,65 +102,67 @@ HYK_DM_FN int hyk_ev_changes(const double *a, int p, double lo, double w, const 
 
 /* Roots of q in (s_lo, s_hi] with direction dir (0: any, +1: dg/dt > 0,
  * -1: dg/dt < 0), in increasing order.  g: coefficients g_0..g_p at stride
- * gs; work: 3 (p + 1) doubles.  Stores at most maxr roots (rs[k * rstride]:
+ * gs; work: 3 (p + 1) numbers.  Stores at most maxr roots (rs[k * rstride]:
  * s, rsg[k * rstride]: direction) and returns how many roots it found, which
  * exceeds maxr when some were not stored; with first_only the walk stops at
  * the first root. */
-HYK_DM_FN int hyk_ev_find(const double *g, long gs, int p, double h, const double *bt, double s_lo, double s_hi,
-                          int dir, int first_only, double *rs, int *rsg, long rstride, int maxr, double *work) {
-    double *a = work, *c = work + (p + 1), *b = work + 2 * (p + 1);
-    double hp = 1.0;
+template <typename R>
+HYK_DM_FN int hyk_ev_find(const R *g, long gs, int p, R h, const R *bt, R s_lo, R s_hi, int dir, int first_only, R *rs,
+                          int *rsg, long rstride, int maxr, R *work) {
+    R *a = work, *c = work + (p + 1), *b = work + 2 * (p + 1);
+    const int depth = sizeof(R) == sizeof(float) ? 22 : HYK_EV_DEPTH;
+    R hp = 1;
     for (int n = 0; n <= p; ++n) {
         a[n] = g[(long)n * gs] * hp;
         hp = hp * h;
     }
-    double sum = 0.0;
-    for (int n = 1; n <= p; ++n) sum = sum + (a[n] < 0.0 ? -a[n] : a[n]);
-    const double a0 = a[0] < 0.0 ? -a[0] : a[0];
+    R sum = 0;
+    for (int n = 1; n <= p; ++n) sum = sum + (a[n] < 0 ? -a[n] : a[n]);
+    const R a0 = a[0] < 0 ? -a[0] : a[0];
     if (!hyk_ev_finite(sum) || !hyk_ev_finite(a0)) return 0;
     if (a0 > sum) return 0;
-    const int hs = h > 0.0 ? 1 : (h < 0.0 ? -1 : 0);
+    const int hs = h > 0 ? 1 : (h < 0 ? -1 : 0);
     int nr = 0, d = 0;
     long long i = 0;
-    double scale = 1.0; /* 2^-d */
+    R scale = 1; /* 2^-d */
     for (;;) {
-        const double lo = (double)i * scale, hi = (double)(i + 1) * scale;
+        const R lo = (R)i * scale, hi = (R)(i + 1) * scale;
         if (lo >= s_hi) break; /* intervals come in increasing order */
         if (hi > s_lo) {
             const int v = hyk_ev_changes(a, p, lo, scale, bt, c, b);
-            if (v >= 2 && d < HYK_EV_DEPTH) {
+            if (v >= 2 && d < depth) {
                 ++d;
                 i = 2 * i;
-                scale = scale * 0.5;
+                scale = scale * (R)0.5;
                 continue;
             }
             if (v >= 1) {
-                double l = lo, r = hi, root = -1.0;
-                double fl = hyk_ev_q(a, p, l), fr = hyk_ev_q(a, p, r);
-                if (fr == 0.0) {
+                R l = lo, r = hi, root = -1;
+                R fl = hyk_ev_q(a, p, l), fr = hyk_ev_q(a, p, r);
+                if (fr == 0) {
                     root = r;
-                } else if (fl != 0.0 && ((fl < 0.0) != (fr < 0.0))) {
+                } else if (fl != 0 && ((fl < 0) != (fr < 0))) {
                     for (int it = 0; it < 200; ++it) {
-                        const double m = l + 0.5 * (r - l);
+                        const R m = l + (R)0.5 * (r - l);
                         if (!(m > l && m < r)) break;
-                        const double fm = hyk_ev_q(a, p, m);
-                        if (fm == 0.0) {
+                        const R fm = hyk_ev_q(a, p, m);
+                        if (fm == 0) {
                             l = m;
                             r = m;
                             break;
                         }
-                        if ((fm < 0.0) == (fl < 0.0)) {
+                        if ((fm < 0) == (fl < 0)) {
                             l = m;
                             fl = fm;
                         } else {
                             r = m;
                         }
                     }
-                    root = l + 0.5 * (r - l);
+                    root = l + (R)0.5 * (r - l);
                 }
                 if (root > s_lo && root <= s_hi) {
-                    const double dq = hyk_ev_dq(a, p, root);
-                    const int sg = (dq > 0.0 ? 1 : (dq < 0.0 ? -1 : 0)) * hs;
+                    const R dq = hyk_ev_dq(a, p, root);
+                    const int sg = (dq > 0 ? 1 : (dq < 0 ? -1 : 0)) * hs;
                     if (dir == 0 || sg == dir) {
                         if (nr < maxr) {
                             rs[(long)nr * rstride] = root;
@@ -163,7 +177,7 @@ HYK_DM_FN int hyk_ev_find(const double *g, long gs, int p, double h, const doubl
         while (d > 0 && (i & 1)) {
             i >>= 1;
             --d;
-            scale = scale * 2.0;
+            scale = scale * (R)2;
         }
         if (d == 0) break;
         ++i;

@@ -259,8 +259,8 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const bool adjoint = (m->cfg.flags & HYK_CFG_ADJOINT) != 0;
     const bool pin = (m->cfg.flags & HYK_CFG_PIN_ARITH) != 0;
     const bool f32 = (m->cfg.flags & HYK_CFG_FLOAT32) != 0;
-    if (f32 && (pin || adjoint || !m->d.ev.empty()))
-        return fail(HYK_ERR_UNSUPPORTED, "single precision supports neither pin arithmetic, the adjoint nor events");
+    if (f32 && (pin || adjoint))
+        return fail(HYK_ERR_UNSUPPORTED, "single precision supports neither pin arithmetic nor the adjoint");
     m->f32 = f32;
     int rc = get_device(device, m->dv);
     if (rc) return rc;

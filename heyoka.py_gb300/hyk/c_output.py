@@ -52,7 +52,7 @@ class continuous_output_batch:
         if n:
             # Search keys: start times of the steps, sign-normalised per lane
             # so that they are non-decreasing for backward propagations too.
-            self._sgn = torch.where(self._thi[-1] < self._thi[0], -1.0, 1.0).to(torch.float64)
+            self._sgn = torch.where(self._thi[-1] < self._thi[0], -1.0, 1.0).to(tcs.dtype)
             self._keys = (self._thi[:n] * self._sgn).t().contiguous()  # (B, n)
 
     @property
@@ -95,11 +95,12 @@ class continuous_output_batch:
         lanes = torch.arange(self._B, device=self._dev)
         tc = self._tcs[idx, :, :, lanes].permute(1, 2, 0).contiguous()  # (dim, order+1, B)
         dt = _dsub_hi(t, self._thi[idx, lanes], self._tlo[idx, lanes]).contiguous()
-        out = torch.empty((self._dim, self._B), dtype=torch.float64, device=self._dev)
+        out = torch.empty((self._dim, self._B), dtype=self._tcs.dtype, device=self._dev)
         L = _lib.load()
+        fn = L.hyk_dense_eval_f32 if self._tcs.dtype == torch.float32 else L.hyk_dense_eval
         with torch.cuda.device(self._dev):
             _lib.check(
-                L.hyk_dense_eval(
+                fn(
                     tc.data_ptr(), self._dim, self._order, self._B, self._B, dt.data_ptr(), out.data_ptr(),
                     stream_handle(self._dev.index),
                 ),
@@ -110,16 +111,18 @@ class continuous_output_batch:
     def __call__(self, tm):
         if self.n_steps == 0:
             raise ValueError("Cannot use a default-constructed continuous_output_batch object")
+        dt = self._tcs.dtype
+        ndt = np.float32 if dt == torch.float32 else np.float64
         if isinstance(tm, torch.Tensor):
-            t = tm.to(device=self._dev, dtype=torch.float64)
+            t = tm.to(device=self._dev, dtype=dt)
         elif np.ndim(tm) == 0:
             # a scalar time applies to every lane (heyoka/taylor_expose_c_output.cpp:272-296)
-            t = torch.full((self._B,), float(tm), dtype=torch.float64, device=self._dev)
+            t = torch.full((self._B,), float(ndt(tm)), dtype=dt, device=self._dev)
         else:
             a = np.asarray(tm)
-            if a.dtype != np.float64:
-                a = a.astype(np.float64, casting="safe")
-            t = torch.tensor(a, dtype=torch.float64, device=self._dev)
+            if a.dtype != ndt:
+                a = a.astype(ndt, casting="safe" if ndt == np.float64 else "same_kind")
+            t = torch.tensor(a, dtype=dt, device=self._dev)
         if t.dim() not in (1, 2):
             raise ValueError(
                 "Invalid time array passed to a continuous_output_batch object: the number of dimensions "
@@ -141,7 +144,7 @@ class continuous_output_batch:
         rows = [self._eval_row(t[i].contiguous()) for i in range(t.shape[0])]
         if rows:
             self._out = rows[-1]
-        res = torch.stack(rows) if rows else torch.empty((0, self._dim, self._B), dtype=torch.float64)
+        res = torch.stack(rows) if rows else torch.empty((0, self._dim, self._B), dtype=dt)
         a = res.cpu().numpy()
         a.flags.writeable = False
         return a

@@ -174,7 +174,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     md = big._check_prop_args(md, None)
     ms = int(kwargs.get("max_steps", 0))
     if tp == "grid":
-        g = torch.tensor(np.repeat(arg.astype(np.float64), n_iter * B).reshape(-1, n_iter * B), device=dev)
+        g = torch.tensor(np.repeat(arg.astype(ta._np_dt), n_iter * B).reshape(-1, n_iter * B), device=dev)
         if not bool((g[0] == big._thi).all()):
             raise ValueError(
                 "When invoking propagate_grid(), the first element of the time grid "
@@ -182,7 +182,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             )
         res = big._run(g[-1].contiguous(), None, ms, md, grid=g, group=B)
     else:
-        tt = torch.full((n_iter * B,), float(arg), dtype=torch.float64, device=dev)
+        tt = torch.full((n_iter * B,), float(ta._np_dt(arg)), dtype=ta._tdt, device=dev)
         if tp == "until":
             tf_hi, tf_lo = tt, None
         else:

@@ -43,8 +43,9 @@ class event_direction(enum.IntEnum):
 
 
 def _check_fp(fp_type):
-    if fp_type not in (float, np.float64):
+    if fp_type not in (float, np.float64, np.float32):
         raise TypeError('The floating-point type "{}" is not recognized/supported'.format(fp_type))
+    return "float" if fp_type is np.float32 else "double"
 
 
 def _check_cb(cb):
@@ -72,7 +73,7 @@ def _load_cb(blob):
 
 class _EventBase:
     def __init__(self, ex, direction, fp_type):
-        _check_fp(fp_type)
+        self._ctype = _check_fp(fp_type)
         self._ex = _e._ex(ex)
         self._dir = event_direction(direction)
 
@@ -123,8 +124,8 @@ class nt_event_batch(_EventBase):
 
     def __repr__(self):
         return (
-            "C++ datatype: double\nEvent type: non-terminal\nEvent equation: {}\nEvent direction: "
-            "event_direction::{}\n".format(self._ex, self._dir.name)
+            "C++ datatype: {}\nEvent type: non-terminal\nEvent equation: {}\nEvent direction: "
+            "event_direction::{}\n".format(self.__dict__.get("_ctype", "double"), self._ex, self._dir.name)
         )
 
 
@@ -146,9 +147,9 @@ class t_event_batch(_EventBase):
 
     def __repr__(self):
         return (
-            "C++ datatype: double\nEvent type: terminal\nEvent equation: {}\nEvent direction: "
+            "C++ datatype: {}\nEvent type: terminal\nEvent equation: {}\nEvent direction: "
             "event_direction::{}\nWith callback: {}\nCooldown: {}\n".format(
-                self._ex, self._dir.name, "yes" if self._cb is not None else "no",
+                self.__dict__.get("_ctype", "double"), self._ex, self._dir.name, "yes" if self._cb is not None else "no",
                 "auto" if self._cooldown < 0 else repr(self._cooldown),
             )
         )

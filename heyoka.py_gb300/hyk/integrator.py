@@ -11,8 +11,10 @@ follow from living on a GPU:
   reference.  ``time``, ``dtime``, ``tc``, ``last_h``, ``d_output`` are
   read-only NumPy copies, as read-only as the reference's.
 * ``batch_size`` is the number of GPU lanes: any size, not the SIMD width.
-* Step callbacks and single precision raise ``NotImplementedError``; LLVM
-  code-generation options are accepted and ignored.  Events run on the
+* ``fp_type`` is ``float`` (double precision) or ``numpy.float32`` (the
+  reference's float batch integrator: float32 tensors, float kernels).  Step
+  callbacks raise ``NotImplementedError``; LLVM code-generation options are
+  accepted and ignored.  Events run on the
   device; their callbacks run on the host when the step or propagation
   returns (``hyk/events.py``).
 * ``propagate_*`` run every lane to its own final time in one persistent
@@ -41,6 +43,16 @@ from .core import get_module, lanes_struct, stream_handle
 from .decompose import order_from_tol, taylor_decompose
 
 EPS = float(np.finfo(np.float64).eps)
+
+
+def _fp_of(fp_type):
+    """(NumPy dtype, torch dtype) of a supported floating-point type (the
+    reference's dispatch: heyoka/__init__.py:55-86)."""
+    if fp_type in (float, np.float64):
+        return np.float64, torch.float64
+    if fp_type is np.float32:
+        return np.float32, torch.float32
+    raise TypeError('The floating-point type "{}" is not recognized/supported'.format(fp_type))
 
 
 class taylor_outcome(enum.IntEnum):
@@ -94,10 +106,12 @@ class _LLVMStateInfo:
             {k: v for k, v in self.__dict__.items() if not k.startswith("_")})
 
 
-def _to_f64_array(x, what):
+def _to_fp_array(x, what, dt=np.float64):
+    """x as a NumPy array of dtype dt: lossless conversions only for double,
+    rounding to the nearest float for single precision."""
     a = np.asarray(x)
-    if a.dtype != np.float64:
-        a = a.astype(np.float64, casting="safe")
+    if a.dtype != dt:
+        a = a.astype(dt, casting="safe" if dt == np.float64 else "same_kind")
     return a
 
 
@@ -132,15 +146,13 @@ def _dadd(xh, xl, yh, yl):
 class LaneArray(torch.Tensor):
     """A device tensor that also accepts what the reference's NumPy views
     accept: assignment from lists, tuples and NumPy arrays (converted to
-    float64 on the tensor's device), comparison with them, and conversion
+    the tensor's dtype on its device), comparison with them, and conversion
     with ``numpy.asarray``."""
 
     def _coerce(self, value):
         if isinstance(value, torch.Tensor):
             return value.to(device=self.device, dtype=self.dtype)
-        a = np.asarray(value)
-        if a.dtype != np.float64:
-            a = a.astype(np.float64, casting="safe")
+        a = _to_fp_array(value, "value", np.float32 if self.dtype == torch.float32 else np.float64)
         return torch.as_tensor(a, device=self.device)
 
     def __setitem__(self, idx, value):
@@ -198,8 +210,8 @@ class taylor_adaptive_batch:
         self._llvm = llvm
         if kwargs:
             raise TypeError("unexpected keyword argument(s): {}".format(", ".join(sorted(kwargs))))
-        if fp_type not in (float, np.float64):
-            raise NotImplementedError("the GPU batch integrator supports double precision (fp_type=float) only")
+        self._np_dt, self._tdt = _fp_of(fp_type)
+        f32 = self._tdt == torch.float32
         self._high_accuracy = bool(high_accuracy)
         from .events import nt_event_batch, t_event_batch
 
@@ -222,7 +234,7 @@ class taylor_adaptive_batch:
         if self._vsys is not None:
             sys = self._vsys.sys
 
-        st = _to_f64_array(state, "state")
+        st = _to_fp_array(state, "state", self._np_dt)
         if st.ndim != 2:
             raise ValueError(
                 "Invalid state vector passed to the constructor of a batch integrator: "
@@ -233,10 +245,10 @@ class taylor_adaptive_batch:
         evs += [(e.expression, False, int(e.direction), -1.0) for e in self._nt_events]
         self._dec = taylor_decompose(sys, events=evs)
         if st.shape[0] == 0:
-            st = np.zeros((self._dec.n_eq, B))  # an empty initial state means zeros (the reference's rule)
+            st = np.zeros((self._dec.n_eq, B), dtype=self._np_dt)  # an empty initial state means zeros (the reference's rule)
         if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
             # the variational part starts from the identity (state arguments) and zero (parameters)
-            st = np.concatenate([st, self._vsys.initial_variational_state(B)])
+            st = np.concatenate([st, self._vsys.initial_variational_state(B).astype(self._np_dt)])
         if st.shape[0] != self._dec.n_eq:
             raise ValueError(
                 "Inconsistent sizes detected in the initialization of an adaptive Taylor integrator: "
@@ -255,7 +267,7 @@ class taylor_adaptive_batch:
                     "the expected array shape is (n, {}), but the input array has either the wrong "
                     "number of dimensions or the wrong shape".format(B)
                 )
-            pa = _to_f64_array(pa, "pars")
+            pa = _to_fp_array(pa, "pars", self._np_dt)
             if pa.shape[0] < np_:
                 raise ValueError(
                     "Invalid number of parameter values passed to the constructor of an adaptive "
@@ -263,7 +275,7 @@ class taylor_adaptive_batch:
                     "{} parameter(s)".format(pa.shape[0] * B, np_ * B)
                 )
         else:
-            pa = np.zeros((np_, B))
+            pa = np.zeros((np_, B), dtype=self._np_dt)
         if time is not None:
             ti = np.asarray(time)
             if ti.ndim != 1 or ti.shape[0] != B:
@@ -272,30 +284,32 @@ class taylor_adaptive_batch:
                     "the expected array shape is ({}), but the input array has either the wrong "
                     "number of dimensions or the wrong shape".format(B)
                 )
-            ti = _to_f64_array(ti, "time")
+            ti = _to_fp_array(ti, "time", self._np_dt)
         else:
-            ti = np.zeros(B)
-        tol = float(tol)
+            ti = np.zeros(B, dtype=self._np_dt)
+        tol = float(self._np_dt(tol))
         if tol == 0.0:
-            tol = EPS
+            tol = float(np.finfo(self._np_dt).eps)
         self._tol = tol
         self._order = order_from_tol(tol)
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
-        self._mod = get_module(self._dec, self._order, self._dev, block_lanes, pin_arith, team_size, persist_ctas,
-                               self._high_accuracy, global_jets)
+        self._mod_opts = dict(block_lanes=int(block_lanes), pin_arith=bool(pin_arith), team_size=int(team_size),
+                              persist_ctas=int(persist_ctas), high_accuracy=self._high_accuracy,
+                              global_jets=bool(global_jets), float32=f32)
+        self._mod = get_module(self._dec, self._order, self._dev, **self._mod_opts)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)
         self._B = B
-        f64 = dict(dtype=torch.float64, device=self._tdev)
-        self._state = torch.tensor(st, **f64).contiguous()
-        self._pars = torch.tensor(pa, **f64).contiguous()
-        self._thi = torch.tensor(ti, **f64)
-        self._tlo = torch.zeros(B, **f64)
-        self._last_h = torch.zeros(B, **f64)
-        self._tc = torch.zeros((self._dec.n_eq, self._order + 1, B), **f64)
-        self._d_out = torch.zeros((self._dec.n_eq, B), **f64)
+        fr = dict(dtype=self._tdt, device=self._tdev)
+        self._state = torch.tensor(st, **fr).contiguous()
+        self._pars = torch.tensor(pa, **fr).contiguous()
+        self._thi = torch.tensor(ti, **fr)
+        self._tlo = torch.zeros(B, **fr)
+        self._last_h = torch.zeros(B, **fr)
+        self._tc = torch.zeros((self._dec.n_eq, self._order + 1, B), **fr)
+        self._d_out = torch.zeros((self._dec.n_eq, B), **fr)
         self._step_res = None
         self._prop = None  # dict of device arrays of the last propagation
         self._final_tc_mask = None  # lanes whose tc must be the final-state jets
@@ -349,6 +363,10 @@ class taylor_adaptive_batch:
         return _LLVMStateInfo(self, self.__dict__.get("_llvm", {}))
 
     @property
+    def fp_type(self):
+        return float if self._np_dt == np.float64 else np.float32
+
+    @property
     def high_accuracy(self):
         return self._high_accuracy
 
@@ -393,7 +411,7 @@ class taylor_adaptive_batch:
     def _tstate_buf(self):
         buf = self.__dict__.get("_tstate")
         if buf is None:
-            buf = np.zeros((self.n_orig_sv, self._B))
+            buf = np.zeros((self.n_orig_sv, self._B), dtype=self._np_dt)
             self._tstate = buf
         return buf
 
@@ -422,11 +440,11 @@ class taylor_adaptive_batch:
                                  "with the internal state of the integrator")
             inputs = inputs.detach().cpu().numpy()
         arr = np.asarray(inputs)
-        if arr.dtype != np.float64:
+        if arr.dtype != self._np_dt:
             if np.issubdtype(arr.dtype, np.integer) and isinstance(inputs, np.ndarray):
                 raise TypeError("Invalid dtype detected for the inputs of a Taylor map evaluation: the expected "
-                                "dtype is float64, but the dtype is {} instead".format(arr.dtype))
-            arr = arr.astype(np.float64)
+                                "dtype is {}, but the dtype is {} instead".format(np.dtype(self._np_dt).name, arr.dtype))
+            arr = arr.astype(self._np_dt)
         if isinstance(inputs, np.ndarray) and not inputs.flags.c_contiguous:
             raise ValueError("Invalid inputs array detected in a Taylor map evaluation: the array is not C-style "
                              "contiguous, please consider using numpy.ascontiguousarray() to turn it into one")
@@ -444,9 +462,9 @@ class taylor_adaptive_batch:
             raise ValueError("The array of inputs provided for the evaluation of a Taylor map may overlap with "
                              "the internal state of the integrator")
         st = self._state.cpu().numpy()
-        out = np.zeros((self.n_orig_sv, B))
+        out = np.zeros((self.n_orig_sv, B), dtype=self._np_dt)
         for row, comp, a, inv_fact in self._vsys.taylor_map_terms():
-            term = st[row] * inv_fact
+            term = st[row] * self._np_dt(inv_fact)
             for j, e in enumerate(a):
                 if e:
                     term = term * arr[j] ** e
@@ -526,7 +544,8 @@ class taylor_adaptive_batch:
                 if t != t:
                     row.append(None)
                 else:
-                    cd = e.cooldown if e.cooldown >= 0 else 1e-12 * max(1.0, abs(t))
+                    rel = 1e-12 if self._np_dt == np.float64 else float(np.float32(5e-4))
+                    cd = e.cooldown if e.cooldown >= 0 else rel * max(1.0, abs(t))
                     row.append((t, cd))
             out.append(row)
         return out
@@ -562,11 +581,11 @@ class taylor_adaptive_batch:
         nt = max(len(self._t_events), 1)
         return {
             "cap": cap,
-            "t_hi": torch.empty((cap, B), dtype=torch.float64, **f),
-            "t_lo": torch.empty((cap, B), dtype=torch.float64, **f),
+            "t_hi": torch.empty((cap, B), dtype=self._tdt, **f),
+            "t_lo": torch.empty((cap, B), dtype=self._tdt, **f),
             "info": torch.empty((cap, B), dtype=torch.int32, **f),
             "count": torch.zeros(B, dtype=torch.int64, **f),
-            "last": torch.full((nt, B), math.nan, dtype=torch.float64, **f),
+            "last": torch.full((nt, B), math.nan, dtype=self._tdt, **f),
             "sign": torch.zeros(B, dtype=torch.int32, **f),
         }
 
@@ -673,8 +692,8 @@ class taylor_adaptive_batch:
     # ------------------------------------------------------------------ time
     def _lane_vec(self, v, what):
         if _is_scalar(v):
-            return torch.full((self._B,), float(v), dtype=torch.float64, device=self._tdev)
-        a = _to_f64_array(v, what)
+            return torch.full((self._B,), float(self._np_dt(v)), dtype=self._tdt, device=self._tdev)
+        a = _to_fp_array(v, what, self._np_dt)
         if a.ndim != 1 or a.shape[0] != self._B:
             raise ValueError(
                 "Invalid {} passed to a batch integrator: the expected array shape is ({}), "
@@ -682,7 +701,7 @@ class taylor_adaptive_batch:
                     what, self._B
                 )
             )
-        return torch.tensor(a, dtype=torch.float64, device=self._tdev)
+        return torch.tensor(a, dtype=self._tdt, device=self._tdev)
 
     def set_time(self, time):
         t = self._lane_vec(time, "time vector")
@@ -705,7 +724,7 @@ class taylor_adaptive_batch:
         L = _lib.load()
         B = self._B
         oc = torch.empty(B, dtype=torch.int64, device=self._tdev)
-        h = torch.empty(B, dtype=torch.float64, device=self._tdev)
+        h = torch.empty(B, dtype=self._tdt, device=self._tdev)
         md = None
         if max_delta_t is not None:
             md = self._lane_vec(max_delta_t, "max_delta_t vector")
@@ -759,9 +778,10 @@ class taylor_adaptive_batch:
             sh, sl = _dadd(self._thi, self._tlo, -self._last_h, torch.zeros_like(self._last_h))
             dt, _ = _dadd(tt, torch.zeros_like(tt), -sh, -sl)
         L = _lib.load()
+        fn = L.hyk_dense_eval_f32 if self._tdt == torch.float32 else L.hyk_dense_eval
         with torch.cuda.device(self._dev):
             _lib.check(
-                L.hyk_dense_eval(
+                fn(
                     self._tc.data_ptr(), self.dim, self._order, self._B, self._B, dt.contiguous().data_ptr(),
                     self._d_out.data_ptr(), stream_handle(self._dev),
                 ),
@@ -780,7 +800,7 @@ class taylor_adaptive_batch:
             return
         tc = torch.empty_like(self._tc)
         st, th, tl = self._state.clone(), self._thi.clone(), self._tlo.clone()
-        zero = torch.zeros(self._B, dtype=torch.float64, device=self._tdev)
+        zero = torch.zeros(self._B, dtype=self._tdt, device=self._tdev)
         oc = torch.empty(self._B, dtype=torch.int64, device=self._tdev)
         h = torch.empty_like(zero)
         L = _lib.load()
@@ -812,15 +832,15 @@ class taylor_adaptive_batch:
     def _alloc_prop(self, with_grid):
         B, f = self._B, dict(device=self._tdev)
         p = {
-            "rem_hi": torch.empty(B, dtype=torch.float64, **f),
-            "rem_lo": torch.empty(B, dtype=torch.float64, **f),
+            "rem_hi": torch.empty(B, dtype=self._tdt, **f),
+            "rem_lo": torch.empty(B, dtype=self._tdt, **f),
             "outcome": torch.empty(B, dtype=torch.int64, **f),
-            "min_h": torch.empty(B, dtype=torch.float64, **f),
-            "max_h": torch.empty(B, dtype=torch.float64, **f),
+            "min_h": torch.empty(B, dtype=self._tdt, **f),
+            "max_h": torch.empty(B, dtype=self._tdt, **f),
             "n_steps": torch.empty(B, dtype=torch.int64, **f),
             "n_iter": torch.empty(B, dtype=torch.int64, **f),
             "grid_idx": torch.empty(B, dtype=torch.int64, **f) if with_grid else None,
-            "last_h": torch.empty(B, dtype=torch.float64, **f),
+            "last_h": torch.empty(B, dtype=self._tdt, **f),
             "status": torch.empty(B, dtype=torch.int32, **f),
         }
         return p
@@ -835,16 +855,16 @@ class taylor_adaptive_batch:
         p = self._alloc_prop(grid is not None)
         grid_out = None
         if grid is not None:
-            grid_out = torch.empty((grid.shape[0], ne, B), dtype=torch.float64, device=self._tdev)
+            grid_out = torch.empty((grid.shape[0], ne, B), dtype=self._tdt, device=self._tdev)
         want_tc = write_tc or c_output
         last_tc = torch.empty_like(self._tc) if want_tc else None
         cap = 0
         tcs = thi = tlo = None
         if c_output:
             cap = 64
-            tcs = torch.empty((cap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
-            thi = torch.empty((cap, B), dtype=torch.float64, device=self._tdev)
-            tlo = torch.empty((cap, B), dtype=torch.float64, device=self._tdev)
+            tcs = torch.empty((cap, ne, order + 1, B), dtype=self._tdt, device=self._tdev)
+            thi = torch.empty((cap, B), dtype=self._tdt, device=self._tdev)
+            tlo = torch.empty((cap, B), dtype=self._tdt, device=self._tdev)
         t0h, t0l = self._thi.clone(), self._tlo.clone()
 
         def desc():
@@ -898,9 +918,9 @@ class taylor_adaptive_batch:
                 if grow and c_output and bool((p["n_iter"] >= cap).any()):
                     # Grow the coefficient store.
                     ncap = cap * 2
-                    ntcs = torch.empty((ncap, ne, order + 1, B), dtype=torch.float64, device=self._tdev)
-                    nthi = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
-                    ntlo = torch.empty((ncap, B), dtype=torch.float64, device=self._tdev)
+                    ntcs = torch.empty((ncap, ne, order + 1, B), dtype=self._tdt, device=self._tdev)
+                    nthi = torch.empty((ncap, B), dtype=self._tdt, device=self._tdev)
+                    ntlo = torch.empty((ncap, B), dtype=self._tdt, device=self._tdev)
                     ntcs[:cap] = tcs
                     nthi[:cap] = thi
                     ntlo[:cap] = tlo
@@ -930,17 +950,17 @@ class taylor_adaptive_batch:
         B = self._B
         st, th, tl = self._state.clone(), self._thi.clone(), self._tlo.clone()
         oc = torch.empty(B, dtype=torch.int64, device=self._tdev)
-        h = torch.empty(B, dtype=torch.float64, device=self._tdev)
+        h = torch.empty(B, dtype=self._tdt, device=self._tdev)
         with torch.cuda.device(self._dev):
             _lib.check(
                 L.hyk_step(self._mod.handle, lanes_struct(st, self._pars, th, tl), None, 0, oc.data_ptr(),
                            h.data_ptr(), None, self._ev_scratch(), stream_handle(self._dev)),
                 "hyk_step",
             )
-        rem = (tf_hi - self._thi).abs()
+        rem = (tf_hi.double() - self._thi.double()).abs()
         if tf_lo is not None:
-            rem = (rem + tf_lo.abs())
-        est = torch.nan_to_num(rem / h.abs(), nan=0.0, posinf=1e300)
+            rem = (rem + tf_lo.double().abs())
+        est = torch.nan_to_num(rem / h.double().abs(), nan=0.0, posinf=1e300)
         return torch.argsort(est, descending=True).contiguous()
 
     def _finish_prop(self, p, group, last_tc):
@@ -967,10 +987,10 @@ class taylor_adaptive_batch:
         nit = p["n_iter"]
         K = int(nit.max().item()) if B else 0
         ne, order = self.dim, self._order
-        f64 = dict(dtype=torch.float64, device=self._tdev)
-        out_tcs = torch.empty((K, ne, order + 1, B), **f64)
-        out_thi = torch.empty((K + 1, B), **f64)
-        out_tlo = torch.empty((K + 1, B), **f64)
+        fr = dict(dtype=self._tdt, device=self._tdev)
+        out_tcs = torch.empty((K, ne, order + 1, B), **fr)
+        out_thi = torch.empty((K + 1, B), **fr)
+        out_tlo = torch.empty((K + 1, B), **fr)
         out_thi[0], out_tlo[0] = t0h, t0l
         if K:
             out_tcs.copy_(tcs[:K])
@@ -1021,8 +1041,8 @@ class taylor_adaptive_batch:
         return (None, self.propagate_grid_tensor(grid, max_steps, max_delta_t, callback).cpu().numpy())
 
     def propagate_grid_tensor(self, grid, max_steps=0, max_delta_t=[], callback=None):  # noqa: B006
-        """``propagate_grid`` with the output left on the device: a float64
-        CUDA tensor of shape ``(n, dim, batch_size)``."""
+        """``propagate_grid`` with the output left on the device: a CUDA
+        tensor of the integrator's dtype, shape ``(n, dim, batch_size)``."""
         md = self._check_prop_args(max_delta_t, callback)
         g = np.asarray(grid) if not isinstance(grid, torch.Tensor) else grid
         if g.ndim != 2:
@@ -1036,9 +1056,9 @@ class taylor_adaptive_batch:
                 "the shape must be ({}, {}) but the number of columns is {} instead".format("n", self._B, g.shape[1])
             )
         if isinstance(g, torch.Tensor):
-            gd = g.to(device=self._tdev, dtype=torch.float64).contiguous()
+            gd = g.to(device=self._tdev, dtype=self._tdt).contiguous()
         else:
-            gd = torch.tensor(_to_f64_array(g, "grid"), dtype=torch.float64, device=self._tdev)
+            gd = torch.tensor(_to_fp_array(g, "grid", self._np_dt), dtype=self._tdt, device=self._tdev)
         if gd.shape[0] == 0:
             raise ValueError("Cannot invoke propagate_grid() in a batch integrator if the time grid is empty")
         if not bool(torch.isfinite(gd).all()):
@@ -1126,11 +1146,12 @@ class taylor_adaptive_batch:
         self.__dict__.setdefault("_t_events", [])
         self.__dict__.setdefault("_nt_events", [])
         self._tdev = dev
-        self._mod = get_module(self._dec, self._order, self._dev, high_accuracy=self.__dict__.get("_high_accuracy", False))
+        opts = self.__dict__.get("_mod_opts") or dict(high_accuracy=self.__dict__.get("_high_accuracy", False))
+        self._mod = get_module(self._dec, self._order, self._dev, **opts)
 
     def __repr__(self):
         return (
-            "C++ datatype            : double (GPU, {})\n"
+            "C++ datatype            : {} (GPU, {})\n"
             "Tolerance               : {!r}\n"
             "High accuracy           : false\n"
             "Compact mode            : {}\n"
@@ -1140,7 +1161,7 @@ class taylor_adaptive_batch:
             "Time                    : {}\n"
             "State                   : {}\n"
         ).format(
-            self._tdev, self._tol, str(self._compact_mode).lower(), self._order, self.dim, self._B,
+            "double" if self._tdt == torch.float64 else "float", self._tdev, self._tol, str(self._compact_mode).lower(), self._order, self.dim, self._B,
             self.time.tolist() if self._B <= 8 else "[...]",
             self._state.cpu().numpy().tolist() if self._B <= 8 else "[...]",
         )

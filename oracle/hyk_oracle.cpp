@@ -921,21 +921,25 @@ int step_one(const Dec &d, uint32_t p, int mode, uint32_t B, double *state, cons
     return 0;
 }
 
-// Per-lane propagation with events, gpu arithmetic (double): every lane is
-// its own batch of one, stepped exactly as the kernels step it (events after
-// the step size, a terminal event ending the lane at its root).
+// Per-lane propagation with events, gpu arithmetic (double, or float for the
+// float32 integrator): every lane is its own batch of one, stepped exactly as
+// the kernels step it (events after the step size, a terminal event ending
+// the lane at its root).
 struct EvRec {
     std::vector<double> t_hi, t_lo;
     std::vector<int32_t> info;
     std::vector<uint32_t> lane;
 };
 
+template <typename T>
 int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const double *pars, double *t_hi,
                  double *t_lo, const double *tf_hi, uint64_t max_steps, int64_t *outcome, uint64_t *n_steps,
                  uint32_t *status, double *ev_last, int32_t *ev_sign, EvRec &rec) {
     const uint32_t ne = d.n_eq, np = d.n_pars;
-    std::vector<double> bt((size_t)(p + 1) * (p + 1)), work(3 * (p + 1)), g(p + 1);
-    hyk_ev_btab((int)p, bt.data());
+    std::vector<double> btd((size_t)(p + 1) * (p + 1));
+    hyk_ev_btab((int)p, btd.data());
+    std::vector<T> bt(btd.begin(), btd.end()), work(3 * (p + 1)), g(p + 1);
+    const T cool_rel = sizeof(T) == sizeof(float) ? T(HYK_EV_COOL_REL_F) : T(HYK_EV_COOL_REL_D);
     uint32_t n_term = 0;
     std::vector<int> idx(d.ev.size());
     {
@@ -943,66 +947,66 @@ int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const doub
         for (size_t k = 0; k < d.ev.size(); ++k) idx[k] = d.ev[k].terminal ? (int)n_term++ : (int)nn++;
     }
     for (uint32_t l = 0; l < B; ++l) {
-        Batch<double> bq(d, p, 1, 1);
-        for (uint32_t i = 0; i < ne; ++i) bq.state[i] = state[(size_t)i * B + l];
-        for (uint32_t i = 0; i < np; ++i) bq.pars[i] = pars ? pars[(size_t)i * B + l] : 0.0;
-        bq.thi[0] = t_hi[l];
-        bq.tlo[0] = t_lo ? t_lo[l] : 0.0;
-        dfl<double> rem = dsub(dnorm(tf_hi[l], 0.0), dfl<double>{bq.thi[0], bq.tlo[0]});
-        const bool dir = dge(rem, dfl<double>{0.0, 0.0});
+        Batch<T> bq(d, p, 1, 1);
+        for (uint32_t i = 0; i < ne; ++i) bq.state[i] = T(state[(size_t)i * B + l]);
+        for (uint32_t i = 0; i < np; ++i) bq.pars[i] = pars ? T(pars[(size_t)i * B + l]) : T(0);
+        bq.thi[0] = T(t_hi[l]);
+        bq.tlo[0] = t_lo ? T(t_lo[l]) : T(0);
+        dfl<T> rem = dsub(dnorm(T(tf_hi[l]), T(0)), dfl<T>{bq.thi[0], bq.tlo[0]});
+        const bool dir = dge(rem, dfl<T>{T(0), T(0)});
         uint64_t nit = 0, nst = 0;
         int64_t oc = HYK_OUTCOME_TIME_LIMIT;
-        uint32_t st = (rem.hi == 0.0 && rem.lo == 0.0) ? HYK_LANE_DONE : 0u;
-        std::vector<double> h(1);
+        uint32_t st = (rem.hi == T(0) && rem.lo == T(0)) ? HYK_LANE_DONE : 0u;
+        std::vector<T> h(1);
         while (!st) {
-            const double lim = dir ? std::min(HUGE_VAL, rem.hi) : std::max(-HUGE_VAL, rem.hi);
+            const T lim = dir ? std::min(M<T>::inf(), rem.hi) : std::max(-M<T>::inf(), rem.hi);
             bq.jets();
             bq.step_size(h);
-            double hh = lim < 0.0 ? -h[0] : h[0];
+            T hh = lim < T(0) ? -h[0] : h[0];
             if (std::fabs(lim) < std::fabs(hh)) hh = lim;
             int64_t soc = (hh == lim) ? HYK_OUTCOME_TIME_LIMIT : HYK_OUTCOME_SUCCESS;
             // events of the step
-            const double th = bq.thi[0], tl = bq.tlo[0];
+            const T th = bq.thi[0], tl = bq.tlo[0];
             int kt = -1, sgt = 0;
-            double stt = 2.0;
+            T stt = 2;
             size_t rec0 = rec.t_hi.size();
-            if (hh != 0.0) {
-                const double ah = std::fabs(hh);
+            if (hh != T(0)) {
+                const T ah = std::fabs(hh);
                 for (size_t k = 0; k < d.ev.size(); ++k) {
                     if (!d.ev[k].terminal) continue;
                     const int j = idx[k];
-                    double slo = 0.0;
-                    const double last = ev_last[(size_t)j * B + l];
+                    T slo = 0;
+                    const T last = T(ev_last[(size_t)j * B + l]);
                     if (last == last) {
-                        const double cd = d.ev[k].cooldown >= 0.0 ? d.ev[k].cooldown
-                                                                  : 1e-12 * (std::fabs(last) > 1.0 ? std::fabs(last) : 1.0);
-                        const double r = cd - std::fabs(th - last);
-                        if (r > 0.0) slo = r / ah;
+                        const T cool = T(d.ev[k].cooldown);
+                        const T cd = cool >= T(0) ? cool : cool_rel * (std::fabs(last) > T(1) ? std::fabs(last) : T(1));
+                        const T r = cd - std::fabs(th - last);
+                        if (r > T(0)) slo = r / ah;
                     }
-                    if (slo >= 1.0) continue;
+                    if (slo >= T(1)) continue;
                     for (uint32_t n = 0; n <= p; ++n) g[n] = bq.arg_coef(d.ev[k].g, n, 0);
-                    double rs = 0.0;
+                    T rs = 0;
                     int rsg = 0;
-                    const int nf = hyk_ev_find(g.data(), 1, (int)p, hh, bt.data(), slo, 1.0, d.ev[k].direction, 1, &rs,
-                                               &rsg, 1, 1, work.data());
+                    const int nf = hyk_ev_find<T>(g.data(), 1, (int)p, hh, bt.data(), slo, T(1), d.ev[k].direction, 1,
+                                                  &rs, &rsg, 1, 1, work.data());
                     if (nf > 0 && rs < stt) {
                         stt = rs;
                         kt = j;
                         sgt = rsg;
                     }
                 }
-                const double shi = kt >= 0 ? stt : 1.0;
+                const T shi = kt >= 0 ? stt : T(1);
                 for (size_t k = 0; k < d.ev.size(); ++k) {
                     if (d.ev[k].terminal) continue;
                     for (uint32_t n = 0; n <= p; ++n) g[n] = bq.arg_coef(d.ev[k].g, n, 0);
-                    std::vector<double> rs(4096);
+                    std::vector<T> rs(4096);
                     std::vector<int> rsg(4096);
-                    const int nf = hyk_ev_find(g.data(), 1, (int)p, hh, bt.data(), 0.0, shi, d.ev[k].direction, 0,
-                                               rs.data(), rsg.data(), 1, 4096, work.data());
+                    const int nf = hyk_ev_find<T>(g.data(), 1, (int)p, hh, bt.data(), T(0), shi, d.ev[k].direction, 0,
+                                                  rs.data(), rsg.data(), 1, 4096, work.data());
                     for (int r = 0; r < std::min(nf, 4096); ++r) {
-                        const dfl<double> t = dadd(dfl<double>{th, tl}, dfl<double>{rs[r] * hh, 0.0});
-                        rec.t_hi.push_back(t.hi);
-                        rec.t_lo.push_back(t.lo);
+                        const dfl<T> t = dadd(dfl<T>{th, tl}, dfl<T>{rs[r] * hh, T(0)});
+                        rec.t_hi.push_back((double)t.hi);
+                        rec.t_lo.push_back((double)t.lo);
                         rec.info.push_back(4 * idx[k] + rsg[r] + 1);
                         rec.lane.push_back(l);
                     }
@@ -1012,9 +1016,9 @@ int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const doub
                     soc = kt;
                 }
             }
-            std::vector<double> ns(ne);
+            std::vector<T> ns(ne);
             bq.horner(&hh, ns.data());
-            const dfl<double> t = dadd(dfl<double>{th, tl}, dfl<double>{hh, 0.0});
+            const dfl<T> t = dadd(dfl<T>{th, tl}, dfl<T>{hh, T(0)});
             bool fin = std::isfinite(t.hi);
             for (uint32_t i = 0; i < ne; ++i) fin = fin && std::isfinite(ns[i]);
             bq.state.assign(ns.begin(), ns.end());
@@ -1030,17 +1034,17 @@ int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const doub
                 st = HYK_LANE_STOPPED;
                 break;
             }
-            nst += hh != 0.0;
-            rem = (hh == rem.hi) ? dfl<double>{0.0, 0.0} : dsub(rem, dfl<double>{hh, 0.0});
+            nst += hh != T(0);
+            rem = (hh == rem.hi) ? dfl<T>{T(0), T(0)} : dsub(rem, dfl<T>{hh, T(0)});
             oc = soc;
             if (kt >= 0) {
-                ev_last[(size_t)kt * B + l] = t.hi;
+                ev_last[(size_t)kt * B + l] = (double)t.hi;
                 ev_sign[l] = sgt;
                 oc = -(int64_t)kt - 1;
                 st = HYK_LANE_STOPPED | HYK_LANE_EVENT;
                 break;
             }
-            if (rem.hi == 0.0 && rem.lo == 0.0) {
+            if (rem.hi == T(0) && rem.lo == T(0)) {
                 oc = HYK_OUTCOME_TIME_LIMIT;
                 st = HYK_LANE_DONE;
                 break;
@@ -1051,9 +1055,9 @@ int propagate_ev(const Dec &d, uint32_t p, uint32_t B, double *state, const doub
                 break;
             }
         }
-        for (uint32_t i = 0; i < ne; ++i) state[(size_t)i * B + l] = bq.state[i];
-        t_hi[l] = bq.thi[0];
-        if (t_lo) t_lo[l] = bq.tlo[0];
+        for (uint32_t i = 0; i < ne; ++i) state[(size_t)i * B + l] = (double)bq.state[i];
+        t_hi[l] = (double)bq.thi[0];
+        if (t_lo) t_lo[l] = (double)bq.tlo[0];
         outcome[l] = oc;
         n_steps[l] = nst;
         status[l] = st;
@@ -1067,7 +1071,8 @@ extern "C" {
 
 const char *hyko_last_error(void) { return g_err.c_str(); }
 
-// Per-lane propagation to tf_hi with events (gpu arithmetic, double).  The
+// Per-lane propagation to tf_hi with events (gpu arithmetic; prec 0 double,
+// 2 float).  The
 // non-terminal roots come back in malloc'ed arrays (free with hyko_free) in
 // the order the kernels record them per lane: (time hi, time lo, info =
 // 4 * event index + direction + 1, lane).  ev_last (n_terminal, B) and ev_sign
@@ -1075,7 +1080,7 @@ const char *hyko_last_error(void) { return g_err.c_str(); }
 int hyko_propagate_ev(const hyk_decomp_t *dd, uint32_t order, uint32_t B, double *state, const double *pars,
                       double *t_hi, double *t_lo, const double *tf_hi, uint64_t max_steps, int64_t *outcome,
                       uint64_t *n_steps, uint32_t *status, double *ev_last, int32_t *ev_sign, uint64_t *n_rec,
-                      double **rec_t_hi, double **rec_t_lo, int32_t **rec_info, uint32_t **rec_lane) {
+                      double **rec_t_hi, double **rec_t_lo, int32_t **rec_info, uint32_t **rec_lane, int prec) {
     Dec d;
     if (!load_dec(dd, d)) return HYK_ERR_INVALID;
     if (order < 2 || B == 0) {
@@ -1083,8 +1088,10 @@ int hyko_propagate_ev(const hyk_decomp_t *dd, uint32_t order, uint32_t B, double
         return HYK_ERR_INVALID;
     }
     EvRec rec;
-    const int r = propagate_ev(d, order, B, state, pars, t_hi, t_lo, tf_hi, max_steps, outcome, n_steps, status,
-                               ev_last, ev_sign, rec);
+    const int r = prec == 2 ? propagate_ev<float>(d, order, B, state, pars, t_hi, t_lo, tf_hi, max_steps, outcome,
+                                                  n_steps, status, ev_last, ev_sign, rec)
+                            : propagate_ev<double>(d, order, B, state, pars, t_hi, t_lo, tf_hi, max_steps, outcome,
+                                                   n_steps, status, ev_last, ev_sign, rec);
     auto dup = [](const void *src, size_t bytes) {
         void *q = std::malloc(std::max<size_t>(bytes, 8));
         if (bytes) std::memcpy(q, src, bytes);
@@ -1104,8 +1111,8 @@ int hyko_ev_find(const double *g, uint32_t p, double h, double s_lo, double s_hi
     std::vector<double> bt((size_t)(p + 1) * (p + 1)), work(3 * (p + 1));
     hyk_ev_btab((int)p, bt.data());
     std::vector<int> sg(std::max(maxr, 1));
-    const int n = hyk_ev_find(g, 1, (int)p, h, bt.data(), s_lo, s_hi, dir, first_only, rs, sg.data(), 1, maxr,
-                              work.data());
+    const int n = hyk_ev_find<double>(g, 1, (int)p, h, bt.data(), s_lo, s_hi, dir, first_only, rs, sg.data(), 1, maxr,
+                                      work.data());
     for (int i = 0; i < std::min(n, maxr); ++i) rsg[i] = sg[i];
     return n;
 }

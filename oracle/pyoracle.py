@@ -60,7 +60,7 @@ def lib():
         L.hyko_propagate_ev.argtypes = [
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_uint32, pd, pd, pd, pd, pd, ctypes.c_uint64, pi64, pu64,
             P(ctypes.c_uint32), pd, P(ctypes.c_int32), pu64, P(pd), P(pd), P(P(ctypes.c_int32)),
-            P(P(ctypes.c_uint32)),
+            P(P(ctypes.c_uint32)), ctypes.c_int,
         ]
         L.hyko_ev_find.argtypes = [pd, ctypes.c_uint32, c_d, c_d, c_d, ctypes.c_int, ctypes.c_int, pd,
                                    P(ctypes.c_int32), ctypes.c_int]
@@ -225,10 +225,11 @@ def ev_find(g, h, s_lo=0.0, s_hi=1.0, direction=0, first_only=False, maxr=256):
     return rs[: min(n, maxr)], rsg[: min(n, maxr)], n
 
 
-def propagate_ev(sys_, events, state, tf, pars=None, order=20, max_steps=0, time=None, ev_last=None, time_lo=None):
+def propagate_ev(sys_, events, state, tf, pars=None, order=20, max_steps=0, time=None, ev_last=None, time_lo=None,
+                 prec=0):
     """Per-lane propagation with events in gpu arithmetic, the kernels'
-    semantics.  events: (expression, terminal, direction, cooldown) tuples in
-    the integrator's order (terminal events first).  Returns a dict with
+    semantics (prec 0 double, 2 float).  events: (expression, terminal,
+    direction, cooldown) tuples in the integrator's order (terminal events first).  Returns a dict with
     state, t_hi, t_lo, outcome, n_steps, status, ev_last, ev_sign and the
     non-terminal records (rec_t_hi, rec_t_lo, rec_info, rec_lane)."""
     dec = taylor_decompose(sys_, events=events)
@@ -252,7 +253,7 @@ def propagate_ev(sys_, events, state, tf, pars=None, order=20, max_steps=0, time
     rc = L.hyko_propagate_ev(ctypes.byref(cdec), order, B, _p(st), _p(pa), _p(th), _p(tl), _p(tfv), max_steps,
                              _p(oc, pi64), _p(ns, pu64), status.ctypes.data_as(P(ctypes.c_uint32)), _p(last),
                              sign.ctypes.data_as(P(ctypes.c_int32)), ctypes.byref(nrec), ctypes.byref(rh),
-                             ctypes.byref(rl), ctypes.byref(ri), ctypes.byref(rln))
+                             ctypes.byref(rl), ctypes.byref(ri), ctypes.byref(rln), int(prec))
     if rc != 0:
         raise RuntimeError(L.hyko_last_error().decode())
     n = nrec.value

@@ -166,3 +166,27 @@ def test_oracle_reference_event_counts(oracle):
         assert list(ks) == [0, 1, 0] * 4
         t = np.sort(r["rec_t_hi"][m])
         assert np.all(np.diff(t) > 0)
+
+
+def test_oracle_events_harmonic_oscillator_float32(oracle):
+    """The float32 event path (root finder and event bookkeeping in single
+    precision): roots of x and v of the harmonic oscillator at the analytic
+    times, to single-precision accuracy; terminal event with the automatic
+    cooldown of the float integrator."""
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -x)]
+    st = np.array([[1.0, 2.0, -0.5], [0.0, 0.0, 0.0]])
+    r = oracle.propagate_ev(sys_, [(x, False, 0, -1.0), (v, False, 1, -1.0)], st, 20.0, order=9, prec=2)
+    for lane in range(3):
+        m = r["rec_lane"] == lane
+        t = r["rec_t_hi"][m] + r["rec_t_lo"][m]
+        info = r["rec_info"][m]
+        tx = np.sort(t[(info >> 2) == 0])
+        assert len(tx) == 6 and np.allclose(tx, [math.pi / 2 + k * math.pi for k in range(6)], atol=2e-5)
+        assert np.all(r["rec_t_hi"][m] == r["rec_t_hi"][m].astype(np.float32))
+    r = oracle.propagate_ev(sys_, [(x, True, 1, -1.0)], st, 20.0, order=9, prec=2)
+    assert list(r["outcome"]) == [-1, -1, -1] and list(r["ev_sign"]) == [1, 1, 1]
+    assert np.allclose(r["t_hi"], [1.5 * math.pi, 1.5 * math.pi, 0.5 * math.pi], atol=2e-5)
+    r2 = oracle.propagate_ev(sys_, [(x, True, 1, -1.0)], r["state"], 20.0, order=9, prec=2, time=r["t_hi"],
+                             time_lo=r["t_lo"], ev_last=r["ev_last"])
+    assert np.allclose(r2["t_hi"], r["t_hi"] + 2 * math.pi, atol=5e-5)

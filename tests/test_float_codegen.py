@@ -1,7 +1,7 @@
 """Single-precision recurrences on the CPU.
 
 The code generator's float32 modules (heyoka's ``taylor_adaptive_batch`` with
-``fp_type=float``) are built for the host, both kernel forms, and compared bit
+``fp_type=numpy.float32``) are built for the host, both kernel forms, and compared bit
 for bit with the oracle's float gpu-arithmetic step: every Taylor
 coefficient and the stepped state.  The systems cover every operation and
 operand kind (the float elementary functions included)."""
@@ -75,16 +75,29 @@ def test_float_step_close_to_double(oracle):
     assert np.allclose(of.state, od.state, rtol=0, atol=5e-6)
 
 
-def test_float_module_rejects_pin_adjoint_events(libhyk):
-    """Single precision has no pin arithmetic, adjoint or events; the module
+def test_float_module_rejects_pin_adjoint(libhyk):
+    """Single precision has no pin arithmetic and no adjoint; the module
     constructor refuses them before it looks for a device."""
     import hyk
 
     x, v = hyk.make_vars("x", "v")
     d, keep = taylor_decompose([(x, v), (v, -hyk.sin(x))]).as_c()
-    de, keep_e = taylor_decompose([(x, v), (v, -hyk.sin(x))], events=[(x, 0, 0, -1.0)]).as_c()
     m = ctypes.c_void_p()
-    for dec, extra in ((d, _lib.HYK_CFG_PIN_ARITH), (d, _lib.HYK_CFG_ADJOINT), (de, 0)):
+    for dec, extra in ((d, _lib.HYK_CFG_PIN_ARITH), (d, _lib.HYK_CFG_ADJOINT)):
         cfg = _lib.hyk_config_t(0, 0, _lib.HYK_CFG_FLOAT32 | extra, 0)
         rc = libhyk.hyk_module_create(ctypes.byref(dec), 9, ctypes.byref(cfg), 0, ctypes.byref(m))
         assert rc == _lib.HYK_ERR_UNSUPPORTED and b"single precision" in libhyk.hyk_last_error()
+
+
+def test_float32_integrator_argument_checks():
+    """Python-side checks of the float32 integrator that run before any device
+    is touched: unsupported floating-point types."""
+    import hyk
+
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -hyk.sin(x))]
+    with pytest.raises(TypeError, match="not recognized/supported"):
+        hyk.taylor_adaptive_batch(sys_, [[0.1], [0.2]], fp_type=np.float16)
+    with pytest.raises(TypeError, match="not recognized/supported"):
+        hyk.t_event_batch(x, fp_type=np.float16)
+    assert repr(hyk.t_event_batch(x, fp_type=np.float32)).startswith("C++ datatype: float")
