@@ -70,23 +70,25 @@ __global__ void dmath_kernel(int fn, const double *__restrict__ x, const double 
     }
 }
 
-// FP64 FMA throughput: each thread runs 8 independent dependency chains of
-// `iters` fused multiply-adds.  The values stay bounded (a*x + b with a < 1).
-__global__ void fp64_fma_kernel(double *sink, uint64_t iters, double a, double b) {
-    double x0 = threadIdx.x * 1e-3, x1 = x0 + 0.1, x2 = x0 + 0.2, x3 = x0 + 0.3;
-    double x4 = x0 + 0.4, x5 = x0 + 0.5, x6 = x0 + 0.6, x7 = x0 + 0.7;
+// FMA throughput (FP64, or FP32 for the float integrator's roofline): each
+// thread runs 8 independent dependency chains of `iters` fused multiply-adds.
+// The values stay bounded (a*x + b with a < 1).
+template <typename R>
+__global__ void fma_probe_kernel(R *sink, uint64_t iters, R a, R b) {
+    R x0 = (R)threadIdx.x * (R)1e-3, x1 = x0 + (R)0.1, x2 = x0 + (R)0.2, x3 = x0 + (R)0.3;
+    R x4 = x0 + (R)0.4, x5 = x0 + (R)0.5, x6 = x0 + (R)0.6, x7 = x0 + (R)0.7;
     for (uint64_t i = 0; i < iters; ++i) {
-        x0 = __fma_rn(x0, a, b);
-        x1 = __fma_rn(x1, a, b);
-        x2 = __fma_rn(x2, a, b);
-        x3 = __fma_rn(x3, a, b);
-        x4 = __fma_rn(x4, a, b);
-        x5 = __fma_rn(x5, a, b);
-        x6 = __fma_rn(x6, a, b);
-        x7 = __fma_rn(x7, a, b);
+        x0 = fma_rn(x0, a, b);
+        x1 = fma_rn(x1, a, b);
+        x2 = fma_rn(x2, a, b);
+        x3 = fma_rn(x3, a, b);
+        x4 = fma_rn(x4, a, b);
+        x5 = fma_rn(x5, a, b);
+        x6 = fma_rn(x6, a, b);
+        x7 = fma_rn(x7, a, b);
     }
-    const double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
-    if (s == 1234.5678) sink[blockIdx.x] = s;  // keeps the chains alive
+    const R s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == (R)1234.5678) sink[blockIdx.x] = s;  // keeps the chains alive
 }
 
 }  // namespace
@@ -122,7 +124,8 @@ extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lan
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
-extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen) {
+template <typename R>
+static int fma_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen) {
     auto bad = [&](cudaError_t e, const char *what) {
         std::snprintf(err, errlen, "%s: %s", what, cudaGetErrorString(e));
         return -2;
@@ -131,10 +134,10 @@ extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_pe
     if (e != cudaSuccess) return bad(e, "cudaSetDevice");
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device);
-    double *sink = nullptr;
+    R *sink = nullptr;
     const int blocks_per_sm = 4, threads = 256;
     const int grid = n_sm * blocks_per_sm;
-    e = cudaMalloc(&sink, sizeof(double) * grid);
+    e = cudaMalloc(&sink, sizeof(R) * grid);
     if (e != cudaSuccess) return bad(e, "cudaMalloc");
     cudaEvent_t a, b;
     cudaEventCreate(&a);
@@ -143,20 +146,20 @@ extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_pe
     uint64_t iters = 1 << 12;
     float ms = 0.f;
     for (int pass = 0; pass < 2; ++pass) {
-        fp64_fma_kernel<<<grid, threads>>>(sink, iters, 0.999999, 1e-6);  // warm-up
+        fma_probe_kernel<R><<<grid, threads>>>(sink, iters, (R)0.999999, (R)1e-6);  // warm-up
         cudaEventRecord(a);
-        fp64_fma_kernel<<<grid, threads>>>(sink, iters, 0.999999, 1e-6);
+        fma_probe_kernel<R><<<grid, threads>>>(sink, iters, (R)0.999999, (R)1e-6);
         cudaEventRecord(b);
         e = cudaEventSynchronize(b);
         if (e != cudaSuccess) {
             cudaFree(sink);
-            return bad(e, "fp64 probe");
+            return bad(e, "FMA probe");
         }
         cudaEventElapsedTime(&ms, a, b);
         if (pass == 0 && ms > 0.f) {
             double scale = millis / ms;
             if (scale < 1.0) scale = 1.0;
-            if (scale > 4096.0) scale = 4096.0;
+            if (scale > 65536.0) scale = 65536.0;
             iters = (uint64_t)(iters * scale);
         }
     }
@@ -166,4 +169,12 @@ extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_pe
     const double fmas = (double)grid * threads * 8.0 * (double)iters;
     *flops_per_s = 2.0 * fmas / (ms * 1e-3);
     return 0;
+}
+
+extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen) {
+    return fma_peak<double>(device, millis, flops_per_s, err, errlen);
+}
+
+extern "C" int hyk_generic_fp32_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen) {
+    return fma_peak<float>(device, millis, flops_per_s, err, errlen);
 }

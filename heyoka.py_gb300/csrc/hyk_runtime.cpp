@@ -34,6 +34,7 @@ extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t 
 extern "C" int hyk_generic_dense_eval_f32(const float *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes,
                                           uint64_t ld, const float *dt, float *out, void *stream);
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
+extern "C" int hyk_generic_fp32_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
 extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
 extern "C" int hyk_noalloc_scratch(int device, void **ptr, size_t *bytes, char *err, size_t errlen);
@@ -337,13 +338,17 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     } else if (blk == 0) {
         // Pick the block size maximising resident lanes per SM under the
         // shared-memory budget (1 KiB per CTA is reserved by the hardware),
-        // capped at 512 lanes per SM and 256 per CTA.
+        // capped at 256 per CTA and at 512 lanes per SM in double precision
+        // (the FP64 pipe saturates with far fewer warps) or 768 in single
+        // precision (more warps hide the dependent-issue latency of the
+        // FP32 pipe).
+        const uint32_t lane_cap = f32 ? 768u : 512u;
         uint32_t best = 0, best_lanes = 0;
         for (uint32_t b = 32; b <= 256; b += 32) {
             const size_t per_cta = b * lane_bytes;
             if (per_cta > (size_t)dv.smem_optin) break;
             uint32_t ctas = (uint32_t)((size_t)dv.smem_per_sm / (per_cta + 1024));
-            uint32_t lanes = std::min<uint32_t>(ctas * b, 512);
+            uint32_t lanes = std::min<uint32_t>(ctas * b, lane_cap);
             if (lanes >= best_lanes) {
                 best_lanes = lanes;
                 best = b;
@@ -798,6 +803,13 @@ int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64
 int hyk_fp64_peak(int device, double millis, double *flops_per_s) {
     char buf[256] = {0};
     const int rc = hyk_generic_fp64_peak(device, millis, flops_per_s, buf, sizeof buf);
+    if (rc) return fail(HYK_ERR_CUDA, buf);
+    return 0;
+}
+
+int hyk_fp32_peak(int device, double millis, double *flops_per_s) {
+    char buf[256] = {0};
+    const int rc = hyk_generic_fp32_peak(device, millis, flops_per_s, buf, sizeof buf);
     if (rc) return fail(HYK_ERR_CUDA, buf);
     return 0;
 }

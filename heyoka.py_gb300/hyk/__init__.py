@@ -39,3 +39,14 @@ def fp64_peak(device=0, millis=200.0):
     v = ctypes.c_double()
     _lib.check(_lib.load().hyk_fp64_peak(int(device), float(millis), ctypes.byref(v)), "hyk_fp64_peak")
     return v.value
+
+
+def fp32_peak(device=0, millis=200.0):
+    """Measured FP32 FMA throughput of the device in flop/s (2 flops per FMA)."""
+    import ctypes
+
+    from . import _lib
+
+    v = ctypes.c_double()
+    _lib.check(_lib.load().hyk_fp32_peak(int(device), float(millis), ctypes.byref(v)), "hyk_fp32_peak")
+    return v.value

@@ -143,6 +143,7 @@ SIGNATURES = {
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_dense_eval_f32": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
+    "hyk_fp32_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),
     "hyk_codegen_check": (
         c_int,

@@ -343,6 +343,8 @@ int hyk_dmath_eval(int fn, const double *x, const double *a, double *out, uint64
  * as the roofline denominator.  Runs for about `millis` milliseconds; uses a
  * one-double-per-CTA scratch buffer of its own. */
 int hyk_fp64_peak(int device, double millis, double *flops_per_s);
+/* The same probe in FP32 (the single-precision integrator's roofline). */
+int hyk_fp32_peak(int device, double millis, double *flops_per_s);
 
 /* Build check without a GPU: generate the module source for `d` at `order`
  * (block size cfg->block_lanes, default 128) and compile it with NVRTC for

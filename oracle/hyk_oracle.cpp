@@ -1203,7 +1203,8 @@ void hyko_dm_eval(int fn, const double *x, const double *a, double *out, uint64_
 // stride n_lanes.  Returns the total number of non-zero steps in *total_steps.
 int hyko_ensemble_until(const hyk_decomp_t *dd, uint32_t order, int mode, uint32_t B, uint64_t n_lanes,
                         double *state, const double *pars, double *t_hi, double *t_lo, const double *tf,
-                        int n_threads, int64_t *outcome, double *min_h, double *max_h, uint64_t *n_steps) {
+                        int n_threads, int64_t *outcome, double *min_h, double *max_h, uint64_t *n_steps,
+                        int prec) {
     Dec d;
     if (!load_dec(dd, d)) return HYK_ERR_INVALID;
     if (order < 2 || B == 0) {
@@ -1236,7 +1237,10 @@ int hyko_ensemble_until(const hyk_decomp_t *dd, uint32_t order, int mode, uint32
         std::vector<double> vt, vh, vl;
         PropIO io{st.data(), pa.data(), th.data(), tl.data(), tfh.data(), nullptr, 0, nullptr, nullptr, 0, nullptr,
                   0, &vt, &vh, &vl, oc.data(), mn.data(), mx.data(), ns.data(), nullptr, nullptr, nullptr};
-        propagate<double>(d, order, mode, bl, io);
+        if (prec == 2)
+            propagate<float>(d, order, mode, bl, io);
+        else
+            propagate<double>(d, order, mode, bl, io);
         for (uint32_t i = 0; i < ne; ++i)
             for (uint32_t l = 0; l < bl; ++l) state[(size_t)i * n_lanes + l0 + l] = st[(size_t)i * bl + l];
         for (uint32_t l = 0; l < bl; ++l) {

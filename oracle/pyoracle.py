@@ -55,7 +55,7 @@ def lib():
         ]
         L.hyko_ensemble_until.argtypes = [
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
-            pd, pd, pd, pd, pd, ctypes.c_int, pi64, pd, pd, pu64,
+            pd, pd, pd, pd, pd, ctypes.c_int, pi64, pd, pd, pu64, ctypes.c_int,
         ]
         L.hyko_propagate_ev.argtypes = [
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_uint32, pd, pd, pd, pd, pd, ctypes.c_uint64, pi64, pu64,
@@ -192,8 +192,9 @@ def _dadd(xh, xl, yh, yl):
     return hi, lo
 
 
-def ensemble_until(sys_or_dec, state, pars, t0, tf, order, batch=8, n_threads=0, mode=1):
-    """Ensemble of batch integrators of `batch` lanes each (OpenMP over batches)."""
+def ensemble_until(sys_or_dec, state, pars, t0, tf, order, batch=8, n_threads=0, mode=1, prec=0):
+    """Ensemble of batch integrators of `batch` lanes each (OpenMP over
+    batches); prec 0 double, 2 float."""
     dec = sys_or_dec if hasattr(sys_or_dec, "ops") else taylor_decompose(sys_or_dec)
     cdec, keep = dec.as_c()
     state = _f64(state).copy()
@@ -207,7 +208,7 @@ def ensemble_until(sys_or_dec, state, pars, t0, tf, order, batch=8, n_threads=0,
     ns = np.zeros(n, dtype=np.uint64)
     rc = lib().hyko_ensemble_until(
         ctypes.byref(cdec), order, mode, batch, n, _p(state), _p(pars) if pars.size else None,
-        _p(t_hi), _p(t_lo), _p(tfa), int(n_threads), _p(oc, pi64), _p(mn), _p(mx), _p(ns, pu64),
+        _p(t_hi), _p(t_lo), _p(tfa), int(n_threads), _p(oc, pi64), _p(mn), _p(mx), _p(ns, pu64), int(prec),
     )
     if rc != 0:
         raise RuntimeError(lib().hyko_last_error().decode())

@@ -208,19 +208,30 @@ def test_reference_propagate_outcome_and_cooldowns():
     assert ta.te_cooldowns[0][0] is None and ta.te_cooldowns[1][0] is None
 
 
+def _nt_noop(ta, t, d_sgn, bidx):
+    pass
+
+
+class _Counting:
+    """A stateful terminal callback (module level, so that plain pickle
+    serialises it where cloudpickle is not installed)."""
+
+    def __init__(self):
+        self.n = 0
+
+    def __call__(self, ta, d_sgn, bidx):
+        self.n += 1
+        return True
+
+
 def test_reference_event_pickling():
     """heyoka/_test_batch_integrator.py:605-690: integrators with events
     survive pickling, stateful callbacks included."""
     import pickle
 
-    pytest.importorskip("cloudpickle")
     x, v, sys_ = pend()
-
-    def cb0(ta, t, d_sgn, bidx):
-        pass
-
     ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]]),
-                                   nt_events=[nt_event_batch(v * v - 1e-6, cb0)])
+                                   nt_events=[nt_event_batch(v * v - 1e-6, _nt_noop)])
     for _ in range(4):
         ta.step()
     ta2 = pickle.loads(pickle.dumps(ta))
@@ -230,15 +241,7 @@ def test_reference_event_pickling():
     ta2.step()
     assert np.all(np.asarray(ta.state) == np.asarray(ta2.state))
 
-    class cb1:
-        def __init__(self):
-            self.n = 0
-
-        def __call__(self, ta, d_sgn, bidx):
-            self.n += 1
-            return True
-
-    clb = cb1()
+    clb = _Counting()
     ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]]),
                                    t_events=[t_event_batch(v, callback=clb)])
     assert id(clb) != id(ta.t_events[0].callback) and ta.t_events[0].callback.n == 0

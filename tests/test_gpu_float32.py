@@ -222,13 +222,11 @@ def test_float32_reference_s11n():
     """heyoka/_test_batch_integrator.py test_s11n, float32 case."""
     import pickle
 
+    from test_gpu_events import _Counting, _nt_noop
+
     x, v, sys_ = _pend()
-
-    def cb0(ta, t, d_sgn, bidx):
-        pass
-
     ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]], dtype=f32),
-                                   nt_events=[hyk.nt_event_batch(v * v - 1e-6, cb0, fp_type=f32)], fp_type=f32)
+                                   nt_events=[hyk.nt_event_batch(v * v - 1e-6, _nt_noop, fp_type=f32)], fp_type=f32)
     for _ in range(4):
         ta.step()
     ta2 = pickle.loads(pickle.dumps(ta))
@@ -243,15 +241,7 @@ def test_float32_reference_s11n():
     ta = pickle.loads(pickle.dumps(ta))
     assert ta.foo == "hello world"
 
-    class cb1:
-        def __init__(self):
-            self.n = 0
-
-        def __call__(self, ta, d_sgn, bidx):
-            self.n = self.n + 1
-            return True
-
-    clb = cb1()
+    clb = _Counting()
     ta = hyk.taylor_adaptive_batch(sys_, np.array([[0, 0.01], [0.25, 0.26]], dtype=f32),
                                    t_events=[hyk.t_event_batch(v, callback=clb, fp_type=f32)], fp_type=f32)
     assert id(clb) != id(ta.t_events[0].callback) and ta.t_events[0].callback.n == 0
