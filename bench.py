@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
     ap.add_argument("--members", type=int, default=65536, help="oss, cr3bp-adjoint: trajectories")
+    ap.add_argument("--autotune", action="store_true",
+                    help="oss: pick the kernel configuration by measurement (hyk.autotune, cached per system)")
     ap.add_argument("--team-size", type=int, default=0,
                     help="threads per trajectory (0: chosen per system, 1: lane form, 2..32: team form)")
     return ap.parse_args()
@@ -396,7 +398,9 @@ def run_oss(args):
     n = args.members
     st, t_end = W.oss_ics(n, seed=2)
     grid = np.linspace(0.0, 1.0, 100).reshape(-1, 1) * t_end.reshape(1, -1)
-    ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=args.team_size)
+    t_tune = time.perf_counter()
+    ta = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=args.team_size, autotune=args.autotune)
+    t_tune = time.perf_counter() - t_tune
     gd = torch.tensor(grid, device="cuda")
     sd = torch.tensor(st, device="cuda")
     g_host = torch.tensor(grid).pin_memory()
@@ -450,6 +454,9 @@ def run_oss(args):
                    "threads_per_trajectory": info["team_size"],
                    "jets": "global memory" if info["smem_per_lane"] == 0 else "shared memory",
                    "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"],
+                   "autotune": None if ta._autotune is None else {"best": ta._autotune["best"],
+                                                                 "cached": ta._autotune["cached"],
+                                                                 "construct_s": t_tune},
                    "l2": "inputs and the 1.9 GB output exceed L2"},
         "trajectory_steps": steps, "device_s": t_dev, "kernel_s": t_k,
         "e2e": {"value": steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -594,9 +601,13 @@ def run_forms(args):
     ]
     for name, sys_, st, pars, tf, teams in cases:
         s0 = torch.tensor(st, device="cuda")
-        for T in teams:
+        for T in teams + ["autotune"]:
             gj = T == "global"  # one thread per trajectory, coefficients in global memory
-            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=1e-15, team_size=1 if gj else T, global_jets=gj)
+            at = T == "autotune"  # measured choice (hyk.autotune)
+            t_c = time.perf_counter()
+            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=1e-15, team_size=1 if gj else (0 if at else T),
+                                           global_jets=gj, autotune=at)
+            t_c = time.perf_counter() - t_c
             info = ta.module_info
             ta.propagate_until(tf * 0.01)
             best = 1e30
@@ -614,7 +625,9 @@ def run_forms(args):
                               "jets": "global" if info["smem_per_lane"] == 0 else "shared",
                               "block_threads": info["block_lanes"], "ctas_per_sm": info["ctas_per_sm"],
                               "regs": info["regs_per_thread"], "s": best, "trajectory_steps_per_s": steps / best,
-                              "fp64_frac_of_measured": fl / peak}), flush=True)
+                              "fp64_frac_of_measured": fl / peak,
+                              **({"autotune_best": ta._autotune["best"], "construct_s": t_c} if at else {})}),
+                  flush=True)
 
 
 def main():

@@ -48,7 +48,7 @@ thread_local std::string g_err;
 // driver entry point goes through this table.
 #define HYK_STR2(x) #x
 #define HYK_STR(x) HYK_STR2(x)
-#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy)
 
 struct DriverApi {
 #define HYK_DECL(f) decltype(&::f) f = nullptr;
@@ -514,14 +514,58 @@ static uint64_t lane_blocks(const hyk_module *m, uint64_t n) {
     return (n + per - 1) / per;
 }
 
+// Grid of a launch of f: in global-memory mode every kernel but the
+// initialisation runs on the fixed grid the coefficient buffer is sized for.
+static uint64_t launch_grid(const hyk_module *m, CUfunction f, uint64_t grid) {
+    if (m->gmem && f != m->f_init) grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * m->ctas_per_sm);
+    return grid;
+}
+
 static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k, void *stream) {
     if (grid == 0) return 0;
     k.jets = reinterpret_cast<double *>(m->jets);
-    // In global-memory mode every kernel runs on the fixed grid the buffer is sized for.
-    if (m->gmem && f != m->f_init) grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * m->ctas_per_sm);
+    grid = launch_grid(m, f, grid);
     if (grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
     void *args[] = {&k};
     HYK_CU(drv().cuLaunchKernel(f, (unsigned)grid, 1, 1, blk, 1, 1, (unsigned)smem, (CUstream)stream, args, nullptr));
+    return 0;
+}
+
+// A CUDA graph of `count` launches of f with the same parameters, in
+// sequence (the plain propagation's launches between two reads of the
+// finished-lane counter).  The parameter block is copied into the nodes.
+struct LaunchGraph {
+    CUgraph g = nullptr;
+    CUgraphExec x = nullptr;
+    ~LaunchGraph() {
+        if (x) drv().cuGraphExecDestroy(x);
+        if (g) drv().cuGraphDestroy(g);
+    }
+};
+
+static int build_graph(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k,
+                       uint32_t count, LaunchGraph &lg) {
+    k.jets = reinterpret_cast<double *>(m->jets);
+    grid = launch_grid(m, f, grid);
+    if (grid == 0 || grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
+    HYK_CU(drv().cuGraphCreate(&lg.g, 0));
+    void *args[] = {&k};
+    CUDA_KERNEL_NODE_PARAMS np;
+    std::memset(&np, 0, sizeof np);
+    np.func = f;
+    np.gridDimX = (unsigned)grid;
+    np.gridDimY = np.gridDimZ = 1;
+    np.blockDimX = blk;
+    np.blockDimY = np.blockDimZ = 1;
+    np.sharedMemBytes = (unsigned)smem;
+    np.kernelParams = args;
+    CUgraphNode prev = nullptr;
+    for (uint32_t c = 0; c < count; ++c) {
+        CUgraphNode node;
+        HYK_CU(drv().cuGraphAddKernelNode(&node, lg.g, prev ? &prev : nullptr, prev ? 1 : 0, &np));
+        prev = node;
+    }
+    HYK_CU(drv().cuGraphInstantiate(&lg.x, lg.g, 0));
     return 0;
 }
 
@@ -649,7 +693,9 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (mode != HYK_MODE_PLAIN) return fail(HYK_ERR_INVALID, "unknown propagation mode");
     // One launch per step.  Completion is detected by counting lanes whose
     // status is done or stopped; the count is read back every check_every
-    // launches (the only host synchronisation of the loop).
+    // launches (the only host synchronisation of the loop).  From the second
+    // round on, the check_every launches of a round are one CUDA graph
+    // (built once per call, replayed each round): one host call per round.
     if (check_every == 0) check_every = 16;
     k.persistent = 0;
     k.iters_per_launch = 1;
@@ -658,10 +704,21 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (rc) return rc;
     uint64_t n = 0;
     uint32_t fin = 0;
-    for (;;) {
+    const bool graphs = check_every > 1 && !std::getenv("HYK_PLAIN_NO_GRAPH");
+    LaunchGraph lg;
+    for (uint64_t round = 0;; ++round) {
         HYK_CU(drv().cuMemcpyDtoHAsync(&fin, (CUdeviceptr)k.finished, sizeof fin, s));
         HYK_CU(drv().cuStreamSynchronize(s));
         if ((uint64_t)fin >= lanes->n_lanes) break;
+        if (graphs && round >= 1) {
+            if (!lg.x) {
+                rc = build_graph(m, m->f_prop, grid, m->blk, m->smem, k, check_every, lg);
+                if (rc) return rc;
+            }
+            HYK_CU(drv().cuGraphLaunch(lg.x, s));
+            n += check_every;
+            continue;
+        }
         for (uint32_t c = 0; c < check_every; ++c) {
             rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
             if (rc) return rc;

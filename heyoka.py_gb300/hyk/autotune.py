@@ -1,0 +1,186 @@
+"""Kernel-configuration autotuner.
+
+The code generator can run one system in several ways: one thread per
+trajectory with the Taylor coefficients in shared memory (several block
+sizes), one thread per trajectory with the coefficients in global memory, or
+a team of 2..32 threads per trajectory.  Every configuration gives the same
+bits; they differ in speed, and which is fastest depends on the system, the
+order and the precision (the module constructor's occupancy estimate gets the
+outer-solar-system problem wrong, for instance: it prefers a team of 16 over
+the global-memory lane form, which is 1.2x faster).
+
+``tune`` measures each configuration that compiles and fits on the device on
+the same short workload (the caller's initial states, replicated to fill the
+GPU several times over, propagated for a fixed number of steps by the
+persistent kernel), keeps the fastest, and stores the choice in a JSON cache
+next to the compiled kernels (``$HYK_CACHE_DIR``, default ``~/.cache/hyk``)
+keyed by the decomposition, the order, the precision, the compensated
+summation flag and the device, so a later integrator of the same system
+starts with it.  ``taylor_adaptive_batch(..., autotune=True)`` calls it.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import threading
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .core import get_module
+from .decompose import Decomposition, order_from_tol, taylor_decompose
+
+_lock = threading.Lock()
+
+# (team_size, global_jets, block_lanes) of the configurations tried; team
+# size 0 and block size 0 let the module constructor choose.  The first entry
+# is the constructor's own choice: another configuration replaces it only
+# when it is faster by more than MARGIN (short measurements are noisy).
+MARGIN = 1.03
+DEFAULT_CANDIDATES = (
+    (0, False, 0),
+    (1, False, 0),
+    (1, False, 64),
+    (1, False, 128),
+    (1, True, 0),
+    (2, False, 0),
+    (4, False, 0),
+    (8, False, 0),
+    (16, False, 0),
+    (32, False, 0),
+)
+
+
+def cache_path():
+    d = os.environ.get("HYK_CACHE_DIR") or os.path.join(os.environ.get("HOME", "/tmp"), ".cache", "hyk")
+    return os.path.join(d, "autotune.json")
+
+
+def cache_key(dec: Decomposition, order: int, device_name: str, float32: bool, high_accuracy: bool) -> str:
+    return "{}|p{}|{}|{}|{}".format(dec.digest(), int(order), "f32" if float32 else "f64",
+                                    "ha" if high_accuracy else "plain", device_name)
+
+
+def _load_cache():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(key, entry):
+    path = cache_path()
+    with _lock:
+        data = _load_cache()
+        data[key] = entry
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".{}.tmp".format(os.getpid())
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+
+
+def lookup(dec, order, device=0, float32=False, high_accuracy=False):
+    """The cached choice for a system, or None."""
+    key = cache_key(dec, order, torch.cuda.get_device_name(device), float32, high_accuracy)
+    e = _load_cache().get(key)
+    return None if e is None else dict(e["best"])
+
+
+def _replicate(a, n):
+    if a is None:
+        return None
+    a = np.asarray(a)
+    reps = -(-n // a.shape[1])
+    return np.ascontiguousarray(np.tile(a, (1, reps))[:, :n])
+
+
+def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, device=None, steps=64,
+         lanes=None, candidates=DEFAULT_CANDIDATES, use_cache=True, verbose=False):
+    """Measure the kernel configurations of ``sys`` and return the fastest as
+    ``{"team_size": T, "global_jets": bool, "block_lanes": b}`` together with
+    the measurements (``result["trials"]``: one entry per configuration,
+    trajectory-steps/s or the reason it was skipped).
+
+    ``state`` (and ``pars``) are representative initial conditions, shape
+    (n_eq, k) (and (n_pars, k)); they are replicated to ``lanes`` trajectories
+    (default: four times the largest resident capacity of the
+    configurations) and propagated for ``steps`` steps each."""
+    from .integrator import _fp_of, taylor_adaptive_batch
+
+    np_dt, t_dt = _fp_of(fp_type)
+    f32 = t_dt == torch.float32
+    dec = sys if isinstance(sys, Decomposition) else taylor_decompose(getattr(sys, "sys", sys))
+    tol = float(np_dt(tol))
+    if tol == 0.0:
+        tol = float(np.finfo(np_dt).eps)
+    order = order_from_tol(tol)
+    dev = torch.cuda.current_device() if device is None else torch.device(device).index or 0
+    key = cache_key(dec, order, torch.cuda.get_device_name(dev), f32, high_accuracy)
+    if use_cache:
+        e = _load_cache().get(key)
+        if e is not None:
+            out = dict(e)
+            out["cached"] = True
+            return out
+    mods = []
+    trials = []
+    for T, gj, blk in candidates:
+        cfg = {"team_size": int(T), "global_jets": bool(gj), "block_lanes": int(blk)}
+        try:
+            m = get_module(dec, order, dev, block_lanes=blk, team_size=T, high_accuracy=high_accuracy,
+                           global_jets=gj, float32=f32)
+        except _lib.HykError as exc:
+            trials.append(dict(cfg, skipped=str(exc).splitlines()[0][:160]))
+            continue
+        i = m.info_dict()
+        sig = (i["team_size"], i["smem_per_lane"] == 0, i["block_lanes"])
+        if any(s == sig for s, _, _ in mods):
+            trials.append(dict(cfg, skipped="same kernel as an earlier configuration"))
+            continue
+        cap = i["n_sm"] * i["ctas_per_sm"] * max(1, i["block_lanes"] // max(1, i["team_size"]))
+        mods.append((sig, cfg, cap))
+    if not mods:
+        raise _lib.HykError("autotune: no kernel configuration of this system fits the device")
+    n = int(lanes) if lanes else min(max(c for _, _, c in mods) * 4, 1 << 20)
+    st = _replicate(np.asarray(state, dtype=np_dt), n)
+    pa = _replicate(None if pars is None else np.asarray(pars, dtype=np_dt), n)
+    best = first = None
+    for sig, cfg, cap in mods:
+        ta = taylor_adaptive_batch(dec.sys, st, pars=pa, tol=tol, fp_type=fp_type, high_accuracy=high_accuracy,
+                                   device=torch.device("cuda", dev), team_size=cfg["team_size"],
+                                   global_jets=cfg["global_jets"], block_lanes=cfg["block_lanes"])
+        s0 = ta._state.clone()
+        rate = 0.0
+        for rep in range(3):  # the first call warms up (module load, first launch)
+            ta._state.copy_(s0)
+            ta.set_time(0.0)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            ta.propagate_until(1e30, max_steps=steps)
+            torch.cuda.synchronize(dev)
+            dt = time.perf_counter() - t0
+            nst = int(ta.propagate_res_tensors["n_steps"].sum().item())
+            if rep:
+                rate = max(rate, nst / dt)
+        info = ta.module_info
+        trials.append(dict(cfg, trajectory_steps_per_s=rate, team=info["team_size"],
+                           jets="global" if info["smem_per_lane"] == 0 else "shared",
+                           block=info["block_lanes"], ctas_per_sm=info["ctas_per_sm"]))
+        if verbose:
+            print("autotune", trials[-1], flush=True)
+        if best is None or rate > best[0] * (MARGIN if best[1] is first else 1.0):
+            best = (rate, cfg)
+        if first is None:
+            first = cfg
+        del ta
+    entry = {"best": best[1], "rate": best[0], "trials": trials, "lanes": n, "steps": int(steps)}
+    if use_cache:
+        _store_cache(key, entry)
+    out = dict(entry)
+    out["cached"] = False
+    return out

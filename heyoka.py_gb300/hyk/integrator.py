@@ -197,6 +197,7 @@ class taylor_adaptive_batch:
         team_size=0,
         persist_ctas=0,
         global_jets=False,
+        autotune=False,
         **kwargs,
     ):
         llvm = {"opt_level": 3, "force_avx512": False, "slp_vectorize": False, "fast_math": False,
@@ -294,6 +295,16 @@ class taylor_adaptive_batch:
         self._order = order_from_tol(tol)
         self._dev = _dev_index(device)
         self._tdev = torch.device("cuda", self._dev)
+        self._autotune = None
+        if autotune and not pin_arith and not (self._t_events or self._nt_events):
+            # measured choice of the kernel form and block size (cached per system)
+            from .autotune import tune
+
+            r = tune(taylor_decompose(sys), st, pars=pa if np_ else None, tol=tol, fp_type=fp_type,
+                     high_accuracy=self._high_accuracy, device=torch.device("cuda", self._dev))
+            best = r["best"]
+            team_size, global_jets, block_lanes = best["team_size"], best["global_jets"], best["block_lanes"]
+            self._autotune = r
         self._mod_opts = dict(block_lanes=int(block_lanes), pin_arith=bool(pin_arith), team_size=int(team_size),
                               persist_ctas=int(persist_ctas), high_accuracy=self._high_accuracy,
                               global_jets=bool(global_jets), float32=f32)
