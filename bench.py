@@ -57,7 +57,8 @@ def parse():
                          "cr3bp-adjoint: 65536 trajectories forward plus discrete adjoint")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
-    ap.add_argument("--slice", type=int, default=64, help="serve: steps per lane per kernel launch")
+    ap.add_argument("--slice", type=int, default=1024, help="serve: the most steps per lane in one slice")
+    ap.add_argument("--quantum-ms", type=float, default=2.0, help="serve: target duration of a slice")
     ap.add_argument("--members", type=int, default=65536, help="oss, cr3bp-adjoint: trajectories")
     ap.add_argument("--autotune", action="store_true",
                     help="oss: pick the kernel configuration by measurement (hyk.autotune, cached per system)")
@@ -239,7 +240,7 @@ def run_serve(args):
 
     systems = {"pendulum": (W.pendulum_sys(), 1e-15), "kepler": (W.kepler_sys(), 1e-15), "cr3bp": (W.cr3bp_sys(), 1e-15)}
     reqs = serve_stream(args.rate, args.duration)
-    srv = serve.Server(systems, hbm_budget=4 << 30, slice_iters=args.slice)
+    srv = serve.Server(systems, hbm_budget=4 << 30, slice_iters=args.slice, quantum_ms=args.quantum_ms)
     srv.run(serve_stream(50.0, 0.2, seed=99), realtime=False)  # warm-up: compile, first launches
     for p in srv.pools.values():
         p.lane_steps = 0
@@ -252,7 +253,7 @@ def run_serve(args):
     steps = srv.trajectory_steps()
     # isolated solve time of a sample of the same requests (alone on the GPU)
     rng = np.random.default_rng(5)
-    sample = rng.choice(len(reqs), size=min(40, len(reqs)), replace=False)
+    sample = rng.choice(len(reqs), size=min(200, len(reqs)), replace=False)
     by_id = {r.rid: r for r in res}
     ratios, iso = [], []
     for i in sample:
@@ -278,7 +279,8 @@ def run_serve(args):
             "workload": "serve: Poisson {:g} req/s for {:g} s, size round(logU[1,4096]), system U{{pendulum,kepler,cr3bp}}, "
                         "horizon logU[1,1000], tol 1e-15".format(args.rate, args.duration),
             "requests": len(reqs),
-            "slice_iters": args.slice,
+            "slice_iters_max": args.slice,
+            "quantum_ms": args.quantum_ms,
             "pool_capacity": {k: p.C for k, p in srv.pools.items()},
         },
         "latency": stats,
