@@ -420,18 +420,21 @@ class Server:
                 while len(pool.inflight) < pool.depth() and pool.launch_slice():
                     progressed = True
             for pool in self.pools.values():
+                n_before = len(pool.inflight) + len(pool.gathers)
                 got = pool.poll(now)
-                if got:
-                    results.extend(got)
+                results.extend(got)
+                if got or len(pool.inflight) + len(pool.gathers) < n_before:
                     progressed = True
             if not progressed:
                 pending = [p for p in self.pools.values() if p.inflight or p.gathers]
-                if not pending and i < n:
+                if pending:
+                    _time.sleep(0.0002)
+                elif any(p.active for p in self.pools.values()):
+                    continue  # the next iteration launches their slice
+                elif i < n:
                     dt = reqs[i].arrival - now()
                     if dt > 0:
                         _time.sleep(min(dt, 0.002))
-                elif pending:
-                    _time.sleep(0.0002)
                 elif any(waiting.values()):
                     # nothing runs and the waiting requests do not fit: cannot progress
                     big = [r for q in waiting.values() for r in q][0]
