@@ -405,14 +405,23 @@ def diff(e, v):
     e, v = _ex(e), _ex(v)
     if v.kind not in (VAR, PAR):
         raise ValueError("Derivatives can be taken only with respect to variables or parameters")
+    return _deriv(e, v)
+
+
+def diff_time(e):
+    """Partial derivative of ``e`` with respect to the explicit time."""
+    return _deriv(_ex(e), time)
+
+
+def _deriv(e, v):
     memo = {}
 
     def d(n):
         if n in memo:
             return memo[n]
-        if n.kind in (VAR, PAR):
+        if n.kind in (VAR, PAR, TIME):
             r = expression(1.0) if n == v else expression(0.0)
-        elif n.kind in (NUM, TIME):
+        elif n.kind == NUM:
             r = expression(0.0)
         else:
             f, a = n.value, n.args
@@ -447,3 +456,59 @@ def diff(e, v):
         return r
 
     return d(e)
+
+
+def evaluate(e, variables, pars=None, t=None):
+    """Numerical value of ``e`` (NumPy, elementwise over lanes): ``variables``
+    maps variable names to values, ``pars`` is indexable by parameter index,
+    ``t`` is the time."""
+    import numpy as np
+
+    memo = {}
+    stack = [(_ex(e), False)]
+    while stack:
+        n, ready = stack.pop()
+        if n in memo:
+            continue
+        if n.kind == NUM:
+            memo[n] = np.float64(n.value)
+        elif n.kind == VAR:
+            memo[n] = np.asarray(variables[n.value], dtype=np.float64)
+        elif n.kind == PAR:
+            memo[n] = np.asarray(pars[n.value], dtype=np.float64)
+        elif n.kind == TIME:
+            memo[n] = np.asarray(t, dtype=np.float64)
+        elif not ready:
+            stack.append((n, True))
+            stack.extend((a, False) for a in n.args if a not in memo)
+        else:
+            a = [memo[x] for x in n.args]
+            f = n.value
+            if f == "add":
+                r = a[0] + a[1]
+            elif f == "sub":
+                r = a[0] - a[1]
+            elif f == "mul":
+                r = a[0] * a[1]
+            elif f == "div":
+                r = a[0] / a[1]
+            elif f == "neg":
+                r = -a[0]
+            elif f == "square":
+                r = a[0] * a[0]
+            elif f == "sqrt":
+                r = np.sqrt(a[0])
+            elif f == "pow":
+                r = np.power(a[0], a[1])
+            elif f == "exp":
+                r = np.exp(a[0])
+            elif f == "log":
+                r = np.log(a[0])
+            elif f == "sin":
+                r = np.sin(a[0])
+            elif f == "cos":
+                r = np.cos(a[0])
+            else:  # pragma: no cover
+                raise NotImplementedError(f)
+            memo[n] = r
+    return memo[_ex(e)]

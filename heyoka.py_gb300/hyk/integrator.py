@@ -247,18 +247,6 @@ class taylor_adaptive_batch:
         self._dec = taylor_decompose(sys, events=evs)
         if st.shape[0] == 0:
             st = np.zeros((self._dec.n_eq, B), dtype=self._np_dt)  # an empty initial state means zeros (the reference's rule)
-        if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
-            # the variational part starts from the identity (state arguments) and zero (parameters)
-            st = np.concatenate([st, self._vsys.initial_variational_state(B).astype(self._np_dt)])
-        if st.shape[0] != self._dec.n_eq:
-            raise ValueError(
-                "Inconsistent sizes detected in the initialization of an adaptive Taylor integrator: "
-                "the state vector has a dimension of {}, while the number of equations is {}".format(
-                    st.shape[0], self._dec.n_eq
-                )
-            )
-        if B == 0:
-            raise ValueError("The batch size in an adaptive Taylor integrator cannot be zero")
         np_ = self._dec.n_pars
         if pars is not None:
             pa = np.asarray(pars)
@@ -288,6 +276,23 @@ class taylor_adaptive_batch:
             ti = _to_fp_array(ti, "time", self._np_dt)
         else:
             ti = np.zeros(B, dtype=self._np_dt)
+        if self._vsys is not None and st.shape[0] == self._vsys.n_orig_sv:
+            # the variational part starts from the identity (state arguments), zero (parameters)
+            # and, for the initial time, values computed from the state, the parameters and t0
+            if self._vsys.has_time:
+                st = np.concatenate([st, self._vsys.initial_variational_state_at(
+                    st, ti, pa[: self._dec.n_pars] if self._dec.n_pars else None).astype(self._np_dt)])
+            else:
+                st = np.concatenate([st, self._vsys.initial_variational_state(B).astype(self._np_dt)])
+        if st.shape[0] != self._dec.n_eq:
+            raise ValueError(
+                "Inconsistent sizes detected in the initialization of an adaptive Taylor integrator: "
+                "the state vector has a dimension of {}, while the number of equations is {}".format(
+                    st.shape[0], self._dec.n_eq
+                )
+            )
+        if B == 0:
+            raise ValueError("The batch size in an adaptive Taylor integrator cannot be zero")
         tol = float(self._np_dt(tol))
         if tol == 0.0:
             tol = float(np.finfo(self._np_dt).eps)

@@ -15,6 +15,19 @@ derivative along argument k: D_k g = sum over the variables v of g of
 (dg/dv) (dv/da_k) + dg/da_k (a_k a parameter), with dx_l/da_k = X_{l,e_k} and
 dX_{l,beta}/da_k = X_{l,beta + e_k}.
 
+The initial time t0 is an argument like an initial condition (the right-hand
+side depends on t0 only through the state), with initial values from the
+flow's time-shift structure: x(t; t0, x0) = Psi(t - t0; x0, s0 = t0) for the
+flow Psi of the system made autonomous by the state s' = 1, so
+d/dt0 = -d/dtau + d/ds0 and, at t = t0, for k >= 1 derivatives in t0,
+beta in the state arguments and gamma in the parameters,
+
+    X_{i,alpha}(t0) = sum_{j=1..k} C(k, j) (-1)^j d_t^(k-j) d_x^beta d_p^gamma L^j(x_i),
+
+with L g = sum_l f_l dg/dx_l + dg/dt the Lie derivative along the system
+(L^j(x_i) / j! is the order-j Taylor coefficient of x_i), evaluated at
+(x0, t0, p).
+
 Layout (heyoka/_test_var_integrator.py:54-65 pins it up to order 1): the
 original state, then for each order 1, 2, ... and each component i, the
 multi-indices of that order in decreasing lexicographic order ((1,0) before
@@ -62,8 +75,6 @@ class var_ode_sys:
         pairs = [(_e._ex(l), _e._ex(r)) for l, r in sys]
         xs = [l for l, _ in pairs]
         if isinstance(args, var_args):
-            if args & var_args.time:
-                raise NotImplementedError("sensitivities with respect to the initial time are not supported")
             vargs = []
             if args & var_args.vars:
                 vargs += xs
@@ -76,13 +87,16 @@ class var_ode_sys:
                         npar = max(npar, n.value + 1)
                     stack.extend(n.args)
                 vargs += [_e.par[i] for i in range(npar)]
+            if args & var_args.time:
+                vargs.append(_e.time)
         else:
             vargs = [_e._ex(a) for a in args]
             for a in vargs:
-                if not (a.kind == _e.PAR or (a.kind == _e.VAR and a in xs)):
-                    raise ValueError("variational arguments must be state variables or parameters")
+                if not (a.kind in (_e.PAR, _e.TIME) or (a.kind == _e.VAR and a in xs)):
+                    raise ValueError("variational arguments must be state variables, parameters or the time")
         n, m = len(pairs), len(vargs)
         self.n_orig_sv = n
+        self._orig = pairs
         self.vargs = vargs
         self.order = order
         # multi-indices per order, and the variable of each (component, multi-index)
@@ -147,6 +161,67 @@ class var_ode_sys:
                     one = r == 1 and self.vargs[a.index(1)].kind == _e.VAR and self.vargs[a.index(1)] == self.sys[i][0]
                     rows.append(np.full(B, 1.0 if one else 0.0))
         return np.stack(rows) if rows else np.zeros((0, B))
+
+    @property
+    def has_time(self):
+        """Whether the initial time is among the arguments (the initial values
+        of the derivatives then depend on the state, the parameters and t0)."""
+        return any(a.kind == _e.TIME for a in self.vargs)
+
+    def initial_variational_state_at(self, x0, t0, pars=None):
+        """The initial values of the derivatives for initial conditions x0
+        (n_orig_sv, B) at times t0 (B,) with parameters pars (n_pars, B):
+        the identity for state arguments at order 1, the Lie-derivative sums
+        of the module docstring for derivatives that involve t0, zero
+        otherwise.  Shape (n_derivatives, B)."""
+        import numpy as np
+
+        x0 = np.asarray(x0, dtype=np.float64)
+        B = x0.shape[1]
+        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (B,))
+        pars = None if pars is None else np.asarray(pars, dtype=np.float64)
+        env = {x.value: x0[i] for i, (x, _) in enumerate(self._orig)}
+        base = self.initial_variational_state(B)
+        ti = [j for j, a in enumerate(self.vargs) if a.kind == _e.TIME]
+        if not ti:
+            return base
+        ti = ti[0]
+        xs = [x for x, _ in self._orig]
+        fs = [f for _, f in self._orig]
+        lie = {}  # (i, j) -> L^j(x_i)
+
+        def L(i, j):
+            if (i, j) not in lie:
+                if j == 1:
+                    lie[(i, j)] = fs[i]
+                else:
+                    g = L(i, j - 1)
+                    terms = [_e.diff(g, x) * f for x, f in zip(xs, fs)]
+                    terms.append(_e.diff_time(g))
+                    lie[(i, j)] = _e.sum(terms)
+            return lie[(i, j)]
+
+        row = 0
+        out = base.copy()
+        for r in range(1, self.order + 1):
+            for i in range(self.n_orig_sv):
+                for a in self._mi[r]:
+                    k = a[ti]
+                    if k:
+                        tot = np.zeros(B)
+                        for j in range(1, k + 1):
+                            g = L(i, j)
+                            for _ in range(k - j):
+                                g = _e.diff_time(g)
+                            for q, c in enumerate(a):
+                                if q != ti:
+                                    for _ in range(c):
+                                        g = _e.diff(g, self.vargs[q])
+                            val = _e.evaluate(g, env, pars, t0)
+                            tot = tot + math.comb(k, j) * (-1.0) ** j * np.broadcast_to(val, (B,))
+                        out[row] = tot
+                    row += 1
+        return out
 
     def _count(self, r):
         return len(self._mi[r]) if r >= 1 else 1

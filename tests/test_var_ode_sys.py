@@ -130,3 +130,76 @@ def test_order2_sensitivities_vs_finite_differences(oracle):
                 continue
             k = [q for q in range(m) if alpha[q] - (1 if q == j else 0) > 0][0]
             assert np.max(np.abs(o.state[row] - d1[comp, k])) < 1e-6, (row, mi, j)
+
+
+def _fd_t0(oracle, sys_, x0, pars, t0, t1, d):
+    """x(t1) for initial times t0 - d, t0, t0 + d (same x0), on the oracle."""
+    out = []
+    for s in (-d, 0.0, d):
+        o = oracle.Oracle(sys_, x0, pars=pars, time=np.full(x0.shape[1], t0 + s), order=20, mode=1)
+        o.propagate_until(t1)
+        out.append(o.state.copy())
+    return out
+
+
+def test_initial_time_sensitivities_vs_finite_differences(oracle):
+    """Derivatives with respect to the initial time (non-autonomous forced
+    pendulum): order 1 and 2 in t0 and the mixed t0 / x0 derivative, against
+    central differences of integrations started at shifted times."""
+    x, v = hyk.make_vars("x", "v")
+    orig = forced()
+    vs = var.var_ode_sys(orig, [v, hyk.time, x], order=2)
+    assert vs.vargs == [v, hyk.time, x] and vs.has_time
+    x0 = np.array([[0.2, -0.4], [0.3, 0.1]])
+    pars = np.array([[0.4, 0.25]])
+    t0, t1 = 0.5, 3.0
+    ic = vs.initial_variational_state_at(x0, t0, pars)
+    o = oracle.Oracle(vs.sys, np.concatenate([x0, ic]), pars=pars, time=np.full(2, t0), order=20, mode=1)
+    o.propagate_until(t1)
+    full = o.state
+    # order 1 in t0: component i, multi-index (0, 1, 0)
+    sl1 = vs.vslice(1)
+    m1 = vs._mi[1]
+    j_t = m1.index([0, 1, 0])
+    d1 = 1e-5
+    a, c, b = _fd_t0(oracle, orig, x0, pars, t0, t1, d1)
+    fd1 = (b - a) / (2 * d1)
+    for i in range(2):
+        got = full[sl1.start + i * len(m1) + j_t]
+        assert np.allclose(got, fd1[i], rtol=1e-7, atol=1e-9), (i, got, fd1[i])
+    # order 2 in t0: multi-index (0, 2, 0)
+    sl2 = vs.vslice(2)
+    m2 = vs._mi[2]
+    j_tt = m2.index([0, 2, 0])
+    d2 = 1e-3
+    a, c, b = _fd_t0(oracle, orig, x0, pars, t0, t1, d2)
+    fd2 = (b - 2 * c + a) / d2**2
+    for i in range(2):
+        got = full[sl2.start + i * len(m2) + j_tt]
+        assert np.allclose(got, fd2[i], rtol=1e-4, atol=1e-6), (i, got, fd2[i])
+    # mixed t0 / x0: multi-index (0, 1, 1) = d^2 x / dt0 dx0, from central
+    # differences in x0 of the order-1 t0 derivative
+    vs1 = var.var_ode_sys(orig, [hyk.time], order=1)
+    d3 = 1e-5
+    vals = []
+    for s in (-d3, d3):
+        xs = x0.copy()
+        xs[0] += s
+        ic1 = vs1.initial_variational_state_at(xs, t0, pars)
+        oo = oracle.Oracle(vs1.sys, np.concatenate([xs, ic1]), pars=pars, time=np.full(2, t0), order=20, mode=1)
+        oo.propagate_until(t1)
+        vals.append(oo.state[2:4].copy())
+    fd3 = (vals[1] - vals[0]) / (2 * d3)
+    j_tx = m2.index([0, 1, 1])
+    for i in range(2):
+        got = full[sl2.start + i * len(m2) + j_tx]
+        assert np.allclose(got, fd3[i], rtol=1e-6, atol=1e-8), (i, got, fd3[i])
+
+
+def test_var_args_time_order_and_errors():
+    x, v = hyk.make_vars("x", "v")
+    vs = var.var_ode_sys(forced(), var.var_args.all)
+    assert vs.vargs == [x, v, hyk.par[0], hyk.time]
+    assert var.var_args.vars | var.var_args.time | var.var_args.params == var.var_args.all
+    with pytest.raises(ValueError, match="variational arguments"):
+        var.var_ode_sys(forced(), [hyk.sin(x)])
