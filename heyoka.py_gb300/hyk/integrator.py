@@ -12,9 +12,12 @@ follow from living on a GPU:
   read-only NumPy copies, as read-only as the reference's.
 * ``batch_size`` is the number of GPU lanes: any size, not the SIMD width.
 * ``fp_type`` is ``float`` (double precision) or ``numpy.float32`` (the
-  reference's float batch integrator: float32 tensors, float kernels).  Step
-  callbacks raise ``NotImplementedError``; LLVM code-generation options are
-  accepted and ignored.  Events run on the
+  reference's float batch integrator: float32 tensors, float kernels).  LLVM
+  code-generation options are accepted and ignored.
+* Step callbacks (``callback=``: one callable, an object with ``pre_hook``, or
+  a list) run on the host after each batch step; the persistent kernel then
+  advances every lane by one step per launch, so a propagation with a
+  callback runs at one launch and one host round trip per step.  Events run on the
   device; their callbacks run on the host when the step or propagation
   returns (``hyk/events.py``).
 * ``propagate_*`` run every lane to its own final time in one persistent
@@ -117,6 +120,28 @@ def _to_fp_array(x, what, dt=np.float64):
 
 def _is_scalar(x):
     return np.ndim(x) == 0
+
+
+def _callbacks(cb):
+    """The step callbacks of a ``callback=`` argument: none, one, or a list
+    (a callback set: every one is called after each step)."""
+    if cb is None:
+        return []
+    return list(cb) if isinstance(cb, (list, tuple)) else [cb]
+
+
+def _run_callbacks(cbs, ta):
+    """Call every step callback on the integrator; False if any asks to stop
+    (reference: heyoka/step_cb_utils.cpp:65-90, the return value must be a bool)."""
+    go = True
+    for cb in cbs:
+        ret = cb(ta)
+        if not isinstance(ret, (bool, np.bool_)):
+            raise TypeError(
+                "The call operator of a step callback is expected to return a boolean, but a value of type '{}' "
+                "was returned instead".format(str(type(ret))))
+        go = go and bool(ret)
+    return go
 
 
 def _dev_index(device):
@@ -832,8 +857,11 @@ class taylor_adaptive_batch:
 
     # ------------------------------------------------------------------ propagation
     def _check_prop_args(self, max_delta_t, callback):
-        if callback is not None:
-            raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
+        for cb in _callbacks(callback):
+            if not callable(cb):
+                raise TypeError(
+                    "An object of type '{}' cannot be used as a step callback because it is not callable".format(
+                        str(type(cb))))
         if max_delta_t is None or (not _is_scalar(max_delta_t) and len(max_delta_t) == 0):
             return None
         md = self._lane_vec(max_delta_t, "max_delta_t vector")
@@ -862,9 +890,20 @@ class taylor_adaptive_batch:
         return p
 
     def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None,
-             lane_order=None):
-        """Initialise and run a propagation of every lane to (tf_hi, tf_lo)."""
+             lane_order=None, callback=None):
+        """Initialise and run a propagation of every lane to (tf_hi, tf_lo).
+
+        With step callbacks the persistent kernel runs one step per lane per
+        launch (its bookkeeping is resumable), and the callbacks are called on
+        the host after each such batch step; one returning False stops every
+        lane with the ``cb_stop`` outcome (reference:
+        heyoka/expose_batch_integrators.cpp:243-392, callback semantics in
+        heyoka/step_cb_utils.cpp:65-112)."""
         L = _lib.load()
+        cbs = _callbacks(callback)
+        for cb in cbs:
+            if hasattr(cb, "pre_hook"):
+                cb.pre_hook(self)
         if max_steps < 0:
             raise ValueError("max_steps must be non-negative")
         B, ne, order = self._B, self.dim, self._order
@@ -896,11 +935,11 @@ class taylor_adaptive_batch:
                 None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
-                0 if lane_order is None else lane_order.numel(), None, None, None, 0, 0,
+                0 if lane_order is None else lane_order.numel(), None, None, None, 0, 1 if cbs else 0,
             ))
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
-        mode = _lib.HYK_MODE_PERSISTENT if self._prop_mode == "persistent" else _lib.HYK_MODE_PLAIN
+        mode = _lib.HYK_MODE_PERSISTENT if (self._prop_mode == "persistent" or cbs) else _lib.HYK_MODE_PLAIN
         if lane_order is None and mode == _lib.HYK_MODE_PERSISTENT and self._schedule == "lpt" and B >= 4096:
             lane_order = self._lpt_order(tf_hi, tf_lo)
         with torch.cuda.device(self._dev):
@@ -917,7 +956,7 @@ class taylor_adaptive_batch:
                 )
                 if ev is not None:
                     ev[1].record(torch.cuda.current_stream(self._dev))
-                if not c_output and self._ev is None:
+                if not c_output and self._ev is None and not cbs:
                     break
                 full = (p["status"] & _lib.LANE_CAPACITY) != 0
                 grow = bool(full.any())
@@ -929,7 +968,17 @@ class taylor_adaptive_batch:
                         idx = torch.nonzero(evl).flatten().cpu().numpy()
                         ks = p["outcome"][evl].cpu().numpy()
                         resume = self._ev_terminal({int(b): -int(k) - 1 for b, k in zip(idx, ks)})
-                if not grow and not resume:
+                if cbs:
+                    # one batch step done: the callbacks, then the next step
+                    # unless every lane is finished
+                    finished = (p["status"] & (_lib.LANE_DONE | _lib.LANE_STOPPED)) != 0
+                    settled = bool((finished & ~full).all()) and not resume
+                    if not _run_callbacks(cbs, self) and not settled:
+                        p["outcome"].fill_(int(taylor_outcome.cb_stop))
+                        break
+                    if settled:
+                        break
+                elif not grow and not resume:
                     break
                 if grow and c_output and bool((p["n_iter"] >= cap).any()):
                     # Grow the coefficient store.
@@ -1037,8 +1086,8 @@ class taylor_adaptive_batch:
         (reference: heyoka/expose_batch_integrators.cpp:279-314)."""
         md = self._check_prop_args(max_delta_t, callback)
         tf = self._check_time(t, "final time vector")
-        r = self._run(tf, None, max_steps, md, write_tc=write_tc, c_output=c_output)
-        return (r.get("c_output"), None)
+        r = self._run(tf, None, max_steps, md, write_tc=write_tc, c_output=c_output, callback=callback)
+        return (r.get("c_output"), callback)
 
     def propagate_for(self, delta_t, max_steps=0, max_delta_t=[], callback=None, write_tc=False, c_output=False):  # noqa: B006
         """Propagate every lane for ``delta_t`` (scalar or per lane); final time =
@@ -1047,14 +1096,14 @@ class taylor_adaptive_batch:
         md = self._check_prop_args(max_delta_t, callback)
         dt = self._check_time(delta_t, "time interval vector")
         hi, lo = _dadd(self._thi, self._tlo, dt, torch.zeros_like(dt))
-        r = self._run(hi, lo, max_steps, md, write_tc=write_tc, c_output=c_output)
-        return (r.get("c_output"), None)
+        r = self._run(hi, lo, max_steps, md, write_tc=write_tc, c_output=c_output, callback=callback)
+        return (r.get("c_output"), callback)
 
     def propagate_grid(self, grid, max_steps=0, max_delta_t=[], callback=None):  # noqa: B006
         """Propagate over a per-lane time grid of shape ``(n, batch_size)``;
         returns ``(None, out)`` with ``out`` of shape ``(n, dim, batch_size)``
         (reference: heyoka/expose_batch_integrators.cpp:315-392)."""
-        return (None, self.propagate_grid_tensor(grid, max_steps, max_delta_t, callback).cpu().numpy())
+        return (callback, self.propagate_grid_tensor(grid, max_steps, max_delta_t, callback).cpu().numpy())
 
     def propagate_grid_tensor(self, grid, max_steps=0, max_delta_t=[], callback=None):  # noqa: B006
         """``propagate_grid`` with the output left on the device: a CUDA
@@ -1091,7 +1140,7 @@ class taylor_adaptive_batch:
             if not bool((fwd | bwd).all()):
                 raise ValueError("A non-monotonic time grid was passed to propagate_grid()")
         tf = gd[-1].contiguous()
-        r = self._run(tf, None, max_steps, md, grid=gd)
+        r = self._run(tf, None, max_steps, md, grid=gd, callback=callback)
         return r["grid_out"]
 
     # ------------------------------------------------------------------ copies

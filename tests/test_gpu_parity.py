@@ -243,8 +243,8 @@ def test_zero_duration_and_errors():
         ta.propagate_until(np.inf)
     with pytest.raises(ValueError, match="max_delta_t"):
         ta.propagate_until(1.0, max_delta_t=-1.0)
-    with pytest.raises(NotImplementedError):
-        ta.propagate_until(1.0, callback=lambda t: True)
+    with pytest.raises(TypeError, match="cannot be used as a step callback"):
+        ta.propagate_until(1.0, callback="hello world")
     with pytest.raises(ValueError, match="dimension of 1"):
         ta.propagate_grid(np.array([], dtype=float))
     with pytest.raises(ValueError, match="number of columns is 2"):
