@@ -26,7 +26,7 @@ from collections.abc import Iterable
 import numpy as np
 import torch
 
-from .integrator import taylor_adaptive_batch
+from .integrator import _callbacks, taylor_adaptive_batch
 
 
 def _host_copy(ta):
@@ -123,8 +123,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     for k in kwargs:
         if k not in allowed:
             raise TypeError("propagate_{}() got an unexpected keyword argument '{}'".format(tp, k))
-    if kwargs.get("callback") is not None:
-        raise NotImplementedError("step callbacks are not supported by the GPU batch integrator")
+    callback = kwargs.get("callback")
     if n_iter == 0:
         return []
     B = ta.batch_size
@@ -151,14 +150,11 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     big._final_tc_mask = None
     big._launch_events = None
     views = None
-    if ta.with_events:
-        # Event buffers for the whole batch (the cooldown state of every
-        # iteration's integrator carried over), and per-iteration integrators
-        # whose tensors are views of the batch's, for the callbacks: a
-        # callback gets its iteration's integrator and its lane within it,
-        # and what it writes (state, time) reaches the batch.
-        big._ev = big._ev_alloc(16)
-        big._ev["last"] = torch.cat([c._ev["last"] for c in copies], dim=-1).to(dev).contiguous()
+    if ta.with_events or callback is not None:
+        # Per-iteration integrators whose tensors are views of the batch's,
+        # for the event and step callbacks: a callback gets its iteration's
+        # integrator (and, for events, its lane within it), and what it
+        # writes (state, time) reaches the batch.
         views = []
         for i, c in enumerate(copies):
             sl = slice(i * B, (i + 1) * B)
@@ -169,9 +165,18 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             vi._thi, vi._tlo = big._thi[sl], big._tlo[sl]
             vi._ev = None
             views.append(vi)
+    if ta.with_events:
+        # Event buffers for the whole batch (the cooldown state of every
+        # iteration's integrator carried over).
+        big._ev = big._ev_alloc(16)
+        big._ev["last"] = torch.cat([c._ev["last"] for c in copies], dim=-1).to(dev).contiguous()
         big._ev_route = (views, B)
     md = kwargs.get("max_delta_t", [])
-    md = big._check_prop_args(md, None)
+    md = big._check_prop_args(md, callback)
+    # Step callbacks: a deep copy per iteration, called with its iteration's
+    # integrator (heyoka/_ensemble_impl.py:27-44).
+    cb_copies = None if callback is None else [_copy.deepcopy(callback) for _ in range(n_iter)]
+    gcb = None if callback is None else [(views[i], _callbacks(cb_copies[i])) for i in range(n_iter)]
     ms = int(kwargs.get("max_steps", 0))
     if tp == "grid":
         g = torch.tensor(np.repeat(arg.astype(ta._np_dt), n_iter * B).reshape(-1, n_iter * B), device=dev)
@@ -180,7 +185,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
                 "When invoking propagate_grid(), the first element of the time grid "
                 "must match the current time coordinate"
             )
-        res = big._run(g[-1].contiguous(), None, ms, md, grid=g, group=B)
+        res = big._run(g[-1].contiguous(), None, ms, md, grid=g, group=B, group_callbacks=gcb)
     else:
         tt = torch.full((n_iter * B,), float(ta._np_dt(arg)), dtype=ta._tdt, device=dev)
         if tp == "until":
@@ -190,7 +195,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
 
             tf_hi, tf_lo = _dadd(big._thi, big._tlo, tt, torch.zeros_like(tt))
         res = big._run(tf_hi, tf_lo, ms, md, write_tc=bool(kwargs.get("write_tc", False)),
-                       c_output=bool(kwargs.get("c_output", False)), group=B)
+                       c_output=bool(kwargs.get("c_output", False)), group=B, group_callbacks=gcb)
     big._refresh_final_tc()
     parts = {name: _split(getattr(big, name), n_iter, B) for name in ("_state", "_pars", "_thi", "_tlo", "_last_h", "_tc", "_d_out")}
     prop = {k: (None if v is None else _split(v, n_iter, B)) for k, v in big._prop.items()}
@@ -202,7 +207,9 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     for i, c in enumerate(copies):
         sl = slice(i * B, (i + 1) * B)
         ti = object.__new__(type(ta))
-        ti.__dict__.update(c.__dict__)
+        # from the callbacks' view when there is one, so that what a callback
+        # set on its integrator (attributes) is on the one returned
+        ti.__dict__.update((views[i] if views is not None else c).__dict__)
         ti._tdev = dev
         for name, v in parts.items():
             ti.__dict__[name] = v[i]
@@ -216,13 +223,14 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             for a in ("t_hi", "t_lo", "info"):
                 ti._ev[a] = big._ev[a][:, sl].contiguous()
         ti.__dict__.pop("_ev_route", None)
+        cb_i = None if cb_copies is None else cb_copies[i]
         if tp == "grid":
-            out.append((ti, None, np.ascontiguousarray(grid_np[:, :, i, :])))
+            out.append((ti, cb_i, np.ascontiguousarray(grid_np[:, :, i, :])))
         else:
             c_out = None
             if "c_output" in res:
                 c_out = res["c_output"].lanes(sl)
-            out.append((ti, c_out, None))
+            out.append((ti, c_out, cb_i))
     return out
 
 

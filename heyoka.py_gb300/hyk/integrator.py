@@ -890,7 +890,7 @@ class taylor_adaptive_batch:
         return p
 
     def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None,
-             lane_order=None, callback=None):
+             lane_order=None, callback=None, group_callbacks=None):
         """Initialise and run a propagation of every lane to (tf_hi, tf_lo).
 
         With step callbacks the persistent kernel runs one step per lane per
@@ -898,12 +898,22 @@ class taylor_adaptive_batch:
         the host after each such batch step; one returning False stops every
         lane with the ``cb_stop`` outcome (reference:
         heyoka/expose_batch_integrators.cpp:243-392, callback semantics in
-        heyoka/step_cb_utils.cpp:65-112)."""
+        heyoka/step_cb_utils.cpp:65-112).
+
+        ``group_callbacks`` (ensembles): one ``(integrator, callbacks)`` per
+        group of ``group`` lanes, called after each batch step in which the
+        group stepped; False stops that group's lanes only."""
         L = _lib.load()
         cbs = _callbacks(callback)
         for cb in cbs:
             if hasattr(cb, "pre_hook"):
                 cb.pre_hook(self)
+        gcbs = group_callbacks or []
+        for view, cl in gcbs:
+            for cb in cl:
+                if hasattr(cb, "pre_hook"):
+                    cb.pre_hook(view)
+        stepped = cbs or gcbs  # one batch step per launch
         if max_steps < 0:
             raise ValueError("max_steps must be non-negative")
         B, ne, order = self._B, self.dim, self._order
@@ -935,13 +945,18 @@ class taylor_adaptive_batch:
                 None if p["grid_idx"] is None else p["grid_idx"].data_ptr(), p["last_h"].data_ptr(),
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
-                0 if lane_order is None else lane_order.numel(), None, None, None, 0, 1 if cbs else 0,
+                0 if lane_order is None else lane_order.numel(), None, None, None, 0, 1 if stepped else 0,
             ))
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
-        mode = _lib.HYK_MODE_PERSISTENT if (self._prop_mode == "persistent" or cbs) else _lib.HYK_MODE_PLAIN
+        mode = _lib.HYK_MODE_PERSISTENT if (self._prop_mode == "persistent" or stepped) else _lib.HYK_MODE_PLAIN
         if lane_order is None and mode == _lib.HYK_MODE_PERSISTENT and self._schedule == "lpt" and B >= 4096:
             lane_order = self._lpt_order(tf_hi, tf_lo)
+        done_mask = _lib.LANE_DONE | _lib.LANE_STOPPED
+        g_open = None
+        if gcbs:
+            G = B // len(gcbs)
+            g_open = [True] * len(gcbs)  # groups with lanes left to step
         with torch.cuda.device(self._dev):
             s = stream_handle(self._dev)
             d = desc()
@@ -956,7 +971,7 @@ class taylor_adaptive_batch:
                 )
                 if ev is not None:
                     ev[1].record(torch.cuda.current_stream(self._dev))
-                if not c_output and self._ev is None and not cbs:
+                if not c_output and self._ev is None and not stepped:
                     break
                 full = (p["status"] & _lib.LANE_CAPACITY) != 0
                 grow = bool(full.any())
@@ -968,12 +983,25 @@ class taylor_adaptive_batch:
                         idx = torch.nonzero(evl).flatten().cpu().numpy()
                         ks = p["outcome"][evl].cpu().numpy()
                         resume = self._ev_terminal({int(b): -int(k) - 1 for b, k in zip(idx, ks)})
-                if cbs:
+                if stepped:
                     # one batch step done: the callbacks, then the next step
                     # unless every lane is finished
-                    finished = (p["status"] & (_lib.LANE_DONE | _lib.LANE_STOPPED)) != 0
+                    finished = (p["status"] & done_mask) != 0
                     settled = bool((finished & ~full).all()) and not resume
-                    if not _run_callbacks(cbs, self) and not settled:
+                    if gcbs:
+                        fin_g = finished.view(len(gcbs), G).all(dim=1).cpu().numpy()
+                        for g, (view, cl) in enumerate(gcbs):
+                            if not g_open[g]:
+                                continue
+                            g_open[g] = not fin_g[g]
+                            if not _run_callbacks(cl, view) and not fin_g[g]:
+                                sl = slice(g * G, (g + 1) * G)
+                                p["status"][sl] |= _lib.LANE_STOPPED
+                                p["outcome"][sl] = int(taylor_outcome.cb_stop)
+                                g_open[g] = False
+                        finished = (p["status"] & done_mask) != 0
+                        settled = bool((finished & ~full).all()) and not resume
+                    if cbs and not _run_callbacks(cbs, self) and not settled:
                         p["outcome"].fill_(int(taylor_outcome.cb_stop))
                         break
                     if settled:

@@ -129,3 +129,91 @@ def test_callback_results_and_stop():
     f = hyk.taylor_adaptive_batch(_pend(), st)
     _, out2 = f.propagate_grid(grid)
     assert np.array_equal(out, out2)
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_reference_step_callback_lists_and_angle_reducer(fp_t):
+    """heyoka/_test_batch_integrator.py test_step_callback."""
+    from hyk.callback import angle_reducer
+
+    x, v = hyk.make_vars("x", "v")
+
+    class cb_hook:
+        def __call__(_, ta):
+            return True
+
+        def pre_hook(self, ta):
+            ta.foo = True
+
+    ta = hyk.taylor_adaptive_batch([(x, v), (v, -9.8 * hyk.sin(x))],
+                                   [[fp_t(0.0), fp_t(0.01)], [fp_t(10.0), fp_t(10.01)]], fp_type=fp_t)
+    cb1, cb2 = cb_hook(), cb_hook()
+    res = ta.propagate_for(fp_t(10.0), callback=[cb1, cb2])
+    assert isinstance(res[1], list) and res[1][0] is cb1 and res[1][1] is cb2
+    assert hasattr(ta, "foo")
+    res = ta.propagate_until(fp_t(20.0), callback=[cb1, angle_reducer([x]), cb2])
+    assert isinstance(res[1][1], angle_reducer) and res[1][0] is cb1 and res[1][2] is cb2
+    st = np.asarray(ta.state)
+    assert 0 <= st[0, 0] < 6.29 and 0 <= st[0, 1] < 6.29
+    res = ta.propagate_grid([[fp_t(20.0), fp_t(20.0)], [fp_t(30.0), fp_t(30.1)]], callback=cb1)
+    assert res[0] is cb1
+    res = ta.propagate_for(fp_t(10.0), callback=angle_reducer([x]))
+    assert isinstance(res[1], angle_reducer)
+    st = np.asarray(ta.state)
+    assert 0 <= st[0, 0] < 6.29 and 0 <= st[0, 1] < 6.29
+
+
+def test_ensemble_callbacks_deep_copied():
+    """heyoka/_test_ensemble.py: the callbacks of an ensemble propagation are
+    deep copies, one per iteration, returned in the results; a callback that
+    stops its iteration stops only that iteration."""
+    from hyk.callback import angle_reducer
+
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    rng = np.random.default_rng(1)
+    ics = [np.stack([rng.uniform(-1, 1, 2), rng.uniform(-0.5, 0.5, 2)]) for _ in range(10)]
+    ta = hyk.taylor_adaptive_batch(sys_, ics[0])
+
+    class step_cb:
+        def __call__(_, ta):
+            assert id(_) != _.orig_id
+            return True
+
+    cb = step_cb()
+    cb.orig_id = id(cb)
+
+    def gen(ta, idx):
+        ta.set_time(0.0)
+        ta.state[:] = ics[idx]
+        return ta
+
+    ret = hyk.ensemble_propagate_for_batch(ta, 20.0, 10, gen, algorithm="thread", max_workers=8, callback=cb)
+    for r in ret:
+        assert isinstance(r[2], step_cb)
+    ret = hyk.ensemble_propagate_for_batch(ta, 20.0, 10, gen, callback=[cb, angle_reducer([x])])
+    for r in ret:
+        assert isinstance(r[2], list) and len(r[2]) == 2
+        assert isinstance(r[2][0], step_cb) and isinstance(r[2][1], angle_reducer)
+
+    class stopper:
+        def __init__(self):
+            self.n = 0
+
+        def __call__(self, ta):
+            self.n += 1
+            return not (ta.stop_me and self.n >= 3)
+
+    def gen2(ta, idx):
+        ta.set_time(0.0)
+        ta.state[:] = ics[idx]
+        ta.stop_me = idx == 4
+        return ta
+
+    ret = hyk.ensemble_propagate_until(ta, 20.0, 10, gen2, callback=stopper())
+    for i, r in enumerate(ret):
+        if i == 4:
+            assert all(o[0] == hyk.taylor_outcome.cb_stop for o in r[0].propagate_res) and r[2].n == 3
+        else:
+            assert all(o[0] == hyk.taylor_outcome.time_limit for o in r[0].propagate_res)
+            assert np.all(r[0].time == 20.0) and r[2].n > 3
