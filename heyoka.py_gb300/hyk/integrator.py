@@ -122,6 +122,22 @@ def _is_scalar(x):
     return np.ndim(x) == 0
 
 
+class _OwnedArray(np.ndarray):
+    """A read-only host array that keeps the integrator it was read from
+    alive, as the reference's views do (their base object is the integrator:
+    heyoka/expose_batch_integrators.cpp:394-541)."""
+
+    def __array_finalize__(self, obj):
+        self._owner = getattr(obj, "_owner", None)
+
+
+def _owned(a, owner):
+    v = np.asarray(a).view(_OwnedArray)
+    v._owner = owner
+    v.flags.writeable = False
+    return v
+
+
 def _callbacks(cb):
     """The step callbacks of a ``callback=`` argument: none, one, or a list
     (a callback set: every one is called after each step)."""
@@ -368,16 +384,11 @@ class taylor_adaptive_batch:
 
     @property
     def time(self):
-        a = self._thi.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._thi.cpu().numpy(), self)
 
     @property
     def dtime(self):
-        hi, lo = self._thi.cpu().numpy(), self._tlo.cpu().numpy()
-        hi.flags.writeable = False
-        lo.flags.writeable = False
-        return hi, lo
+        return _owned(self._thi.cpu().numpy(), self), _owned(self._tlo.cpu().numpy(), self)
 
     @property
     def order(self):
@@ -461,9 +472,7 @@ class taylor_adaptive_batch:
         """The result of the last ``eval_taylor_map`` (read-only, shape (n_orig_sv, batch_size))."""
         if self._vsys is None:
             raise ValueError("The integrator is not variational")
-        v = self._tstate_buf().view()
-        v.flags.writeable = False
-        return v
+        return _owned(self._tstate_buf(), self)
 
     def eval_taylor_map(self, inputs):
         """Evaluate the Taylor map of the variational state at the argument
@@ -534,22 +543,16 @@ class taylor_adaptive_batch:
 
     @property
     def last_h(self):
-        a = self._last_h.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._last_h.cpu().numpy(), self)
 
     @property
     def tc(self):
         self._refresh_final_tc()
-        a = self._tc.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._tc.cpu().numpy(), self)
 
     @property
     def d_output(self):
-        a = self._d_out.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._d_out.cpu().numpy(), self)
 
     @property
     def step_res(self):
