@@ -114,8 +114,14 @@ def _validate(tp, arg, n_iter, kwargs):
 
 
 def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
+    from .scalar import continuous_output, taylor_adaptive
+
+    scalar = isinstance(ta, taylor_adaptive)  # a scalar template: one lane per iteration
+    if scalar:
+        ta = ta._b
     if not isinstance(ta, taylor_adaptive_batch):
-        raise TypeError("the GPU ensemble propagation needs a hyk.taylor_adaptive_batch template integrator")
+        raise TypeError("the GPU ensemble propagation needs a hyk.taylor_adaptive or hyk.taylor_adaptive_batch "
+                        "template integrator")
     arg = _validate(tp, arg, n_iter, kwargs)
     allowed = {"max_steps", "max_delta_t", "callback", "write_tc", "c_output"}
     if tp == "grid":
@@ -128,7 +134,15 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
         return []
     B = ta.batch_size
     tmpl = _host_copy(ta)
-    copies = [gen(_clone_host(tmpl), i) for i in range(n_iter)]
+    scopies = None
+    if scalar:
+        scopies = [gen(taylor_adaptive._wrap(_clone_host(tmpl)), i) for i in range(n_iter)]
+        for sc in scopies:
+            if not isinstance(sc, taylor_adaptive):
+                raise TypeError("the ensemble generator must return the integrator it was given")
+        copies = [sc._b for sc in scopies]
+    else:
+        copies = [gen(_clone_host(tmpl), i) for i in range(n_iter)]
     for c in copies:
         if not isinstance(c, taylor_adaptive_batch) or c.batch_size != B or c._dec is not ta._dec:
             raise TypeError("the ensemble generator must return the integrator it was given")
@@ -176,7 +190,11 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     # Step callbacks: a deep copy per iteration, called with its iteration's
     # integrator (heyoka/_ensemble_impl.py:27-44).
     cb_copies = None if callback is None else [_copy.deepcopy(callback) for _ in range(n_iter)]
-    gcb = None if callback is None else [(views[i], _callbacks(cb_copies[i])) for i in range(n_iter)]
+    if scalar and views is not None:
+        for sc, vi in zip(scopies, views):
+            sc._b = vi  # the callbacks see their iteration's scalar integrator
+    gcb = None if callback is None else [((scopies[i] if scalar else views[i]), _callbacks(cb_copies[i]))
+                                         for i in range(n_iter)]
     ms = int(kwargs.get("max_steps", 0))
     if tp == "grid":
         g = torch.tensor(np.repeat(arg.astype(ta._np_dt), n_iter * B).reshape(-1, n_iter * B), device=dev)
@@ -224,7 +242,17 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
                 ti._ev[a] = big._ev[a][:, sl].contiguous()
         ti.__dict__.pop("_ev_route", None)
         cb_i = None if cb_copies is None else cb_copies[i]
-        if tp == "grid":
+        if scalar:
+            # the scalar integrator the generator returned, now on its result
+            sc = scopies[i]
+            sc._b = ti
+            r = ti.propagate_res[0]
+            if tp == "grid":
+                out.append((sc,) + tuple(r) + (cb_i, np.ascontiguousarray(grid_np[:, :, i, 0])))
+            else:
+                c_out = continuous_output(res["c_output"].lanes(sl)) if "c_output" in res else None
+                out.append((sc,) + tuple(r) + (c_out, cb_i))
+        elif tp == "grid":
             out.append((ti, cb_i, np.ascontiguousarray(grid_np[:, :, i, :])))
         else:
             c_out = None

@@ -1,0 +1,267 @@
+"""``taylor_adaptive``: the reference's scalar integrator, as one lane.
+
+The reference's scalar integrator (heyoka/taylor_expose_integrator.cpp:90-420)
+integrates one trajectory; its ensembles (``ensemble_propagate_until`` etc.
+with a scalar template, heyoka/_ensemble_impl.py:21-68) are the most common
+way to integrate many.  Here a scalar integrator is a batch integrator of one
+lane with the scalar API on top: 1-D ``state`` and ``pars`` (writable views of
+the lane), a float ``time`` and ``dtime`` that can be assigned, ``step``
+returning ``(outcome, h)``, ``propagate_until/for`` returning ``(outcome,
+min_h, max_h, n_steps, c_output, callback)`` and ``propagate_grid`` returning
+``(outcome, min_h, max_h, n_steps, callback, states)``.  Its ensembles run as
+one device batch of all the iterations' lanes (``hyk/ensemble.py``).  Events
+of the scalar integrator (``t_event``/``nt_event``) are not provided: the
+batch integrator's ``t_event_batch``/``nt_event_batch`` are.
+"""
+
+from __future__ import annotations
+
+import copy as _copy
+
+import numpy as np
+
+from .integrator import _callbacks, _fp_of, taylor_adaptive_batch, taylor_outcome
+
+
+class continuous_output:
+    """Dense output of a scalar propagation (reference:
+    heyoka/taylor_expose_c_output.cpp:21-258): ``c(t)`` gives the state at t
+    (shape (dim,)), ``c(array of n times)`` the states (shape (n, dim))."""
+
+    def __init__(self, batch_c):
+        self._c = batch_c
+
+    def __call__(self, t):
+        a = np.asarray(t)
+        if a.ndim == 0:
+            return self._c(np.full(1, float(a)))[:, 0]
+        if a.ndim != 1:
+            raise ValueError("Invalid time array passed to a continuous_output object: the number of dimensions "
+                             "must be 0 or 1, but it is {} instead".format(a.ndim))
+        return self._c(a.reshape(-1, 1))[:, :, 0]
+
+    @property
+    def output(self):
+        o = self._c.output
+        return None if o is None else o[:, 0]
+
+    @property
+    def times(self):
+        return self._c.times[:, 0]
+
+    @property
+    def tcs(self):
+        return self._c.tcs[..., 0]
+
+    @property
+    def bounds(self):
+        t = self.times
+        return (float(t[0]), float(t[-1]))
+
+    @property
+    def n_steps(self):
+        return self._c.n_steps
+
+    def __copy__(self):
+        return continuous_output(_copy.copy(self._c))
+
+    def __deepcopy__(self, memo):
+        return continuous_output(_copy.deepcopy(self._c, memo))
+
+    def __repr__(self):
+        return "Direction : {}\nTime range: {}\nN of steps: {}\n".format(
+            "forward" if self.bounds[1] >= self.bounds[0] else "backward", self.bounds, self.n_steps)
+
+
+class _ScalarCallback:
+    """A step callback of the scalar integrator, called by the one-lane batch
+    with the scalar integrator as its argument (the object itself is called:
+    no copies)."""
+
+    def __init__(self, ta, cb):
+        self._ta, self._cb = ta, cb
+
+    def __call__(self, _batch):
+        return self._cb(self._ta)
+
+    def pre_hook(self, _batch):
+        if hasattr(self._cb, "pre_hook"):
+            self._cb.pre_hook(self._ta)
+
+
+class taylor_adaptive:
+    """Adaptive Taylor integrator of one trajectory (one GPU lane)."""
+
+    def __init__(self, sys, state=[], time=0.0, pars=[], tol=0.0, high_accuracy=False,  # noqa: B006
+                 compact_mode=False, t_events=[], nt_events=[], parallel_mode=False, *, fp_type=float,  # noqa: B006
+                 **kwargs):
+        if list(t_events) or list(nt_events):
+            raise NotImplementedError("events of the scalar GPU integrator are not provided; use "
+                                      "taylor_adaptive_batch with t_event_batch / nt_event_batch")
+        np_dt, _ = _fp_of(fp_type)
+        st = np.asarray(state)
+        if st.ndim != 1:
+            raise ValueError("The state vector passed to the constructor of a scalar integrator must be "
+                             "one-dimensional, but it has {} dimensions".format(st.ndim))
+        pa = np.asarray(pars)
+        if pa.ndim != 1:
+            raise ValueError("The parameter vector passed to the constructor of a scalar integrator must be "
+                             "one-dimensional, but it has {} dimensions".format(pa.ndim))
+        self._b = taylor_adaptive_batch(
+            sys, st.reshape(-1, 1) if st.size else np.zeros((0, 1), dtype=np_dt),
+            time=np.full(1, np_dt(time)), pars=pa.reshape(-1, 1) if pa.size else None, tol=tol,
+            high_accuracy=high_accuracy, compact_mode=compact_mode, parallel_mode=parallel_mode, fp_type=fp_type,
+            **kwargs)
+
+    @classmethod
+    def _wrap(cls, batch):
+        new = object.__new__(cls)
+        new._b = batch
+        return new
+
+    # ------------------------------------------------------------ state
+    @property
+    def state(self):
+        return self._b.state[:, 0]
+
+    @property
+    def pars(self):
+        return self._b.pars[:, 0]
+
+    @property
+    def time(self):
+        return float(self._b.time[0])
+
+    @time.setter
+    def time(self, t):
+        self._b.set_time(self._b._np_dt(t))
+
+    @property
+    def dtime(self):
+        hi, lo = self._b.dtime
+        return (float(hi[0]), float(lo[0]))
+
+    @dtime.setter
+    def dtime(self, p):
+        hi, lo = p
+        self._b.set_dtime(self._b._np_dt(hi), self._b._np_dt(lo))
+
+    @property
+    def tc(self):
+        return self._b.tc[:, :, 0]
+
+    @property
+    def last_h(self):
+        return float(self._b.last_h[0])
+
+    @property
+    def d_output(self):
+        return self._b.d_output[:, 0]
+
+    @property
+    def tstate(self):
+        return self._b.tstate[:, 0]
+
+    def __getattr__(self, name):
+        # order, tol, dim, sys, decomposition, compact_mode, high_accuracy,
+        # llvm_state, is_variational, vargs, vorder, n_orig_sv, fp_type, ...
+        if name.startswith("_"):
+            raise AttributeError(name)
+        return getattr(self._b, name)
+
+    @property
+    def with_events(self):
+        return False
+
+    def get_vslice(self, order, component=None):
+        return self._b.get_vslice(order, component)
+
+    def get_mindex(self, i):
+        return self._b.get_mindex(i)
+
+    def eval_taylor_map(self, inputs):
+        a = np.asarray(inputs)
+        if a.ndim != 1:
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map must be "
+                             "one-dimensional, but it has {} dimensions".format(a.ndim))
+        return self._b.eval_taylor_map(a.reshape(-1, 1))[:, 0]
+
+    # ------------------------------------------------------------ stepping
+    def step(self, max_delta_t=None, write_tc=False):
+        if isinstance(max_delta_t, bool):
+            write_tc, max_delta_t = max_delta_t, None
+        self._b.step(None if max_delta_t is None else [max_delta_t], write_tc=write_tc)
+        oc, h = self._b.step_res[0]
+        return (oc, h)
+
+    def step_backward(self, write_tc=False):
+        self._b.step_backward(write_tc=write_tc)
+        oc, h = self._b.step_res[0]
+        return (oc, h)
+
+    def update_d_output(self, t, rel_time=False):
+        return self._b.update_d_output(self._b._np_dt(t), rel_time=rel_time)[:, 0]
+
+    # ------------------------------------------------------------ propagation
+    def _cbs(self, callback):
+        if callback is None:
+            return None
+        return [_ScalarCallback(self, cb) for cb in _callbacks(callback)]
+
+    def _res(self):
+        oc, mn, mx, ns = self._b.propagate_res[0]
+        return oc, mn, mx, ns
+
+    def propagate_until(self, t, max_steps=0, max_delta_t=np.inf, callback=None, write_tc=False, c_output=False):
+        self._b._check_prop_args(None, callback)
+        c, _ = self._b.propagate_until(self._b._np_dt(t), max_steps=max_steps, max_delta_t=_mdt(max_delta_t),
+                                       callback=self._cbs(callback), write_tc=write_tc, c_output=c_output)
+        return self._res() + (None if c is None else continuous_output(c), callback)
+
+    def propagate_for(self, delta_t, max_steps=0, max_delta_t=np.inf, callback=None, write_tc=False, c_output=False):
+        self._b._check_prop_args(None, callback)
+        c, _ = self._b.propagate_for(self._b._np_dt(delta_t), max_steps=max_steps, max_delta_t=_mdt(max_delta_t),
+                                     callback=self._cbs(callback), write_tc=write_tc, c_output=c_output)
+        return self._res() + (None if c is None else continuous_output(c), callback)
+
+    def propagate_grid(self, grid, max_steps=0, max_delta_t=np.inf, callback=None):
+        self._b._check_prop_args(None, callback)
+        g = np.asarray(grid)
+        if g.ndim != 1:
+            raise ValueError("Invalid grid passed to the propagate_grid() method of a scalar integrator: the grid "
+                             "must be one-dimensional, but it has {} dimensions".format(g.ndim))
+        _, out = self._b.propagate_grid(g.reshape(-1, 1), max_steps=max_steps, max_delta_t=_mdt(max_delta_t),
+                                        callback=self._cbs(callback))
+        return self._res() + (callback, np.ascontiguousarray(out[:, :, 0]))
+
+    # ------------------------------------------------------------ copies
+    def __copy__(self):
+        new = taylor_adaptive._wrap(_copy.copy(self._b))
+        new.__dict__.update({k: v for k, v in self.__dict__.items() if k != "_b"})
+        return new
+
+    def __deepcopy__(self, memo):
+        new = taylor_adaptive._wrap(_copy.deepcopy(self._b, memo))
+        memo[id(self)] = new
+        for k, v in self.__dict__.items():
+            if k != "_b":
+                new.__dict__[k] = _copy.deepcopy(v, memo)
+        return new
+
+    def __getstate__(self):
+        return dict(self.__dict__)
+
+    def __setstate__(self, st):
+        self.__dict__.update(st)
+
+    def __repr__(self):
+        return repr(self._b).replace("Batch size              : 1\n", "")
+
+
+def _mdt(max_delta_t):
+    """The batch integrator's max_delta_t for a scalar one (+inf: none)."""
+    v = float(max_delta_t)
+    return [] if v == np.inf else v
+
+
+__all__ = ["continuous_output", "taylor_adaptive", "taylor_outcome"]

@@ -1,0 +1,152 @@
+"""The scalar integrator ``taylor_adaptive`` (one lane) and ensembles of it:
+the reference's scalar API (heyoka/taylor_expose_integrator.cpp:90-420) and
+its ensemble tests (heyoka/_test_ensemble.py test_scalar), and the
+batch/scalar agreement of heyoka/_test_batch_integrator.py
+test_propagate_grid (bit for bit here: a lane's arithmetic does not depend
+on its batch)."""
+
+import pickle
+from copy import deepcopy
+
+import numpy as np
+import pytest
+
+import hyk
+
+pytestmark = pytest.mark.gpu
+
+
+def _sys():
+    x, v = hyk.make_vars("x", "v")
+    return [(x, v), (v, -9.8 * hyk.sin(x))]
+
+
+def test_scalar_api(oracle):
+    ta = hyk.taylor_adaptive(_sys(), [0.05, 0.025])
+    assert ta.order == 20 and ta.dim == 2 and ta.time == 0.0 and ta.state.shape == (2,)
+    oc, h = ta.step()
+    assert oc == hyk.taylor_outcome.success and h > 0
+    o = oracle.Oracle(_sys(), np.array([[0.05], [0.025]]), order=20, mode=1)
+    _, oh = o.step()
+    assert h == oh[0] and np.array_equal(np.asarray(ta.state), o.state[:, 0])
+    oc, h = ta.step(0.01)
+    assert oc == hyk.taylor_outcome.time_limit and h == 0.01
+    oc, h = ta.step_backward()
+    assert h < 0
+    ta.time = 0.0
+    ta.state[:] = [0.05, 0.025]
+    r = ta.propagate_until(20.0)
+    assert len(r) == 6 and r[0] == hyk.taylor_outcome.time_limit and r[4] is None and r[5] is None
+    assert ta.time == 20.0
+    ta.time = 0.0
+    ta.state[:] = [0.05, 0.025]
+    r = ta.propagate_for(5.0, c_output=True)
+    c = r[4]
+    assert isinstance(c, hyk.continuous_output) and c.bounds == (0.0, 5.0)
+    assert np.allclose(c(5.0), np.asarray(ta.state), rtol=1e-14, atol=1e-15)
+    assert c(np.array([1.0, 2.0, 3.0])).shape == (3, 2)
+    d = ta.update_d_output(5.0)
+    assert d.shape == (2,)
+    ta.dtime = (1.0, 0.5)
+    assert ta.dtime == (1.5, 0.0)
+    ta.time = 0.0
+    ta.state[:] = [0.05, 0.025]
+    res = ta.propagate_grid(np.linspace(0.0, 10.0, 11))
+    assert len(res) == 6 and res[4] is None and res[5].shape == (11, 2)
+    ta.foo = 1
+    t2 = deepcopy(ta)
+    assert t2.foo == 1 and np.array_equal(np.asarray(t2.state), np.asarray(ta.state))
+    t3 = pickle.loads(pickle.dumps(ta))
+    assert t3.time == ta.time and np.array_equal(np.asarray(t3.state), np.asarray(ta.state))
+
+    calls = []
+
+    def cb(ta_):
+        assert ta_ is ta
+        calls.append(ta_.time)
+        return True
+
+    ta.time = 0.0
+    r = ta.propagate_until(3.0, callback=cb)
+    assert r[5] is cb and len(calls) == r[3]
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_batch_scalar_grid_agreement(fp_t):
+    x, v = hyk.make_vars("x", "v")
+    eqns = [(x, v), (v, -9.8 * hyk.sin(x))]
+    x_ic = np.array([0.06, 0.07, 0.08, 0.09], dtype=fp_t)
+    v_ic = np.array([0.025, 0.026, 0.027, 0.028], dtype=fp_t)
+    ta = hyk.taylor_adaptive_batch(eqns, [x_ic, v_ic], fp_type=fp_t)
+    tas = [hyk.taylor_adaptive(eqns, [x0, v0], fp_type=fp_t) for x0, v0 in zip(x_ic, v_ic)]
+    grid = np.array([[-0.1, -0.2, -0.3, -0.4], [0.01, 0.02, 0.03, 0.9], [1.0, 1.1, 1.2, 1.3],
+                     [11.0, 11.1, 11.2, 11.3]], dtype=fp_t)
+    ta.propagate_until(grid[0, :])
+    bres = ta.propagate_grid(grid)
+    assert bres[0] is None
+    for i, s in enumerate(tas):
+        s.propagate_until(grid[0, i])
+        sres = s.propagate_grid(grid[:, i])
+        assert np.array_equal(sres[5], bres[1][:, :, i])
+
+
+def test_scalar_ensembles():
+    """heyoka/_test_ensemble.py test_scalar (thread algorithm)."""
+    ta = hyk.taylor_adaptive(_sys(), [0.0] * 2)
+    ics = np.array([[0.05, 0.025]] * 10)
+    for i in range(10):
+        ics[i] += i / 100.0
+
+    def gen(ta, idx):
+        ta.time = 0.0
+        ta.state[:] = ics[idx]
+        return ta
+
+    ret = hyk.ensemble_propagate_until(ta, 20.0, 10, gen, algorithm="thread", max_workers=8)
+    assert len(ret) == 10 and all(r[1] == hyk.taylor_outcome.time_limit for r in ret)
+    for i in range(10):
+        ta.time = 0.0
+        ta.state[:] = ics[i]
+        loc = ta.propagate_until(20.0)
+        assert ret[i][0].time == 20.0
+        assert np.all(np.asarray(ta.state) == np.asarray(ret[i][0].state))
+        assert loc == ret[i][1:]
+    ret = hyk.ensemble_propagate_until(ta, 20.0, 10, gen, c_output=True)
+    for i in range(10):
+        ta.time = 0.0
+        ta.state[:] = ics[i]
+        loc = ta.propagate_until(20.0, c_output=True)
+        assert loc[:-2] == ret[i][1:-2]
+        assert np.all(loc[-2](5.0) == ret[i][-2](5.0))
+
+    def gen_for(ta, idx):
+        ta.time = 10.0
+        ta.state[:] = ics[idx]
+        return ta
+
+    ret = hyk.ensemble_propagate_for(ta, 20.0, 10, gen_for)
+    for i in range(10):
+        ta.time = 10.0
+        ta.state[:] = ics[i]
+        loc = ta.propagate_for(20.0)
+        assert ret[i][0].time == 30.0 and loc == ret[i][1:]
+
+    grid = np.linspace(0.0, 20.0, 80)
+    ret = hyk.ensemble_propagate_grid(ta, grid, 10, gen)
+    for i in range(10):
+        ta.time = 0.0
+        ta.state[:] = ics[i]
+        loc = ta.propagate_grid(grid)
+        assert loc[:4] == ret[i][1:5] and np.array_equal(loc[5], ret[i][6])
+
+    class step_cb:
+        def __call__(_, ta):
+            assert id(_) != _.orig_id
+            ta.seen = True
+            return True
+
+    cb = step_cb()
+    cb.orig_id = id(cb)
+    ret = hyk.ensemble_propagate_until(ta, 20.0, 10, gen, callback=cb)
+    for r in ret:
+        assert isinstance(r[-1], step_cb) and r[0].seen
