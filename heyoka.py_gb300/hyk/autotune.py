@@ -10,9 +10,11 @@ outer-solar-system problem wrong, for instance: it prefers a team of 16 over
 the global-memory lane form, which is 1.2x faster).
 
 ``tune`` measures each configuration that compiles and fits on the device on
-the same short workload (the caller's initial states, replicated to fill the
+the same short workloads (the caller's initial states, replicated to fill the
 GPU several times over, propagated for a fixed number of steps by the
-persistent kernel), keeps the fastest, and stores the choice in a JSON cache
+persistent kernel, once without and once with a dense output grid of about
+two points per step), keeps the fastest for each, and stores the choices
+in a JSON cache
 next to the compiled kernels (``$HYK_CACHE_DIR``, default ``~/.cache/hyk``)
 keyed by the decomposition, the order, the precision, the compensated
 summation flag and the device, so a later integrator of the same system
@@ -102,8 +104,11 @@ def _replicate(a, n):
 def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, device=None, steps=64,
          lanes=None, candidates=DEFAULT_CANDIDATES, use_cache=True, verbose=False):
     """Measure the kernel configurations of ``sys`` and return the fastest as
-    ``{"team_size": T, "global_jets": bool, "block_lanes": b}`` together with
-    the measurements (``result["trials"]``: one entry per configuration,
+    ``result["best"] = {"team_size": T, "global_jets": bool, "block_lanes": b}``
+    (propagate_until / propagate_for) and ``result["best_grid"]``
+    (propagate_grid: the dense output reads every coefficient once per grid
+    point, which favours coefficients in shared memory), together with the
+    measurements (``result["trials"]``: one entry per configuration,
     trajectory-steps/s or the reason it was skipped).
 
     ``state`` (and ``pars``) are representative initial conditions, shape
@@ -149,38 +154,118 @@ def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, 
     n = int(lanes) if lanes else min(max(c for _, _, c in mods) * 4, 1 << 20)
     st = _replicate(np.asarray(state, dtype=np_dt), n)
     pa = _replicate(None if pars is None else np.asarray(pars, dtype=np_dt), n)
-    best = first = None
+    best = best_g = first = None
+    grid = None
     for sig, cfg, cap in mods:
         ta = taylor_adaptive_batch(dec.sys, st, pars=pa, tol=tol, fp_type=fp_type, high_accuracy=high_accuracy,
                                    device=torch.device("cuda", dev), team_size=cfg["team_size"],
                                    global_jets=cfg["global_jets"], block_lanes=cfg["block_lanes"])
         s0 = ta._state.clone()
-        rate = 0.0
-        for rep in range(3):  # the first call warms up (module load, first launch)
+        if grid is None:
+            # a grid of about two points per step of each lane (dense output
+            # dominates grids of many points over short propagations)
+            ta.step()
+            h = ta._last_h.abs().double().clamp(min=1e-300)
             ta._state.copy_(s0)
             ta.set_time(0.0)
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            ta.propagate_until(1e30, max_steps=steps)
-            torch.cuda.synchronize(dev)
-            dt = time.perf_counter() - t0
-            nst = int(ta.propagate_res_tensors["n_steps"].sum().item())
-            if rep:
-                rate = max(rate, nst / dt)
+            frac = torch.linspace(0.0, 1.0, 2 * steps, dtype=torch.float64, device=h.device)
+            grid = (frac.view(-1, 1) * (h * steps * 0.9).view(1, -1)).to(ta._tdt).contiguous()
+        rate = rate_g = 0.0
+        for rep in range(3):  # the first call warms up (module load, first launch)
+            for g in (None, grid):
+                ta._state.copy_(s0)
+                ta.set_time(0.0)
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                if g is None:
+                    ta.propagate_until(1e30, max_steps=steps)
+                else:
+                    ta.propagate_grid_tensor(g, max_steps=steps)
+                torch.cuda.synchronize(dev)
+                dt = time.perf_counter() - t0
+                nst = int(ta.propagate_res_tensors["n_steps"].sum().item())
+                if rep and g is None:
+                    rate = max(rate, nst / dt)
+                elif rep:
+                    rate_g = max(rate_g, nst / dt)
         info = ta.module_info
-        trials.append(dict(cfg, trajectory_steps_per_s=rate, team=info["team_size"],
-                           jets="global" if info["smem_per_lane"] == 0 else "shared",
+        trials.append(dict(cfg, trajectory_steps_per_s=rate, grid_trajectory_steps_per_s=rate_g,
+                           team=info["team_size"], jets="global" if info["smem_per_lane"] == 0 else "shared",
                            block=info["block_lanes"], ctas_per_sm=info["ctas_per_sm"]))
         if verbose:
             print("autotune", trials[-1], flush=True)
         if best is None or rate > best[0] * (MARGIN if best[1] is first else 1.0):
             best = (rate, cfg)
+        if best_g is None or rate_g > best_g[0] * (MARGIN if best_g[1] is first else 1.0):
+            best_g = (rate_g, cfg)
         if first is None:
             first = cfg
         del ta
-    entry = {"best": best[1], "rate": best[0], "trials": trials, "lanes": n, "steps": int(steps)}
+    entry = {"best": best[1], "rate": best[0], "best_grid": best_g[1], "rate_grid": best_g[0], "trials": trials,
+             "lanes": n, "steps": int(steps)}
     if use_cache:
         _store_cache(key, entry)
     out = dict(entry)
     out["cached"] = False
     return out
+
+
+def tune_call(ta, call, candidates=DEFAULT_CANDIDATES, repeats=2, apply=True, verbose=False):
+    """Measure ``call(ta)`` (a propagation of the caller's own workload) with
+    every kernel configuration of ``ta``'s system and keep the fastest.
+
+    The state, time and parameters are restored before each run and at the
+    end, so the call is timed on the same inputs each time (every
+    configuration gives the same bits).  With ``apply`` the integrator then
+    uses the fastest configuration for every call.  Returns ``{"best": cfg,
+    "seconds": s, "trials": [...]}``; unlike ``tune`` nothing is cached (the
+    measurement belongs to this workload)."""
+    st0, th0, tl0, pa0 = ta._state.clone(), ta._thi.clone(), ta._tlo.clone(), ta._pars.clone()
+    orig = (ta._mod, ta._mod_opts, ta.__dict__.get("_mod_grid"), ta.__dict__.get("_mod_grid_opts"))
+    dev = ta._dev
+
+    def restore():
+        ta._state.copy_(st0)
+        ta._thi.copy_(th0)
+        ta._tlo.copy_(tl0)
+        ta._pars.copy_(pa0)
+
+    seen, trials, best = [], [], None
+    for T, gj, blk in candidates:
+        cfg = {"team_size": int(T), "global_jets": bool(gj), "block_lanes": int(blk)}
+        opts = dict(ta._mod_opts, team_size=int(T), global_jets=bool(gj), block_lanes=int(blk))
+        try:
+            m = get_module(ta._dec, ta._order, dev, **opts)
+        except _lib.HykError as exc:
+            trials.append(dict(cfg, skipped=str(exc).splitlines()[0][:160]))
+            continue
+        i = m.info_dict()
+        sig = (i["team_size"], i["smem_per_lane"] == 0, i["block_lanes"])
+        if sig in seen:
+            trials.append(dict(cfg, skipped="same kernel as an earlier configuration"))
+            continue
+        seen.append(sig)
+        ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = m, opts, None, None
+        secs = float("inf")
+        for rep in range(repeats + 1):  # the first run warms up
+            restore()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            call(ta)
+            torch.cuda.synchronize(dev)
+            if rep:
+                secs = min(secs, time.perf_counter() - t0)
+        trials.append(dict(cfg, seconds=secs, team=i["team_size"],
+                           jets="global" if i["smem_per_lane"] == 0 else "shared", block=i["block_lanes"]))
+        if verbose:
+            print("tune_call", trials[-1], flush=True)
+        if best is None or secs < best[0]:
+            best = (secs, cfg, m, opts)
+    restore()
+    if best is None:
+        raise _lib.HykError("autotune: no kernel configuration of this system fits the device")
+    if apply:
+        ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = best[2], best[3], None, None
+    else:
+        ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = orig
+    return {"best": best[1], "seconds": best[0], "trials": trials}

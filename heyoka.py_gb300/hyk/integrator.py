@@ -355,6 +355,15 @@ class taylor_adaptive_batch:
                               persist_ctas=int(persist_ctas), high_accuracy=self._high_accuracy,
                               global_jets=bool(global_jets), float32=f32)
         self._mod = get_module(self._dec, self._order, self._dev, **self._mod_opts)
+        # propagate_grid's own measured choice, when the autotuner found a
+        # different one (its modules share the bookkeeping layout)
+        self._mod_grid_opts = None
+        self._mod_grid = None
+        bg = self._autotune.get("best_grid") if self._autotune else None
+        if bg and (bg["team_size"], bg["global_jets"], bg["block_lanes"]) != (team_size, global_jets, block_lanes):
+            self._mod_grid_opts = dict(self._mod_opts, team_size=int(bg["team_size"]),
+                                       global_jets=bool(bg["global_jets"]), block_lanes=int(bg["block_lanes"]))
+            self._mod_grid = get_module(self._dec, self._order, self._dev, **self._mod_grid_opts)
         self._prop_mode = prop_mode
         self._schedule = schedule
         self._compact_mode = bool(compact_mode)
@@ -963,13 +972,14 @@ class taylor_adaptive_batch:
         with torch.cuda.device(self._dev):
             s = stream_handle(self._dev)
             d = desc()
-            _lib.check(L.hyk_prop_init(self._mod.handle, lanes, d, s), "hyk_prop_init")
+            mod = self._mod_grid if (grid is not None and self.__dict__.get("_mod_grid") is not None) else self._mod
+            _lib.check(L.hyk_prop_init(mod.handle, lanes, d, s), "hyk_prop_init")
             ev = self._launch_events  # optional (start, end) CUDA events around the propagation launch(es)
             if ev is not None:
                 ev[0].record(torch.cuda.current_stream(self._dev))
             while True:
                 _lib.check(
-                    L.hyk_propagate(self._mod.handle, lanes, d, mode, self._mod.ws.data_ptr(), self._mod.ws_bytes, 16, None, s),
+                    L.hyk_propagate(mod.handle, lanes, d, mode, mod.ws.data_ptr(), mod.ws_bytes, 16, None, s),
                     "hyk_propagate",
                 )
                 if ev is not None:
@@ -1186,7 +1196,7 @@ class taylor_adaptive_batch:
         for k, v in self.__dict__.items():
             if isinstance(v, torch.Tensor):
                 new.__dict__[k] = v.clone()
-            elif k in ("_mod", "_dec"):
+            elif k in ("_mod", "_mod_grid", "_dec"):
                 new.__dict__[k] = v
             elif k in ("_prop",):
                 new.__dict__[k] = None if v is None else {a: (None if b is None else b.clone()) for a, b in v.items()}
@@ -1208,7 +1218,7 @@ class taylor_adaptive_batch:
     def __getstate__(self):
         d = {}
         for k, v in self.__dict__.items():
-            if k == "_mod":
+            if k in ("_mod", "_mod_grid"):
                 continue
             if isinstance(v, torch.Tensor):
                 d[k] = v.cpu()
@@ -1244,6 +1254,8 @@ class taylor_adaptive_batch:
         self._tdev = dev
         opts = self.__dict__.get("_mod_opts") or dict(high_accuracy=self.__dict__.get("_high_accuracy", False))
         self._mod = get_module(self._dec, self._order, self._dev, **opts)
+        gopts = self.__dict__.get("_mod_grid_opts")
+        self._mod_grid = None if gopts is None else get_module(self._dec, self._order, self._dev, **gopts)
 
     def __repr__(self):
         return (
