@@ -1752,7 +1752,7 @@ bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err)
 }
 
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc, bool f32) {
+                   std::string &err, bool high_acc, bool f32, bool gmem) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1775,7 +1775,8 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
     h << "// Generated by libhyk (team form, " << team << " threads per trajectory): " << d.n_eq << " equations, "
       << d.n_ops << " u-operations, order " << order << "\n";
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
-      << "\n#define HYK_TPB " << tpb << "\n#define HYK_TEAM " << team << "\n#define HYK_XS " << tg.XS
+      << "\n#define HYK_TPB " << tpb << "\n#define HYK_TEAM " << team << "\n#define HYK_GMEM " << (gmem ? 1 : 0)
+      << "\n#define HYK_XS " << tg.XS
       << "\n#define HYK_NT " << nt << "\n#define HYK_NSLOT " << tg.nslot << "\n#define HYK_PAR_SLOT " << tg.par_slot
       << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(recip(p)) << "\n#define HYK_INV_PM1 "
       << lit(recip(p - 1.0)) << "\n";

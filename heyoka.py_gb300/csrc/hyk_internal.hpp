@@ -49,7 +49,7 @@ struct TeamInfo {
 // false (with the reason) when an operation has no team-form code.
 bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err);
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc = false, bool f32 = false);
+                   std::string &err, bool high_acc = false, bool f32 = false, bool gmem = false);
 
 // Host (CPU) translation unit of the same recurrences, for checks of the
 // generator (team: the team form's recurrences, run by a team of one).

@@ -326,8 +326,14 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     const size_t smem_warps = (size_t)dv.smem_per_sm / (lane_bytes * 32 + 1024);
     m->gmem = !m->team && (lane_bytes * 32 > (size_t)dv.smem_optin || smem_warps < 4 ||
                            (m->cfg.flags & HYK_CFG_GLOBAL_JETS) != 0);
+    // Team form with its coefficient regions in global memory (on request):
+    // one region per team of a fixed resident grid, few enough to stay in L2,
+    // so more warps per SM than shared memory holds.
+    if (m->team && (m->cfg.flags & HYK_CFG_GLOBAL_JETS) != 0) m->gmem = true;
     if (m->team) {
-        // one CTA per warp by default: finest packing of the shared memory
+        // one CTA per warp by default: finest packing of the shared memory;
+        // with global-memory regions four warps per CTA
+        if (m->gmem && blk == 0) blk = 128;
     } else if (m->gmem) {
         // Two CTAs of 128 threads per SM by default: at most 255 registers a
         // thread, so both fit the register file, and eight warps hide the
@@ -373,7 +379,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     hyk::GenOut g;
     const bool high_acc = (m->cfg.flags & HYK_CFG_HIGH_ACCURACY) != 0;
     if (m->team) {
-        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32))
+        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32, m->gmem))
             return fail(HYK_ERR_INVALID, err);
     } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
                               high_acc, f32)) {
@@ -420,7 +426,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     m->compile_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 
     HYK_CU(drv().cuModuleLoadData(&m->mod, cubin.data()));
-    if (m->gmem) HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->gmem_threads * lane_bytes));
+    if (m->gmem && !m->team) HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->gmem_threads * lane_bytes));
     HYK_CU(drv().cuModuleGetFunction(&m->f_step, m->mod, "hyk_step_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_prop, m->mod, "hyk_prop_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
@@ -433,7 +439,23 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuFuncGetAttribute(&m->regs, CU_FUNC_ATTRIBUTE_NUM_REGS, m->f_prop));
     HYK_CU(drv().cuFuncGetAttribute(&m->local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, m->f_prop));
     HYK_CU(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&m->ctas_per_sm, m->f_prop, (int)blk, m->smem));
-    if (m->gmem) {
+    if (m->gmem && m->team) {
+        // CTAs per SM: the occupancy limit, at most as many as keep the
+        // teams' regions within 100 MB (of the 126 MB L2), or the caller's
+        // persist_ctas
+        const uint64_t cta_bytes = (uint64_t)(blk / m->team) * lane_bytes;
+        const int by_l2 = (int)std::max<uint64_t>(1, (100ull << 20) / (cta_bytes * (uint64_t)dv.n_sm));
+        int c = std::min(m->ctas_per_sm, by_l2);
+        if (m->cfg.persist_ctas) {
+            if ((int)m->cfg.persist_ctas > m->ctas_per_sm)
+                return fail(HYK_ERR_UNSUPPORTED, "persist_ctas exceeds the CTAs that can be resident on an SM");
+            c = (int)m->cfg.persist_ctas;
+        }
+        if (c < 1) return fail(HYK_ERR_UNSUPPORTED, "the propagation kernel cannot be resident on an SM");
+        m->ctas_per_sm = c;
+        m->gmem_threads = (uint64_t)dv.n_sm * c * blk;
+        HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)dv.n_sm * c * cta_bytes));
+    } else if (m->gmem) {
         const int want = (int)(m->gmem_threads / ((uint64_t)dv.n_sm * blk));
         if (m->ctas_per_sm < want) return fail(HYK_ERR_UNSUPPORTED, "the global-memory grid cannot be resident");
         m->ctas_per_sm = want;
@@ -821,8 +843,9 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     hyk::GenOut g;
     const bool high_acc = cfg && (cfg->flags & HYK_CFG_HIGH_ACCURACY);
     if (team > 1) {
-        if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : 32, sizeof(KParams), g, err,
-                                high_acc, f32))
+        const bool tg = (cfg->flags & HYK_CFG_GLOBAL_JETS) != 0;
+        if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : (tg ? 128 : 32), sizeof(KParams),
+                                g, err, high_acc, f32, tg))
             return fail(HYK_ERR_UNSUPPORTED, err);
     } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32)) {
         return fail(HYK_ERR_INVALID, err);

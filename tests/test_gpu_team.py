@@ -107,3 +107,34 @@ def test_team_sliced_persistent_identical():
     b.propagate_until(tf)
     assert np.array_equal(np.asarray(a.state), np.asarray(b.state))
     assert torch.equal(a.propagate_res_tensors["n_steps"], b.propagate_res_tensors["n_steps"])
+
+
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("team", [4, 16])
+def test_team_global_memory_bitwise(oracle, team, mode):
+    """Team form with the coefficient regions in global memory (one region per
+    team of a fixed resident grid): more trajectories than resident teams, so
+    the step and plain kernels loop over lanes; bit-for-bit with the oracle."""
+    st = W.kepler_ics(20000, seed=35)
+    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=1e-15, prop_mode=mode, team_size=team, global_jets=True)
+    info = ta.module_info
+    assert info["team_size"] == team and info["smem_per_lane"] == 0
+    assert info["n_sm"] * info["ctas_per_sm"] * info["block_lanes"] // team < 20000
+    o = oracle.Oracle(W.kepler_sys(), st, order=ta.order, mode=1)
+    ta.step(write_tc=True)
+    o.step()
+    assert np.array_equal(np.asarray(ta.state), o.state) and np.array_equal(ta.tc, o.tc)
+    ta.propagate_until(3.0)
+    r = o.propagate_until(3.0)
+    assert np.array_equal(np.asarray(ta.state), o.state)
+    assert np.array_equal(res_arrays(ta)["n_steps"], r["n_steps"].astype(np.int64))
+
+
+def test_team_global_memory_oss_matches_shared():
+    st, t_end = W.oss_ics(400, seed=36)
+    grid = np.linspace(0.0, 1.0, 20).reshape(-1, 1) * t_end.reshape(1, -1)
+    a = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=16)
+    b = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, team_size=16, global_jets=True)
+    _, ga = a.propagate_grid(grid)
+    _, gb = b.propagate_grid(grid)
+    assert np.array_equal(ga, gb) and torch.equal(a.state, b.state)
