@@ -24,3 +24,17 @@ def test_high_accuracy_bitwise(oracle, team):
     plain.propagate_until(30.0)
     assert not np.array_equal(np.asarray(plain.state), np.asarray(ta.state))
     assert np.max(np.abs(np.asarray(plain.state) - np.asarray(ta.state))) < 1e-11
+
+
+@pytest.mark.parametrize("team", [1, 4])
+def test_high_accuracy_float32_bitwise(oracle, team):
+    """The reference's basic test constructs float32 integrators with
+    high_accuracy=True; the compensated update in single precision matches
+    the oracle's float arithmetic bit for bit."""
+    st = W.kepler_ics(64, seed=52).astype(np.float32)
+    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, high_accuracy=True, team_size=team, fp_type=np.float32)
+    assert ta.high_accuracy and ta.order == 9
+    ta.propagate_until(10.0)
+    o = oracle.Oracle(W.kepler_sys(), st.astype(np.float64), order=ta.order, prec=2, mode=3)
+    o.propagate_until(10.0)
+    assert np.array_equal(np.asarray(ta.state).astype(np.float64), o.state)
