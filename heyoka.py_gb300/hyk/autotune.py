@@ -32,7 +32,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .core import get_module
+from .core import _cache_lock, _modules, get_module
 from .decompose import Decomposition, order_from_tol, taylor_decompose
 
 _lock = threading.Lock()
@@ -134,6 +134,7 @@ def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, 
             return out
     mods = []
     trials = []
+    m_of = {}  # id(cfg) -> its module
     for T, gj, blk in candidates:
         cfg = {"team_size": int(T), "global_jets": bool(gj), "block_lanes": int(blk)}
         try:
@@ -149,6 +150,7 @@ def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, 
             continue
         cap = i["n_sm"] * i["ctas_per_sm"] * max(1, i["block_lanes"] // max(1, i["team_size"]))
         mods.append((sig, cfg, cap))
+        m_of[id(cfg)] = m
     if not mods:
         raise _lib.HykError("autotune: no kernel configuration of this system fits the device")
     n = int(lanes) if lanes else min(max(c for _, _, c in mods) * 4, 1 << 20)
@@ -203,6 +205,7 @@ def tune(sys, state, pars=None, tol=0.0, *, fp_type=float, high_accuracy=False, 
         del ta
     entry = {"best": best[1], "rate": best[0], "best_grid": best_g[1], "rate_grid": best_g[0], "trials": trials,
              "lanes": n, "steps": int(steps)}
+    _forget_losers(dec, order, dev, [(m_of[id(best[1])]), m_of[id(best_g[1])]], [m for m in m_of.values()])
     if use_cache:
         _store_cache(key, entry)
     out = dict(entry)
@@ -230,7 +233,7 @@ def tune_call(ta, call, candidates=DEFAULT_CANDIDATES, repeats=2, apply=True, ve
         ta._tlo.copy_(tl0)
         ta._pars.copy_(pa0)
 
-    seen, trials, best = [], [], None
+    seen, trials, best, tried = [], [], None, []
     for T, gj, blk in candidates:
         cfg = {"team_size": int(T), "global_jets": bool(gj), "block_lanes": int(blk)}
         opts = dict(ta._mod_opts, team_size=int(T), global_jets=bool(gj), block_lanes=int(blk))
@@ -245,6 +248,7 @@ def tune_call(ta, call, candidates=DEFAULT_CANDIDATES, repeats=2, apply=True, ve
             trials.append(dict(cfg, skipped="same kernel as an earlier configuration"))
             continue
         seen.append(sig)
+        tried.append(m)
         ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = m, opts, None, None
         secs = float("inf")
         for rep in range(repeats + 1):  # the first run warms up
@@ -264,8 +268,21 @@ def tune_call(ta, call, candidates=DEFAULT_CANDIDATES, repeats=2, apply=True, ve
     restore()
     if best is None:
         raise _lib.HykError("autotune: no kernel configuration of this system fits the device")
+    keep = [best[2]] + ([] if apply else [orig[0]] + ([orig[2]] if orig[2] is not None else []))
+    _forget_losers(ta._dec, ta._order, dev, keep, tried)
     if apply:
         ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = best[2], best[3], None, None
     else:
         ta._mod, ta._mod_opts, ta._mod_grid, ta._mod_grid_opts = orig
     return {"best": best[1], "seconds": best[0], "trials": trials}
+
+
+def _forget_losers(dec, order, dev, keep, tried):
+    """Drop the measured modules that lost from the module cache (their device
+    buffers, up to hundreds of MB for large systems in global memory, are
+    freed once nothing uses them)."""
+    keep_ids = {id(m) for m in keep}
+    loser_ids = {id(m) for m in tried if id(m) not in keep_ids}
+    with _cache_lock:
+        for k in [k for k, m in _modules.items() if id(m) in loser_ids]:
+            del _modules[k]

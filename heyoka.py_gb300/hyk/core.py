@@ -44,6 +44,19 @@ class Module:
         if self.ws.data_ptr() % 256 != 0:  # pragma: no cover - torch allocations are 512-byte aligned
             raise _lib.HykError("workspace misaligned")
 
+    def close(self):
+        """Unload the module and free its device buffers (after its last use)."""
+        h, self.handle = getattr(self, "handle", None), None
+        if h is not None and h.value:
+            torch.cuda.synchronize(self.device)  # no launch of the module may still be running
+            _lib.load().hyk_module_destroy(h)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown: nothing left to free
+            pass
+
     @property
     def source(self) -> str:
         return _lib.load().hyk_module_source(self.handle).decode()
@@ -79,6 +92,15 @@ def get_module(dec: Decomposition, order: int, device: int, block_lanes: int = 0
                        float32)
             _modules[key] = m
         return m
+
+
+def drop_modules(keep=()):
+    """Forget the cached modules except those in ``keep``: each is unloaded
+    (and its device buffers freed) when no integrator uses it any more."""
+    keep_ids = {id(m) for m in keep}
+    with _cache_lock:
+        for k in [k for k, m in _modules.items() if id(m) not in keep_ids]:
+            del _modules[k]
 
 
 def _ptr(t):

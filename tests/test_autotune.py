@@ -74,3 +74,22 @@ def test_tune_call_on_the_callers_workload():
     ref.propagate_until(2.0)
     assert torch.equal(ta.state, ref.state) and ta.propagate_res == ref.propagate_res
     assert ta._mod_opts["team_size"] == r["best"]["team_size"]
+
+
+@pytest.mark.gpu
+def test_modules_are_freed():
+    from hyk import core
+
+    st = W.pendulum_ics(8, seed=1)
+    ta = hyk.taylor_adaptive_batch(W.pendulum_sys(), st, team_size=2)
+    m = ta._mod
+    core.drop_modules()
+    assert m.handle is not None  # still used by ta
+    ta.propagate_until(1.0)
+    del ta
+    import gc
+
+    gc.collect()
+    assert m.handle is not None  # the test's own reference keeps it
+    m.close()
+    assert m.handle is None
