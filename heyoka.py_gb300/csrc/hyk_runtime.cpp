@@ -240,12 +240,21 @@ struct hyk_module {
     size_t smem = 0;
     int regs = 0, local_bytes = 0, ctas_per_sm = 0;
     double flops = 0, compile_s = 0;
+
+    // Releases the loaded code and the coefficient buffer (also on the error
+    // paths of hyk_module_create).
+    ~hyk_module() {
+        if (!mod && !jets) return;
+        if (dv) drv().cuCtxSetCurrent(dv->ctx);
+        if (jets) drv().cuMemFree(jets);
+        if (mod) drv().cuModuleUnload(mod);
+    }
 };
 
 extern "C" {
 
 const char *hyk_last_error(void) { return g_err.c_str(); }
-const char *hyk_version(void) { return "hyk 0.1 (sm_103a, FP64 Taylor, NVRTC)"; }
+const char *hyk_version(void) { return "hyk 0.1 (sm_103a, FP64 and FP32 Taylor, NVRTC)"; }
 
 int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t *cfg, int device, hyk_module **out) {
     if (!out) return fail(HYK_ERR_INVALID, "null output pointer");
@@ -479,13 +488,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
 }
 
 int hyk_module_destroy(hyk_module *m) {
-    if (!m) return 0;
-    if (m->mod) {
-        drv().cuCtxSetCurrent(m->dv->ctx);
-        drv().cuModuleUnload(m->mod);
-    }
-    if (m->jets) drv().cuMemFree(m->jets);
-    delete m;
+    delete m;  // the destructor unloads the module and frees its buffer
     return 0;
 }
 
