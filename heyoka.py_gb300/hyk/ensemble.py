@@ -193,6 +193,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     if scalar and views is not None:
         for sc, vi in zip(scopies, views):
             sc._b = vi  # the callbacks see their iteration's scalar integrator
+            vi._scalar = sc
     gcb = None if callback is None else [((scopies[i] if scalar else views[i]), _callbacks(cb_copies[i]))
                                          for i in range(n_iter)]
     ms = int(kwargs.get("max_steps", 0))
@@ -246,6 +247,7 @@ def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
             # the scalar integrator the generator returned, now on its result
             sc = scopies[i]
             sc._b = ti
+            ti._scalar = sc
             r = ti.propagate_res[0]
             if tp == "grid":
                 out.append((sc,) + tuple(r) + (cb_i, np.ascontiguousarray(grid_np[:, :, i, 0])))

@@ -31,7 +31,7 @@ import numpy as np
 
 from . import expr as _e
 
-__all__ = ["event_direction", "nt_event_batch", "t_event_batch"]
+__all__ = ["event_direction", "nt_event", "nt_event_batch", "t_event", "t_event_batch"]
 
 
 class event_direction(enum.IntEnum):
@@ -153,6 +153,72 @@ class t_event_batch(_EventBase):
                 "auto" if self._cooldown < 0 else repr(self._cooldown),
             )
         )
+
+
+class nt_event(_EventBase):
+    """Non-terminal event of the scalar integrator: ``callback(ta, t, d_sgn)``
+    at every root of ``ex`` (reference: heyoka/taylor_expose_events.cpp:202-250)."""
+
+    def __init__(self, ex, callback, direction=event_direction.any, fp_type=float):
+        super().__init__(ex, direction, fp_type)
+        _check_cb(callback)
+        self._cb = _copy.deepcopy(callback)
+
+    __repr__ = nt_event_batch.__repr__
+
+
+class t_event(_EventBase):
+    """Terminal event of the scalar integrator: the step ends at the first
+    root of ``ex``; optional ``callback(ta, d_sgn) -> bool`` (True resumes the
+    propagation) (reference: heyoka/taylor_expose_events.cpp:252-311)."""
+
+    def __init__(self, ex, callback=None, direction=event_direction.any, cooldown=-1.0, fp_type=float):
+        super().__init__(ex, direction, fp_type)
+        if callback is not None:
+            _check_cb(callback)
+        self._cb = None if callback is None else _copy.deepcopy(callback)
+        self._cooldown = float(cooldown)
+
+    cooldown = t_event_batch.cooldown
+    __repr__ = t_event_batch.__repr__
+
+
+class _ScalarNt:
+    """A scalar event's non-terminal callback under the one-lane batch: the
+    lane index is dropped."""
+
+    def __init__(self, cb):
+        self.cb = cb
+
+    def __call__(self, ta, t, d_sgn, bidx):
+        self.cb(ta, t, d_sgn)
+
+
+class _ScalarT:
+    """A scalar event's terminal callback under the one-lane batch."""
+
+    def __init__(self, cb):
+        self.cb = cb
+
+    def __call__(self, ta, d_sgn, bidx):
+        return self.cb(ta, d_sgn)
+
+
+def batch_events_of_scalar(t_events, nt_events, fp_type):
+    """The batch events that carry the scalar events (the callback objects
+    are shared, not copied: the scalar events already hold their copies)."""
+    tb, nb = [], []
+    for e in t_events:
+        be = object.__new__(t_event_batch)
+        be.__dict__.update(e.__dict__)
+        be._cb = None if e._cb is None else _ScalarT(e._cb)
+        tb.append(be)
+    for e in nt_events:
+        be = object.__new__(nt_event_batch)
+        be.__dict__.update(e.__dict__)
+        be._cb = _ScalarNt(e._cb)
+        nb.append(be)
+    return tb, nb
 
 
 class _BoundEvent:

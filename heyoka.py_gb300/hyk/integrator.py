@@ -676,13 +676,20 @@ class taylor_adaptive_batch:
         return d
 
     def _ev_target(self, b):
-        """The integrator and lane a callback for batch lane b is given: this
-        one, or in an ensemble's combined batch the lane's iteration."""
+        """The integrator and lane of batch lane b: this one, or in an
+        ensemble's combined batch the lane's iteration.  Its callbacks are
+        given ``_ev_arg`` of it."""
         route = self.__dict__.get("_ev_route")
         if route is None:
             return self, b
         views, B = route
         return views[b // B], b % B
+
+    @staticmethod
+    def _ev_arg(tgt):
+        """The integrator an event callback is given: the scalar integrator a
+        one-lane batch stands for, when there is one."""
+        return tgt.__dict__.get("_scalar") or tgt
 
     def _ev_dispatch_nt(self):
         """Run the non-terminal callbacks for the recorded roots, in
@@ -708,7 +715,7 @@ class taylor_adaptive_batch:
                 k, sg = int(inf[r]) >> 2, (int(inf[r]) & 3) - 1
                 cb = tgt._nt_events[k].callback
                 try:
-                    cb(tgt, float(th[r]), sg, lb)
+                    cb(self._ev_arg(tgt), float(th[r]), sg, lb)
                 except Exception as exc:  # noqa: BLE001 - re-raised as the reference does
                     raise callback_error(exc) from exc
 
@@ -728,7 +735,7 @@ class taylor_adaptive_batch:
             if cb is None:
                 continue
             try:
-                ret = cb(tgt, int(sg[b]), lb)
+                ret = cb(self._ev_arg(tgt), int(sg[b]), lb)
             except Exception as exc:  # noqa: BLE001
                 raise callback_error(exc) from exc
             if check_bool_retval(ret):

@@ -9,9 +9,9 @@ the lane), a float ``time`` and ``dtime`` that can be assigned, ``step``
 returning ``(outcome, h)``, ``propagate_until/for`` returning ``(outcome,
 min_h, max_h, n_steps, c_output, callback)`` and ``propagate_grid`` returning
 ``(outcome, min_h, max_h, n_steps, callback, states)``.  Its ensembles run as
-one device batch of all the iterations' lanes (``hyk/ensemble.py``).  Events
-of the scalar integrator (``t_event``/``nt_event``) are not provided: the
-batch integrator's ``t_event_batch``/``nt_event_batch`` are.
+one device batch of all the iterations' lanes (``hyk/ensemble.py``).  Its
+events (``t_event``/``nt_event``, callbacks without the lane index) run as the
+one-lane batch's events, their callbacks called with the scalar integrator.
 """
 
 from __future__ import annotations
@@ -95,9 +95,16 @@ class taylor_adaptive:
     def __init__(self, sys, state=[], time=0.0, pars=[], tol=0.0, high_accuracy=False,  # noqa: B006
                  compact_mode=False, t_events=[], nt_events=[], parallel_mode=False, *, fp_type=float,  # noqa: B006
                  **kwargs):
-        if list(t_events) or list(nt_events):
-            raise NotImplementedError("events of the scalar GPU integrator are not provided; use "
-                                      "taylor_adaptive_batch with t_event_batch / nt_event_batch")
+        from .events import batch_events_of_scalar, nt_event, t_event
+
+        t_events, nt_events = list(t_events), list(nt_events)
+        for e in t_events:
+            if not isinstance(e, t_event):
+                raise TypeError("the t_events argument must be a list of t_event objects")
+        for e in nt_events:
+            if not isinstance(e, nt_event):
+                raise TypeError("the nt_events argument must be a list of nt_event objects")
+        tb, nb = batch_events_of_scalar(t_events, nt_events, fp_type)
         np_dt, _ = _fp_of(fp_type)
         st = np.asarray(state)
         if st.ndim != 1:
@@ -110,13 +117,15 @@ class taylor_adaptive:
         self._b = taylor_adaptive_batch(
             sys, st.reshape(-1, 1) if st.size else np.zeros((0, 1), dtype=np_dt),
             time=np.full(1, np_dt(time)), pars=pa.reshape(-1, 1) if pa.size else None, tol=tol,
-            high_accuracy=high_accuracy, compact_mode=compact_mode, parallel_mode=parallel_mode, fp_type=fp_type,
-            **kwargs)
+            high_accuracy=high_accuracy, compact_mode=compact_mode, t_events=tb, nt_events=nb,
+            parallel_mode=parallel_mode, fp_type=fp_type, **kwargs)
+        self._b._scalar = self  # event callbacks are given the scalar integrator
 
     @classmethod
     def _wrap(cls, batch):
         new = object.__new__(cls)
         new._b = batch
+        batch._scalar = new
         return new
 
     # ------------------------------------------------------------ state
@@ -171,7 +180,38 @@ class taylor_adaptive:
 
     @property
     def with_events(self):
-        return False
+        return self._b.with_events
+
+    @property
+    def t_events(self):
+        from .events import _BoundEvent, t_event
+
+        out = []
+        for be in self._b._t_events:
+            e = object.__new__(t_event)
+            e.__dict__.update(be.__dict__)
+            e._cb = None if be._cb is None else be._cb.cb
+            out.append(_BoundEvent(self, e))
+        return out
+
+    @property
+    def nt_events(self):
+        from .events import _BoundEvent, nt_event
+
+        out = []
+        for be in self._b._nt_events:
+            e = object.__new__(nt_event)
+            e.__dict__.update(be.__dict__)
+            e._cb = be._cb.cb
+            out.append(_BoundEvent(self, e))
+        return out
+
+    @property
+    def te_cooldowns(self):
+        return self._b.te_cooldowns[0]
+
+    def reset_cooldowns(self):
+        self._b.reset_cooldowns()
 
     def get_vslice(self, order, component=None):
         return self._b.get_vslice(order, component)
@@ -241,8 +281,10 @@ class taylor_adaptive:
         return new
 
     def __deepcopy__(self, memo):
-        new = taylor_adaptive._wrap(_copy.deepcopy(self._b, memo))
+        new = object.__new__(taylor_adaptive)
         memo[id(self)] = new
+        new._b = _copy.deepcopy(self._b, memo)
+        new._b._scalar = new
         for k, v in self.__dict__.items():
             if k != "_b":
                 new.__dict__[k] = _copy.deepcopy(v, memo)
@@ -253,6 +295,7 @@ class taylor_adaptive:
 
     def __setstate__(self, st):
         self.__dict__.update(st)
+        self._b._scalar = self
 
     def __repr__(self):
         return repr(self._b).replace("Batch size              : 1\n", "")

@@ -150,3 +150,80 @@ def test_scalar_ensembles():
     ret = hyk.ensemble_propagate_until(ta, 20.0, 10, gen, callback=cb)
     for r in ret:
         assert isinstance(r[-1], step_cb) and r[0].seen
+
+
+def test_scalar_events():
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    roots = []
+
+    def cb(ta, t, d_sgn):
+        assert isinstance(ta, hyk.taylor_adaptive)
+        roots.append((t, d_sgn))
+
+    ta = hyk.taylor_adaptive(sys_, [0.05, 0.025], nt_events=[hyk.nt_event(v, cb)])
+    assert ta.with_events and len(ta.nt_events) == 1
+    assert id(ta.nt_events[0].callback) == id(ta.nt_events[0].callback)
+    r = ta.propagate_until(10.0)
+    assert r[0] == hyk.taylor_outcome.time_limit
+    # the same roots as the batch integrator's (one lane)
+    broots = []
+    tb = hyk.taylor_adaptive_batch(sys_, [[0.05], [0.025]],
+                                   nt_events=[hyk.nt_event_batch(v, lambda ta, t, d, b: broots.append((t, d)))])
+    tb.propagate_until(10.0)
+    assert roots == broots and len(roots) > 5
+    # the callback objects belong to the integrator: a deep copy has its own
+    # (functions deep-copy to themselves; a callable object does not)
+
+    class cbk:
+        def __call__(self, ta, t, d_sgn):
+            pass
+
+    ta3 = hyk.taylor_adaptive(sys_, [0.05, 0.025], nt_events=[hyk.nt_event(v, cbk())])
+    t2 = deepcopy(ta3)
+    assert id(t2.nt_events[0].callback) != id(ta3.nt_events[0].callback)
+
+    class stop:
+        def __init__(self):
+            self.n = 0
+
+        def __call__(self, ta, d_sgn):
+            self.n += 1
+            return False
+
+    ta = hyk.taylor_adaptive(sys_, [0.05, 0.025], t_events=[hyk.t_event(v, callback=stop(),
+                                                                          direction=hyk.event_direction.negative)])
+    r = ta.propagate_until(10.0)
+    assert int(r[0]) == -1 and ta.time < 10.0
+    assert ta.t_events[0].callback.n == 1
+    assert ta.te_cooldowns[0] is not None
+    ta.reset_cooldowns()
+    assert ta.te_cooldowns[0] is None
+    oc, h = ta.step()
+    assert oc == hyk.taylor_outcome.success or int(oc) >= 0
+
+
+def test_scalar_ensemble_with_events():
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+
+    class counter:
+        def __init__(self):
+            self.n = 0
+
+        def __call__(self, ta, t, d_sgn):
+            assert isinstance(ta, hyk.taylor_adaptive)
+            self.n += 1
+            ta.seen = True
+
+    ta = hyk.taylor_adaptive(sys_, [0.05, 0.025], nt_events=[hyk.nt_event(v, counter())])
+
+    def gen(ta, i):
+        ta.time = 0.0
+        ta.state[:] = [0.05 + 0.01 * i, 0.025]
+        return ta
+
+    ret = hyk.ensemble_propagate_until(ta, 10.0, 6, gen)
+    for r in ret:
+        assert r[1] == hyk.taylor_outcome.time_limit
+        assert r[0].nt_events[0].callback.n > 5 and r[0].seen
