@@ -227,3 +227,45 @@ def test_scalar_ensemble_with_events():
     for r in ret:
         assert r[1] == hyk.taylor_outcome.time_limit
         assert r[0].nt_events[0].callback.n > 5 and r[0].seen
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_reference_scalar_nt_event_pattern(fp_t):
+    """heyoka/test.py event_detection_test_case.test_scalar, non-terminal
+    part: two events (v^2 - delta, v) on the pendulum, their roots in the
+    order (v^2 - delta, v, v^2 - delta) around each turning point, twelve up
+    to t = 4, each callback given the integrator itself."""
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    small = 1e-6 if fp_t == np.float32 else 1e-10
+    state = {"n": 0, "t": fp_t(0), "id": None}
+
+    def cb0(ta, t, d_sgn):
+        assert t > state["t"] and state["n"] % 3 in (0, 2) and id(ta) == state["id"]
+        state["n"] += 1
+        state["t"] = t
+
+    def cb1(ta, t, d_sgn):
+        assert t > state["t"] and state["n"] % 3 == 1 and id(ta) == state["id"]
+        state["n"] += 1
+        state["t"] = t
+
+    ta = hyk.taylor_adaptive(sys_, [fp_t(0), fp_t(0.25)], fp_type=fp_t,
+                             nt_events=[hyk.nt_event(v * v - small, cb0, fp_type=fp_t),
+                                        hyk.nt_event(v, cb1, fp_type=fp_t)])
+    state["id"] = id(ta)
+    assert ta.propagate_until(fp_t(4))[0] == hyk.taylor_outcome.time_limit
+    assert state["n"] == 12
+
+
+def test_reference_gil_bug_construction_error():
+    """heyoka/test.py test_gil_bug: a failing construction with events raises
+    ValueError cleanly."""
+    x, v = hyk.make_vars("x", "v")
+
+    class cb0:
+        def __call__(self, ta, t, d_sgn):
+            pass
+
+    with pytest.raises(ValueError):
+        hyk.taylor_adaptive([(x, v), (v, -9.8 * hyk.sin(x))], [0.0], nt_events=[hyk.nt_event(x, cb0())])
