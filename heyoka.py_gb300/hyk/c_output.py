@@ -37,8 +37,26 @@ def _dsub_hi(ah, bh, bl):
     return s + e
 
 
+_DEFAULT_MSG = "Cannot use a default-constructed continuous_output_batch object"
+
+
+class _DenseOutputState:
+    """What ``llvm_state`` reports for a continuous output: the evaluator is
+    libhyk's dense-output kernel, not JIT-compiled code."""
+
+    ir = "hyk_dense_eval: Horner evaluation of the stored Taylor coefficients (CUDA, sm_103a)"
+
+    def __repr__(self):
+        return self.ir
+
+
 class continuous_output_batch:
-    def __init__(self, tcs, t_hi, t_lo, order, n_iter=None):
+    def __init__(self, tcs=None, t_hi=None, t_lo=None, order=0, n_iter=None):
+        if tcs is None:
+            # a default-constructed object (reference: usable only after a propagation fills one)
+            self._tcs = self._thi = self._tlo = None
+            self._order, self._B, self._dim, self._out, self._nit = 0, 0, 0, None, None
+            return
         self._tcs = tcs.contiguous()
         self._thi = t_hi.contiguous()
         self._tlo = t_lo.contiguous()
@@ -55,8 +73,17 @@ class continuous_output_batch:
             self._sgn = torch.where(self._thi[-1] < self._thi[0], -1.0, 1.0).to(tcs.dtype)
             self._keys = (self._thi[:n] * self._sgn).t().contiguous()  # (B, n)
 
+    def _check(self):
+        if self._tcs is None:
+            raise ValueError(_DEFAULT_MSG)
+
+    @property
+    def llvm_state(self):
+        return _DenseOutputState()
+
     @property
     def n_steps(self):
+        self._check()
         return int(self._tcs.shape[0])
 
     @property
@@ -65,12 +92,16 @@ class continuous_output_batch:
 
     @property
     def tcs(self):
+        if self._tcs is None:
+            return None
         a = self._tcs.cpu().numpy()
         a.flags.writeable = False
         return a
 
     @property
     def times(self):
+        if self._thi is None:
+            return None
         a = self._thi.cpu().numpy()
         a.flags.writeable = False
         return a
@@ -85,6 +116,7 @@ class continuous_output_batch:
 
     @property
     def bounds(self):
+        self._check()
         t = self._thi.cpu().numpy()
         return (np.array(t[0]), np.array(t[-1]))
 
@@ -108,9 +140,11 @@ class continuous_output_batch:
             )
         return out
 
-    def __call__(self, tm):
-        if self.n_steps == 0:
-            raise ValueError("Cannot use a default-constructed continuous_output_batch object")
+    def __call__(self, tm=None, time=None):
+        if tm is None:
+            tm = time
+        if self._tcs is None or self.n_steps == 0:
+            raise ValueError(_DEFAULT_MSG)
         dt = self._tcs.dtype
         ndt = np.float32 if dt == torch.float32 else np.float64
         if isinstance(tm, torch.Tensor):
@@ -162,12 +196,21 @@ class continuous_output_batch:
         )
 
     def __copy__(self):
+        if self._tcs is None:
+            return continuous_output_batch()
         return continuous_output_batch(self._tcs.clone(), self._thi.clone(), self._tlo.clone(), self._order)
 
     def __deepcopy__(self, memo):
         return self.__copy__()
 
     def __repr__(self):
+        if self._tcs is None:
+            return "Default-constructed continuous_output_batch"
         return "Directions : {}\nNumber of steps: {}\nBatch size: {}\n".format(
             "forward/backward per lane", self.n_steps, self._B
         )
+
+
+# The reference's per-precision class names (the class here serves both).
+continuous_output_batch_dbl = continuous_output_batch
+continuous_output_batch_flt = continuous_output_batch

@@ -28,11 +28,22 @@ class continuous_output:
     heyoka/taylor_expose_c_output.cpp:21-258): ``c(t)`` gives the state at t
     (shape (dim,)), ``c(array of n times)`` the states (shape (n, dim))."""
 
-    def __init__(self, batch_c):
-        self._c = batch_c
+    def __init__(self, batch_c=None):
+        from .c_output import continuous_output_batch
 
-    def __call__(self, t):
-        a = np.asarray(t)
+        self._c = continuous_output_batch() if batch_c is None else batch_c
+
+    def _check(self):
+        if self._c._tcs is None:
+            raise ValueError("Cannot use a default-constructed continuous_output object")
+
+    @property
+    def llvm_state(self):
+        return self._c.llvm_state
+
+    def __call__(self, t=None, time=None):
+        self._check()
+        a = np.asarray(t if t is not None else time)
         if a.ndim == 0:
             return self._c(np.full(1, float(a)))[:, 0]
         if a.ndim != 1:
@@ -47,19 +58,23 @@ class continuous_output:
 
     @property
     def times(self):
-        return self._c.times[:, 0]
+        t = self._c.times
+        return None if t is None else t[:, 0]
 
     @property
     def tcs(self):
-        return self._c.tcs[..., 0]
+        t = self._c.tcs
+        return None if t is None else t[..., 0]
 
     @property
     def bounds(self):
+        self._check()
         t = self.times
         return (float(t[0]), float(t[-1]))
 
     @property
     def n_steps(self):
+        self._check()
         return self._c.n_steps
 
     def __copy__(self):
@@ -69,6 +84,8 @@ class continuous_output:
         return continuous_output(_copy.deepcopy(self._c, memo))
 
     def __repr__(self):
+        if self._c._tcs is None:
+            return "Default-constructed continuous_output"
         return "Direction : {}\nTime range: {}\nN of steps: {}\n".format(
             "forward" if self.bounds[1] >= self.bounds[0] else "backward", self.bounds, self.n_steps)
 

@@ -82,3 +82,31 @@ def test_models():
     xx, px, y = hyk.make_vars("x", "px", "y")
     assert dyn[0][0] == xx and dyn[0][1] == px + y
     assert len(D.taylor_decompose(model.nbody(6)).ops) > 100
+
+
+def test_default_constructed_continuous_outputs():
+    """heyoka/test.py c_output_test_case: default-constructed continuous
+    outputs (no device needed)."""
+    import pickle
+    from copy import copy, deepcopy
+
+    import numpy as np
+
+    import hyk
+
+    for c in (hyk.continuous_output_batch_dbl(), hyk.continuous_output_batch_flt()):
+        for obj in (c, copy(c), deepcopy(c), pickle.loads(pickle.dumps(c))):
+            with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output_batch object"):
+                obj(np.zeros((0,)))
+            with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output_batch object"):
+                obj(time=[0.0, 0.0])
+            assert obj.output is None and obj.times is None and obj.tcs is None
+            with pytest.raises(ValueError, match="default-constructed"):
+                obj.bounds
+            with pytest.raises(ValueError, match="default-constructed"):
+                obj.n_steps
+            assert obj.batch_size == 0 and "forward" not in repr(obj) and obj.llvm_state.ir != ""
+    s = hyk.continuous_output()
+    with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output object"):
+        s(1.0)
+    assert s.times is None and s.tcs is None and "forward" not in repr(s)
