@@ -22,6 +22,7 @@ import torch
 
 from . import _lib
 from .core import stream_handle
+from .integrator import _owned
 
 
 def _two_sum(a, b):
@@ -94,25 +95,19 @@ class continuous_output_batch:
     def tcs(self):
         if self._tcs is None:
             return None
-        a = self._tcs.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._tcs.cpu().numpy(), self)
 
     @property
     def times(self):
         if self._thi is None:
             return None
-        a = self._thi.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._thi.cpu().numpy(), self)
 
     @property
     def output(self):
         if self._out is None:
             return None
-        a = self._out.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(self._out.cpu().numpy(), self)
 
     @property
     def bounds(self):
@@ -179,9 +174,7 @@ class continuous_output_batch:
         if rows:
             self._out = rows[-1]
         res = torch.stack(rows) if rows else torch.empty((0, self._dim, self._B), dtype=dt)
-        a = res.cpu().numpy()
-        a.flags.writeable = False
-        return a
+        return _owned(res.cpu().numpy(), self)
 
     def lanes(self, sl):
         """The continuous output of a contiguous subset of lanes (one batch of

@@ -269,3 +269,59 @@ def test_reference_gil_bug_construction_error():
 
     with pytest.raises(ValueError):
         hyk.taylor_adaptive([(x, v), (v, -9.8 * hyk.sin(x))], [0.0], nt_events=[hyk.nt_event(x, cb0())])
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_reference_c_output_batch_behaviour(fp_t):
+    """heyoka/test.py c_output_test_case.test_batch, functional part."""
+    from sys import getrefcount
+
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    ic = np.array([[0.0, 0.01, 0.02, 0.03], [0.25, 0.26, 0.27, 0.28]], dtype=fp_t)
+    ta = hyk.taylor_adaptive_batch(sys_, ic, fp_type=fp_t)
+    scal = [hyk.taylor_adaptive(sys_, ic[:, i], fp_type=fp_t) for i in range(4)]
+    final_tm = np.array([10.0, 10.4, 10.5, 11.0], dtype=fp_t)
+    check_tm = np.array([0.1, 1.3, 5.6, 9.1], dtype=fp_t)
+    c_out, cb = ta.propagate_until(final_tm)
+    assert cb is None and c_out is None
+    ta.state[:] = ic
+    ta.set_time(fp_t(0))
+    c_out, cb = ta.propagate_until(final_tm, c_output=True)
+    assert cb is None and c_out is not None
+    assert c_out(check_tm).shape == (2, 4)
+    with pytest.raises(ValueError):
+        c_out(check_tm)[0] = 0.5
+    rc = getrefcount(c_out)
+    tmp = c_out(check_tm)  # noqa: F841
+    assert getrefcount(c_out) == rc + 1
+    with pytest.raises(ValueError, match="the number of dimensions must be 1 or 2, but it is 3 instead"):
+        c_out(np.zeros((1, 1, 1), dtype=fp_t))
+    for n in (1, 0, 5):
+        with pytest.raises(ValueError, match="the length must be 4 but it is {} instead".format(n)):
+            c_out(np.zeros((n,), dtype=fp_t))
+    eps = np.finfo(fp_t).eps * 10
+    c_scal = [s.propagate_until(final_tm[i], c_output=True)[4] for i, s in enumerate(scal)]
+    c_out(check_tm)
+    for i in range(4):
+        c_scal[i](check_tm[i])
+        assert np.allclose(c_scal[i].output, c_out.output[:, i], rtol=eps, atol=eps)
+    scal_res = c_out(fp_t(0.42)).copy()
+    assert np.all(scal_res == c_out([fp_t(0.42)] * 4))
+    nc = np.vstack([check_tm, np.zeros((4,), dtype=fp_t)]).T.flatten()[::2]
+    c_out(nc)
+    for i in range(4):
+        assert np.allclose(c_scal[i].output, c_out.output[:, i], rtol=eps, atol=eps)
+    with pytest.raises(ValueError, match="the number of columns must be 4 but it is 3 instead"):
+        c_out(np.zeros((5, 3), dtype=fp_t))
+    b = np.repeat(check_tm, 5, axis=0).reshape((4, 5)).T
+    out_b = c_out(b)
+    assert out_b.shape == (5, 2, 4)
+    assert c_out(np.zeros((0, 4), dtype=fp_t)).shape == (0, 2, 4)
+    assert c_out.times.shape == (c_out.n_steps + 1, 4) and np.all(np.isfinite(c_out.times))
+    with pytest.raises(ValueError):
+        c_out.times[0] = 0.5
+    rc = getrefcount(c_out)
+    tmp3 = c_out.times  # noqa: F841
+    assert getrefcount(c_out) == rc + 1
+    assert c_out.tcs.shape == (c_out.n_steps, 2, ta.order + 1, 4)
