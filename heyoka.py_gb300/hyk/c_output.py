@@ -17,6 +17,8 @@ step start (libhyk's dense-output kernel).
 
 from __future__ import annotations
 
+import copy as _copy
+
 import numpy as np
 import torch
 
@@ -188,13 +190,27 @@ class continuous_output_batch:
             self._tlo[: k + 1, sl].contiguous(), self._order, None if self._nit is None else self._nit[sl],
         )
 
-    def __copy__(self):
+    def _clone(self):
         if self._tcs is None:
             return continuous_output_batch()
-        return continuous_output_batch(self._tcs.clone(), self._thi.clone(), self._tlo.clone(), self._order)
+        new = continuous_output_batch(self._tcs.clone(), self._thi.clone(), self._tlo.clone(), self._order,
+                                      None if self._nit is None else self._nit.clone())
+        new._out = None if self._out is None else self._out.clone()
+        return new
+
+    def __copy__(self):
+        # The data are copied (the reference's object is a value); attributes
+        # added from Python are shared, as a shallow copy of the instance
+        # dictionary (heyoka/taylor_expose_c_output.cpp:518-522, heyoka/common_utils.hpp:96-150).
+        new = self._clone()
+        new.__dict__.update({k: v for k, v in self.__dict__.items() if k not in new.__dict__})
+        return new
 
     def __deepcopy__(self, memo):
-        return self.__copy__()
+        new = self._clone()
+        memo[id(self)] = new
+        new.__dict__.update({k: _copy.deepcopy(v, memo) for k, v in self.__dict__.items() if k not in new.__dict__})
+        return new
 
     def __repr__(self):
         if self._tcs is None:

@@ -19,14 +19,17 @@ from __future__ import annotations
 import copy as _copy
 
 import numpy as np
+import torch
 
-from .integrator import _callbacks, _fp_of, taylor_adaptive_batch, taylor_outcome
+from .integrator import _callbacks, _fp_of, _owned, taylor_adaptive_batch, taylor_outcome
 
 
 class continuous_output:
     """Dense output of a scalar propagation (reference:
     heyoka/taylor_expose_c_output.cpp:21-258): ``c(t)`` gives the state at t
-    (shape (dim,)), ``c(array of n times)`` the states (shape (n, dim))."""
+    (shape (dim,)), ``c(array of n times)`` the states (shape (n, dim)).  The
+    host arrays it returns are read-only and keep it alive, as the
+    reference's do."""
 
     def __init__(self, batch_c=None):
         from .c_output import continuous_output_batch
@@ -42,29 +45,36 @@ class continuous_output:
         return self._c.llvm_state
 
     def __call__(self, t=None, time=None):
-        self._check()
         a = np.asarray(t if t is not None else time)
+        if a.ndim == 1 and a.size == 0:
+            # no times: an empty (0, dim) array, dim 0 for a default-constructed object
+            return _owned(np.zeros((0, self._c._dim), dtype=self._dtype()), self)
+        self._check()
         if a.ndim == 0:
-            return self._c(np.full(1, float(a)))[:, 0]
+            return _owned(np.asarray(self._c(np.full(1, a))[:, 0]), self)
         if a.ndim != 1:
             raise ValueError("Invalid time array passed to a continuous_output object: the number of dimensions "
-                             "must be 0 or 1, but it is {} instead".format(a.ndim))
-        return self._c(a.reshape(-1, 1))[:, :, 0]
+                             "must be 1, but it is {} instead".format(a.ndim))
+        return _owned(np.ascontiguousarray(self._c(a.reshape(-1, 1))[:, :, 0]), self)
+
+    def _dtype(self):
+        tc = self._c._tcs
+        return np.float64 if tc is None or tc.dtype == torch.float64 else np.float32
 
     @property
     def output(self):
         o = self._c.output
-        return None if o is None else o[:, 0]
+        return None if o is None else _owned(np.asarray(o[:, 0]), self)
 
     @property
     def times(self):
         t = self._c.times
-        return None if t is None else t[:, 0]
+        return None if t is None else _owned(np.asarray(t[:, 0]), self)
 
     @property
     def tcs(self):
         t = self._c.tcs
-        return None if t is None else t[..., 0]
+        return None if t is None else _owned(np.asarray(t[..., 0]), self)
 
     @property
     def bounds(self):
@@ -77,11 +87,18 @@ class continuous_output:
         self._check()
         return self._c.n_steps
 
+    # Copies: the data are copied, attributes added from Python are shared by
+    # a copy and deep-copied by a deep copy (heyoka/common_utils.hpp:96-150).
     def __copy__(self):
-        return continuous_output(_copy.copy(self._c))
+        new = continuous_output(_copy.copy(self._c))
+        new.__dict__.update({k: v for k, v in self.__dict__.items() if k not in new.__dict__})
+        return new
 
     def __deepcopy__(self, memo):
-        return continuous_output(_copy.deepcopy(self._c, memo))
+        new = continuous_output(_copy.deepcopy(self._c, memo))
+        memo[id(self)] = new
+        new.__dict__.update({k: _copy.deepcopy(v, memo) for k, v in self.__dict__.items() if k not in new.__dict__})
+        return new
 
     def __repr__(self):
         if self._c._tcs is None:
@@ -324,4 +341,8 @@ def _mdt(max_delta_t):
     return [] if v == np.inf else v
 
 
-__all__ = ["continuous_output", "taylor_adaptive", "taylor_outcome"]
+# The reference's per-precision class names (the class here serves both).
+continuous_output_dbl = continuous_output
+continuous_output_flt = continuous_output
+
+__all__ = ["continuous_output", "continuous_output_dbl", "continuous_output_flt", "taylor_adaptive", "taylor_outcome"]

@@ -325,3 +325,118 @@ def test_reference_c_output_batch_behaviour(fp_t):
     tmp3 = c_out.times  # noqa: F841
     assert getrefcount(c_out) == rc + 1
     assert c_out.tcs.shape == (c_out.n_steps, 2, ta.order + 1, 4)
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_reference_c_output_scalar_behaviour(fp_t):
+    """heyoka/test.py c_output_test_case.test_scalar (default construction,
+    views that keep the object alive, shapes, errors, copies, pickling)."""
+    import pickle
+    from copy import copy, deepcopy
+    from sys import getrefcount
+
+    c_out = hyk.continuous_output_dbl() if fp_t is float else hyk.continuous_output_flt()
+    with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output object"):
+        c_out(fp_t(0))
+    with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output object"):
+        c_out(time=[fp_t(0), fp_t(0)])
+    assert c_out(time=np.zeros((0,), dtype=fp_t)).shape == (0, 0)
+    assert c_out.output is None and c_out.times is None and c_out.tcs is None
+    for obj in (c_out, copy(c_out), deepcopy(c_out), pickle.loads(pickle.dumps(c_out))):
+        with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output object"):
+            obj.n_steps
+        with pytest.raises(ValueError, match="Cannot use a default-constructed continuous_output object"):
+            obj.bounds
+        assert "forward" not in repr(obj) and obj.llvm_state.ir != ""
+
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    ic = [fp_t(0), fp_t(0.25)]
+    ta = hyk.taylor_adaptive(sys=sys_, state=ic, fp_type=fp_t)
+
+    def reset():
+        ta.state[:] = ic
+        ta.time = fp_t(0)
+
+    assert ta.propagate_until(fp_t(10))[4] is None
+    reset()
+    assert ta.propagate_until(fp_t(10), c_output=False)[4] is None
+    reset()
+    _, _, _, nsteps, c_out, cb = ta.propagate_until(fp_t(10), c_output=True)
+    assert cb is None and c_out is not None
+    assert c_out(fp_t(0.1)).shape == (2,)
+    with pytest.raises(ValueError):
+        c_out(fp_t(0.1))[0] = 0.5
+    rc = getrefcount(c_out)
+    tmp = c_out(fp_t(0.1))  # noqa: F841
+    assert getrefcount(c_out) == rc + 1
+    assert c_out(np.zeros((0,), dtype=fp_t)).shape == (0, 2)
+    tmp = c_out([fp_t(0), fp_t(1), fp_t(2)])
+    for i in range(3):
+        assert np.all(c_out(fp_t(i)) == tmp[i])
+    with pytest.raises(ValueError, match="Invalid time array passed to a continuous_output object: the number of "
+                                         "dimensions must be 1, but it is 2 instead"):
+        c_out([[fp_t(0)], [fp_t(1)], [fp_t(2)]])
+    assert np.all(c_out.output == tmp[2])
+    with pytest.raises(ValueError):
+        c_out.output[0] = 0.5
+    for name in ("output", "times", "tcs"):
+        rc = getrefcount(c_out)
+        held = getattr(c_out, name)  # noqa: F841
+        assert getrefcount(c_out) == rc + 1
+        del held
+    assert c_out.times.shape == (nsteps + 1,)
+    with pytest.raises(ValueError):
+        c_out.times[0] = 0.5
+    assert c_out.tcs.shape == (nsteps, 2, ta.order + 1) and np.all(np.isfinite(c_out.tcs))
+    with pytest.raises(ValueError):
+        c_out.tcs[0, 0, 0] = 0.5
+    assert c_out.bounds == (0, 10) and c_out.n_steps > 0
+    assert "forward" in repr(c_out) and c_out.llvm_state.ir != ""
+    for c in (copy(c_out), deepcopy(c_out), pickle.loads(pickle.dumps(c_out))):
+        assert c.tcs.shape == (nsteps, 2, ta.order + 1) and np.all(np.isfinite(c.tcs))
+        with pytest.raises(ValueError):
+            c.tcs[0, 0, 0] = 0.5
+
+    class foo:
+        pass
+
+    c_copy = deepcopy(c_out)
+    c_copy.bar = foo()
+    assert id(c_copy.bar) == id(copy(c_copy).bar)
+    assert id(c_copy.bar) != id(deepcopy(c_copy).bar)
+    assert np.all(c_copy(fp_t(0.1)) == copy(c_copy)(fp_t(0.1)))
+    assert np.all(c_copy(fp_t(0.1)) == deepcopy(c_copy)(fp_t(0.1)))
+    c_out.foo = []
+    c_out = pickle.loads(pickle.dumps(c_out))
+    assert c_out.tcs.shape == (nsteps, 2, ta.order + 1) and c_out.foo == []
+
+
+@pytest.mark.parametrize("fp_t", [np.float32, float])
+def test_reference_c_output_batch_copies(fp_t):
+    """heyoka/test.py c_output_test_case.test_batch: copies and pickles of a
+    batch continuous output, with attributes added from Python."""
+    import pickle
+    from copy import copy, deepcopy
+
+    x, v = hyk.make_vars("x", "v")
+    sys_ = [(x, v), (v, -9.8 * hyk.sin(x))]
+    ic = np.array([[0.0, 0.01, 0.02, 0.03], [0.25, 0.26, 0.27, 0.28]], dtype=fp_t)
+    ta = hyk.taylor_adaptive_batch(sys_, ic, fp_type=fp_t)
+    c_out = ta.propagate_until(np.array([10.0, 10.4, 10.5, 11.0], dtype=fp_t), c_output=True)[0]
+    assert "forward" in repr(c_out)
+    for c in (copy(c_out), deepcopy(c_out), pickle.loads(pickle.dumps(c_out))):
+        assert c.tcs.shape == (c.n_steps, 2, ta.order + 1, 4) and c.llvm_state.ir != ""
+
+    class foo:
+        pass
+
+    c_copy = deepcopy(c_out)
+    c_copy.bar = foo()
+    assert id(c_copy.bar) == id(copy(c_copy).bar)
+    assert id(c_copy.bar) != id(deepcopy(c_copy).bar)
+    assert np.all(c_copy(fp_t(0.1)) == copy(c_copy)(fp_t(0.1)))
+    assert np.all(c_copy(fp_t(0.1)) == deepcopy(c_copy)(fp_t(0.1)))
+    c_out.foo = []
+    c_out = pickle.loads(pickle.dumps(c_out))
+    assert c_out.tcs.shape == (c_out.n_steps, 2, ta.order + 1, 4) and c_out.foo == []
