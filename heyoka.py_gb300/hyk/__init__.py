@@ -15,6 +15,7 @@ from . import callback, model, workloads  # noqa: F401
 from .integrator import code_model, taylor_adaptive_batch, taylor_outcome  # noqa: F401
 from .events import event_direction, nt_event, nt_event_batch, t_event, t_event_batch  # noqa: F401
 from .c_output import continuous_output_batch, continuous_output_batch_dbl, continuous_output_batch_flt  # noqa: F401
+from .s11n import get_serialization_backend, set_serialization_backend  # noqa: F401
 from .scalar import continuous_output, continuous_output_dbl, continuous_output_flt, taylor_adaptive  # noqa: F401
 from .ensemble import (  # noqa: F401
     ensemble_propagate_for,

@@ -45,7 +45,7 @@ class angle_reducer:
         if self._idx is None:
             self.pre_hook(ta)
         if self._idx:
-            st = ta._state
+            st = getattr(ta, "_b", ta)._state  # a scalar integrator's state is its one-lane batch's
             dt = st.dtype
             two_pi = torch.tensor(_TWO_PI, dtype=dt, device=st.device)
             rows = st[self._idx]

@@ -25,11 +25,11 @@ from __future__ import annotations
 
 import copy as _copy
 import enum
-import pickle
 
 import numpy as np
 
 from . import expr as _e
+from . import s11n as _s11n
 
 __all__ = ["event_direction", "nt_event", "nt_event_batch", "t_event", "t_event_batch"]
 
@@ -58,17 +58,11 @@ def _check_cb(cb):
 
 
 def _dump_cb(cb):
-    try:
-        import cloudpickle
-
-        return ("cloudpickle", cloudpickle.dumps(cb))
-    except ImportError:  # pragma: no cover - the GPU host has no cloudpickle
-        return ("pickle", pickle.dumps(cb))
+    return _s11n.dumps(cb)
 
 
 def _load_cb(blob):
-    kind, data = blob
-    return pickle.loads(data)  # both formats load with pickle
+    return _s11n.loads(blob)
 
 
 class _EventBase:

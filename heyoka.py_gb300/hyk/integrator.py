@@ -132,9 +132,12 @@ class _OwnedArray(np.ndarray):
 
 
 def _owned(a, owner):
-    v = np.asarray(a).view(_OwnedArray)
+    # The array under the view is made read-only too, so that the view's
+    # writeability cannot be turned back on (as with the reference's arrays).
+    base = np.asarray(a)
+    base.flags.writeable = False
+    v = base.view(_OwnedArray)
     v._owner = owner
-    v.flags.writeable = False
     return v
 
 
@@ -528,7 +531,9 @@ class taylor_adaptive_batch:
                 if e:
                     term = term * arr[j] ** e
             out[comp] += term
+        buf.flags.writeable = True  # the buffer owns its memory; the views handed out stay read-only
         buf[...] = out
+        buf.flags.writeable = False
         return self.tstate
 
     @property
