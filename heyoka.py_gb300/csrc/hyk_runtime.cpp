@@ -36,6 +36,8 @@ extern "C" int hyk_generic_dense_eval_f32(const float *tc, uint32_t n_eq, uint32
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_fp32_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
+extern "C" int hyk_generic_compact_active(const uint32_t *status, uint64_t n_lanes, uint64_t *list, uint32_t *count,
+                                          void *stream);
 extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
 extern "C" int hyk_noalloc_scratch(int device, void **ptr, size_t *bytes, char *err, size_t errlen);
 
@@ -128,6 +130,7 @@ struct KParams {
     uint32_t *finished;
     const uint64_t *lane_order;
     uint64_t n_order;
+    const uint32_t *act_count;
     double *ck_x, *ck_t, *ck_h;
     uint64_t ck_cap;
     const int64_t *adj_steps;
@@ -682,11 +685,20 @@ int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     return launch(m, m->f_init, (lanes->n_lanes + 127) / 128, 128, 0, k, stream);
 }
 
+// Counters: the queue (8 B at 0), the finished-lane count (4 B at 8) and the
+// active-lane count (4 B at 12), padded to 256 B.  The plain form of a
+// lane-form module also takes, after them, the list of unfinished lanes (8 B
+// per lane); with a workspace of only the counters it steps the lanes in
+// place (thread = lane) instead.
+static constexpr size_t kWsCounters = 256;
+
+static bool plain_compacts(const hyk_module *m, uint64_t n_lanes, size_t workspace_bytes) {
+    return m && !m->team && n_lanes > 0 && workspace_bytes >= kWsCounters + 8 * n_lanes;
+}
+
 size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode) {
-    (void)m;
-    (void)n_lanes;
-    (void)mode;
-    return 256;  // queue counter (8 B) + finished counter (4 B), padded
+    if (mode == HYK_MODE_PLAIN && m && !m->team) return kWsCounters + 8 * n_lanes;
+    return kWsCounters;
 }
 
 int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
@@ -695,8 +707,7 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (rc) return rc;
     if (iters) *iters = 0;
     if (lanes->n_lanes == 0) return 0;
-    if (!workspace || workspace_bytes < hyk_propagate_workspace_size(m, lanes->n_lanes, mode))
-        return fail(HYK_ERR_INVALID, "workspace too small");
+    if (!workspace || workspace_bytes < kWsCounters) return fail(HYK_ERR_INVALID, "workspace too small");
     if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return fail(HYK_ERR_INVALID, "workspace must be 256-byte aligned");
     HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
     KParams k;
@@ -716,25 +727,50 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
         return 0;
     }
     if (mode != HYK_MODE_PLAIN) return fail(HYK_ERR_INVALID, "unknown propagation mode");
-    // One launch per step.  Completion is detected by counting lanes whose
-    // status is done or stopped; the count is read back every check_every
-    // launches (the only host synchronisation of the loop).  From the second
-    // round on, the check_every launches of a round are one CUDA graph
-    // (built once per call, replayed each round): one host call per round.
+    // One launch per step, in rounds of check_every launches; between rounds
+    // one word is read back (the only host synchronisation of the loop).
+    // With room for the lane list, each round starts by compacting the
+    // unfinished lanes into it, and the launches of the round step only those
+    // (a grid of at most the resident capacity looping over the list), so
+    // warps are not left half idle by finished lanes; the word read back is
+    // the list's length.  Without it, every launch covers all lanes and the
+    // word is the number of finished lanes.  From the second round on, the
+    // check_every launches of a round are one CUDA graph (built once per call
+    // and replayed: the list's length is read by the kernel from device
+    // memory, so the launch parameters do not change between rounds).
     if (check_every == 0) check_every = 16;
     k.persistent = 0;
     k.iters_per_launch = 1;
-    const uint64_t grid = lane_blocks(m, lanes->n_lanes);
-    rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
-    if (rc) return rc;
+    const bool compact = plain_compacts(m, lanes->n_lanes, workspace_bytes);
+    uint64_t *list = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(workspace) + kWsCounters);
+    uint32_t *act = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(workspace) + 12);
+    uint64_t grid = lane_blocks(m, lanes->n_lanes);
+    if (compact) {
+        k.lane_order = list;
+        k.n_order = 0;
+        k.act_count = act;
+        grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm);
+    }
+    if (!compact) {
+        rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
+        if (rc) return rc;
+    }
     uint64_t n = 0;
-    uint32_t fin = 0;
+    uint32_t word = 0;
     const bool graphs = check_every > 1 && !std::getenv("HYK_PLAIN_NO_GRAPH");
     LaunchGraph lg;
     for (uint64_t round = 0;; ++round) {
-        HYK_CU(drv().cuMemcpyDtoHAsync(&fin, (CUdeviceptr)k.finished, sizeof fin, s));
-        HYK_CU(drv().cuStreamSynchronize(s));
-        if ((uint64_t)fin >= lanes->n_lanes) break;
+        if (compact) {
+            if (hyk_generic_compact_active(p->status, lanes->n_lanes, list, act, stream))
+                return fail(HYK_ERR_CUDA, "launch of the lane compaction kernel failed");
+            HYK_CU(drv().cuMemcpyDtoHAsync(&word, (CUdeviceptr)act, sizeof word, s));
+            HYK_CU(drv().cuStreamSynchronize(s));
+            if (word == 0) break;
+        } else {
+            HYK_CU(drv().cuMemcpyDtoHAsync(&word, (CUdeviceptr)k.finished, sizeof word, s));
+            HYK_CU(drv().cuStreamSynchronize(s));
+            if ((uint64_t)word >= lanes->n_lanes) break;
+        }
         if (graphs && round >= 1) {
             if (!lg.x) {
                 rc = build_graph(m, m->f_prop, grid, m->blk, m->smem, k, check_every, lg);
@@ -767,11 +803,10 @@ int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
     size_t cap = 0;
     char buf[256] = {0};
     if (hyk_noalloc_scratch(m->device, &ws, &cap, buf, sizeof buf)) return fail(HYK_ERR_CUDA, buf);
-    const size_t need = hyk_propagate_workspace_size(m, lanes ? lanes->n_lanes : 0, mode);
-    if (need > cap)
-        return fail(HYK_ERR_INVALID, "hyk_propagate_noalloc: this propagation needs " + std::to_string(need) +
-                                         " bytes of scratch, more than the " + std::to_string(cap) +
-                                         " bytes the no-allocation entry point holds; use hyk_propagate with a workspace");
+    // The counters always fit; the plain form's lane list does when the
+    // batch is small enough, and the plain form steps the lanes in place
+    // otherwise.
+    if (kWsCounters > cap) return fail(HYK_ERR_INVALID, "hyk_propagate_noalloc: the scratch array is too small");
     return hyk_propagate(m, lanes, p, mode, ws, cap, check_every, iters, stream);
 }
 

@@ -989,9 +989,14 @@ class taylor_adaptive_batch:
             ev = self._launch_events  # optional (start, end) CUDA events around the propagation launch(es)
             if ev is not None:
                 ev[0].record(torch.cuda.current_stream(self._dev))
+            ws, ws_bytes = mod.ws, mod.ws_bytes
+            if mode == _lib.HYK_MODE_PLAIN:
+                # counters plus the list of unfinished lanes the plain form steps
+                ws_bytes = int(L.hyk_propagate_workspace_size(mod.handle, B, mode))
+                ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self._tdev)
             while True:
                 _lib.check(
-                    L.hyk_propagate(mod.handle, lanes, d, mode, mod.ws.data_ptr(), mod.ws_bytes, 16, None, s),
+                    L.hyk_propagate(mod.handle, lanes, d, mode, ws.data_ptr(), ws_bytes, 16, None, s),
                     "hyk_propagate",
                 )
                 if ev is not None:

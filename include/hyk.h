@@ -274,7 +274,12 @@ int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 #define HYK_MODE_PLAIN 0      /* one kernel launch per step (drop-in form) */
 #define HYK_MODE_PERSISTENT 1 /* persistent kernel, per-lane loops, lane queue */
 
-/* Device workspace needed by hyk_propagate (bytes, 256-byte aligned pointer). */
+/* Device workspace for hyk_propagate (bytes, 256-byte aligned pointer):
+ * 256 bytes of counters, plus, for the PLAIN mode of a lane-form module, a
+ * list of 8 bytes per lane.  hyk_propagate accepts any workspace of at least
+ * 256 bytes; with less than this size the PLAIN mode steps the lanes in
+ * place instead of compacting the unfinished ones (same results, slower
+ * when lanes finish at different times). */
 size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode);
 
 /* Advance every unfinished lane until it is done or stopped.
@@ -293,9 +298,10 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
  * counterpart in the reference: it has no device memory at all.
  * The counters hyk_propagate keeps in its workspace live instead in one
  * file-scope device array of HYK_NOALLOC_SCRATCH_BYTES (4096) bytes, held by
- * every GPU that loads libhyk until the process exits; a propagation whose
- * hyk_propagate_workspace_size() exceeds it is rejected with HYK_ERR_INVALID.
- * The current kernels need 256 bytes whatever the number of lanes.
+ * every GPU that loads libhyk until the process exits.
+ * The counters (256 bytes) always fit; the PLAIN mode compacts the
+ * unfinished lanes when the lane list fits too (up to 480 lanes) and steps
+ * the lanes in place otherwise.
  * The first call on a device looks up the array's device address; make that
  * first call before any stream capture.  Every call clears the counters it
  * needs before using them, so a call never sees the previous call's values,

@@ -17,6 +17,7 @@ import pytest
 import torch
 
 import hyk
+from hyk import _lib
 from hyk import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -329,3 +330,39 @@ def test_pin_arithmetic_module_close_to_oracle_pin(oracle):
     rel = np.max(np.abs(np.asarray(ta.state) - o.state), axis=0) / np.max(np.abs(o.state), axis=0)
     assert rel.max() < 1e-11
     assert np.mean(res_arrays(ta)["n_steps"] == r["n_steps"]) >= 0.99
+
+
+@pytest.mark.parametrize("what", ["until", "grid", "c_output"])
+def test_plain_compacted_in_place_and_persistent_identical(monkeypatch, what):
+    """The plain form steps a compacted list of the unfinished lanes when its
+    workspace holds the list, and every lane in place when it holds only the
+    counters; both give the persistent form's bits (lanes with end times from
+    1 to 20, so that they finish many launches apart)."""
+    sys_ = W.kepler_sys()
+    n = 3000
+    st = W.kepler_ics(n, seed=5)
+    tf = np.linspace(1.0, 20.0, n)
+    grid = np.linspace(0.0, 1.0, 7).reshape(-1, 1) * tf.reshape(1, -1)
+
+    def run(mode):
+        ta = hyk.taylor_adaptive_batch(sys_, st, tol=1e-15, prop_mode=mode)
+        if what == "grid":
+            out = ta.propagate_grid(grid)[1]
+        elif what == "c_output":
+            c = ta.propagate_until(tf, c_output=True)[0]
+            out = c(0.5 * tf)
+        else:
+            ta.propagate_until(tf)
+            out = None
+        return np.asarray(ta.state), ta.propagate_res, out
+
+    ref = run("persistent")
+    comp = run("plain")
+    L = _lib.load()
+    monkeypatch.setattr(L, "hyk_propagate_workspace_size", lambda *a: 256)
+    inplace = run("plain")
+    for r in (comp, inplace):
+        assert np.array_equal(r[0], ref[0])
+        assert r[1] == ref[1]
+        if ref[2] is not None:
+            assert np.array_equal(r[2], ref[2], equal_nan=True)
