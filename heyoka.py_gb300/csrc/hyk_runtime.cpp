@@ -686,18 +686,17 @@ int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 }
 
 // Counters: the queue (8 B at 0), the finished-lane count (4 B at 8) and the
-// active-lane count (4 B at 12), padded to 256 B.  The plain form of a
-// lane-form module also takes, after them, the list of unfinished lanes (8 B
-// per lane); with a workspace of only the counters it steps the lanes in
-// place (thread = lane) instead.
+// active-lane count (4 B at 12), padded to 256 B.  The plain form also takes,
+// after them, the list of unfinished lanes (8 B per lane); with a workspace
+// of only the counters it steps the lanes in place instead.
 static constexpr size_t kWsCounters = 256;
 
 static bool plain_compacts(const hyk_module *m, uint64_t n_lanes, size_t workspace_bytes) {
-    return m && !m->team && n_lanes > 0 && workspace_bytes >= kWsCounters + 8 * n_lanes;
+    return m && n_lanes > 0 && workspace_bytes >= kWsCounters + 8 * n_lanes;
 }
 
 size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode) {
-    if (mode == HYK_MODE_PLAIN && m && !m->team) return kWsCounters + 8 * n_lanes;
+    if (mode == HYK_MODE_PLAIN && m) return kWsCounters + 8 * n_lanes;
     return kWsCounters;
 }
 

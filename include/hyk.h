@@ -275,8 +275,8 @@ int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 #define HYK_MODE_PERSISTENT 1 /* persistent kernel, per-lane loops, lane queue */
 
 /* Device workspace for hyk_propagate (bytes, 256-byte aligned pointer):
- * 256 bytes of counters, plus, for the PLAIN mode of a lane-form module, a
- * list of 8 bytes per lane.  hyk_propagate accepts any workspace of at least
+ * 256 bytes of counters, plus, for the PLAIN mode, a list of 8 bytes per
+ * lane.  hyk_propagate accepts any workspace of at least
  * 256 bytes; with less than this size the PLAIN mode steps the lanes in
  * place instead of compacting the unfinished ones (same results, slower
  * when lanes finish at different times). */

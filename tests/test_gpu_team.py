@@ -138,3 +138,28 @@ def test_team_global_memory_oss_matches_shared():
     _, ga = a.propagate_grid(grid)
     _, gb = b.propagate_grid(grid)
     assert np.array_equal(ga, gb) and torch.equal(a.state, b.state)
+
+
+@pytest.mark.parametrize("gmem", [False, True])
+def test_team_plain_compacted_and_in_place_identical(monkeypatch, gmem):
+    """The team form's plain propagation over the compacted list of unfinished
+    trajectories, and over all of them in place (a workspace of only the
+    counters), gives the persistent form's bits; end times from 1 to 20, so
+    that trajectories finish many launches apart."""
+    from hyk import _lib
+
+    n = 2000
+    st = W.kepler_ics(n, seed=36)
+    tf = np.linspace(1.0, 20.0, n)
+
+    def run(mode):
+        ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=1e-15, prop_mode=mode, team_size=4, global_jets=gmem)
+        ta.propagate_until(tf)
+        return np.asarray(ta.state), ta.propagate_res
+
+    ref = run("persistent")
+    comp = run("plain")
+    monkeypatch.setattr(_lib.load(), "hyk_propagate_workspace_size", lambda *a: 256)
+    inplace = run("plain")
+    for r in (comp, inplace):
+        assert np.array_equal(r[0], ref[0]) and r[1] == ref[1]
