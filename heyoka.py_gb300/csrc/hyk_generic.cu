@@ -42,23 +42,6 @@ __global__ void count_finished_kernel(const uint32_t *__restrict__ status, uint6
 
 __global__ void zero_u32(uint32_t *p) { *p = 0; }
 
-// The unfinished lanes (status neither done nor stopped), appended to list;
-// *count (zeroed before) ends as their number.  One atomic per warp; the
-// lanes of a warp keep their order, the warps' runs land in any order.
-__global__ void compact_active_kernel(const uint32_t *__restrict__ status, uint64_t n_lanes, uint64_t *__restrict__ list,
-                                      uint32_t *count) {
-    const unsigned lane_id = threadIdx.x & 31u;
-    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n_lanes; base += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t l = base + threadIdx.x;
-        const bool act = l < n_lanes && (status[l] & 3u) == 0u;
-        const unsigned m = __ballot_sync(0xffffffffu, act);
-        uint32_t off = 0;
-        if (lane_id == 0 && m) off = atomicAdd(count, (uint32_t)__popc(m));
-        off = __shfl_sync(0xffffffffu, off, 0);
-        if (act) list[off + __popc(m & ((1u << lane_id) - 1u))] = l;
-    }
-}
-
 __global__ void dmath_kernel(int fn, const double *__restrict__ x, const double *__restrict__ a, double *__restrict__ out,
                              uint64_t n) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -138,16 +121,6 @@ extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lan
     if (grid > 4096) grid = 4096;
     if (grid == 0) grid = 1;
     count_finished_kernel<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(status, n_lanes, finished);
-    return cudaGetLastError() == cudaSuccess ? 0 : -2;
-}
-
-extern "C" int hyk_generic_compact_active(const uint32_t *status, uint64_t n_lanes, uint64_t *list, uint32_t *count,
-                                          void *stream) {
-    zero_u32<<<1, 1, 0, (cudaStream_t)stream>>>(count);
-    uint64_t grid = (n_lanes + 255) / 256;
-    if (grid > 4096) grid = 4096;
-    if (grid == 0) grid = 1;
-    compact_active_kernel<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(status, n_lanes, list, count);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 

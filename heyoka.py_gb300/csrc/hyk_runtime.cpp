@@ -36,8 +36,6 @@ extern "C" int hyk_generic_dense_eval_f32(const float *tc, uint32_t n_eq, uint32
 extern "C" int hyk_generic_fp64_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_fp32_peak(int device, double millis, double *flops_per_s, char *err, size_t errlen);
 extern "C" int hyk_generic_count_finished(const uint32_t *status, uint64_t n_lanes, uint32_t *finished, void *stream);
-extern "C" int hyk_generic_compact_active(const uint32_t *status, uint64_t n_lanes, uint64_t *list, uint32_t *count,
-                                          void *stream);
 extern "C" int hyk_generic_dmath(int fn, const double *x, const double *a, double *out, uint64_t n, void *stream);
 extern "C" int hyk_noalloc_scratch(int device, void **ptr, size_t *bytes, char *err, size_t errlen);
 
@@ -232,6 +230,7 @@ struct hyk_module {
     Device *dv = nullptr;
     CUmodule mod = nullptr;
     CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
+    CUfunction f_azero = nullptr, f_alist = nullptr;  // the plain form's list of unfinished lanes
     int adj_ctas_per_sm = 0;
     uint32_t team = 0;           // threads per trajectory (team form); 0 = lane form
     bool f32 = false;            // single precision
@@ -442,6 +441,8 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuModuleGetFunction(&m->f_step, m->mod, "hyk_step_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_prop, m->mod, "hyk_prop_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
+    HYK_CU(drv().cuModuleGetFunction(&m->f_azero, m->mod, "hyk_act_zero_kernel"));
+    HYK_CU(drv().cuModuleGetFunction(&m->f_alist, m->mod, "hyk_act_list_kernel"));
     for (CUfunction f : {m->f_step, m->f_prop}) {
         HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
         // Global-memory coefficients: no shared memory, the whole unified
@@ -559,9 +560,9 @@ static int launch(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size
     return 0;
 }
 
-// A CUDA graph of `count` launches of f with the same parameters, in
-// sequence (the plain propagation's launches between two reads of the
-// finished-lane counter).  The parameter block is copied into the nodes.
+// A CUDA graph of a chain of launches with the same parameter block (the
+// plain propagation's launches between two reads of the unfinished-lane
+// count).  The parameter block is copied into the nodes.
 struct LaunchGraph {
     CUgraph g = nullptr;
     CUgraphExec x = nullptr;
@@ -571,24 +572,30 @@ struct LaunchGraph {
     }
 };
 
-static int build_graph(hyk_module *m, CUfunction f, uint64_t grid, uint32_t blk, size_t smem, KParams &k,
-                       uint32_t count, LaunchGraph &lg) {
+struct LaunchSpec {
+    CUfunction f;
+    uint64_t grid;
+    uint32_t blk;
+    size_t smem;
+};
+
+static int build_graph(hyk_module *m, const std::vector<LaunchSpec> &chain, KParams &k, LaunchGraph &lg) {
     k.jets = reinterpret_cast<double *>(m->jets);
-    grid = launch_grid(m, f, grid);
-    if (grid == 0 || grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
     HYK_CU(drv().cuGraphCreate(&lg.g, 0));
     void *args[] = {&k};
-    CUDA_KERNEL_NODE_PARAMS np;
-    std::memset(&np, 0, sizeof np);
-    np.func = f;
-    np.gridDimX = (unsigned)grid;
-    np.gridDimY = np.gridDimZ = 1;
-    np.blockDimX = blk;
-    np.blockDimY = np.blockDimZ = 1;
-    np.sharedMemBytes = (unsigned)smem;
-    np.kernelParams = args;
     CUgraphNode prev = nullptr;
-    for (uint32_t c = 0; c < count; ++c) {
+    for (const LaunchSpec &ls : chain) {
+        const uint64_t grid = launch_grid(m, ls.f, ls.grid);
+        if (grid == 0 || grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
+        CUDA_KERNEL_NODE_PARAMS np;
+        std::memset(&np, 0, sizeof np);
+        np.func = ls.f;
+        np.gridDimX = (unsigned)grid;
+        np.gridDimY = np.gridDimZ = 1;
+        np.blockDimX = ls.blk;
+        np.blockDimY = np.blockDimZ = 1;
+        np.sharedMemBytes = (unsigned)ls.smem;
+        np.kernelParams = args;
         CUgraphNode node;
         HYK_CU(drv().cuGraphAddKernelNode(&node, lg.g, prev ? &prev : nullptr, prev ? 1 : 0, &np));
         prev = node;
@@ -728,31 +735,38 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     if (mode != HYK_MODE_PLAIN) return fail(HYK_ERR_INVALID, "unknown propagation mode");
     // One launch per step, in rounds of check_every launches; between rounds
     // one word is read back (the only host synchronisation of the loop).
-    // With room for the lane list, each round starts by compacting the
-    // unfinished lanes into it, and the launches of the round step only those
-    // (a grid of at most the resident capacity looping over the list), so
-    // warps are not left half idle by finished lanes; the word read back is
-    // the list's length.  Without it, every launch covers all lanes and the
-    // word is the number of finished lanes.  From the second round on, the
-    // check_every launches of a round are one CUDA graph (built once per call
-    // and replayed: the list's length is read by the kernel from device
-    // memory, so the launch parameters do not change between rounds).
+    // With room for the lane list, every step launch is preceded by two small
+    // launches that list the unfinished lanes (hyk_act_zero_kernel,
+    // hyk_act_list_kernel), and the step launch steps only those (a grid of
+    // at most the resident capacity looping over the list, whose length it
+    // reads from device memory), so warps are not left half idle by lanes
+    // that finished; the word read back is the list's length.  Without it,
+    // every launch covers all lanes and the word is the number of finished
+    // lanes.  From the second round on, a round's launches are one CUDA graph
+    // (built once per call and replayed: the launch parameters do not change).
     if (check_every == 0) check_every = 16;
     k.persistent = 0;
     k.iters_per_launch = 1;
     const bool compact = plain_compacts(m, lanes->n_lanes, workspace_bytes);
-    uint64_t *list = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(workspace) + kWsCounters);
-    uint32_t *act = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(workspace) + 12);
     uint64_t grid = lane_blocks(m, lanes->n_lanes);
+    std::vector<LaunchSpec> round_chain;  // the launches of one round after its first listing
     if (compact) {
-        k.lane_order = list;
+        k.lane_order = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(workspace) + kWsCounters);
         k.n_order = 0;
-        k.act_count = act;
+        k.act_count = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(workspace) + 12);
         grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm);
-    }
-    if (!compact) {
+        const uint64_t lgrid = std::min<uint64_t>(4096, (lanes->n_lanes + 255) / 256);
+        for (uint32_t c = 0; c < check_every; ++c) {
+            if (c) {
+                round_chain.push_back({m->f_azero, 1, 32, 0});
+                round_chain.push_back({m->f_alist, lgrid, 256, 0});
+            }
+            round_chain.push_back({m->f_prop, grid, m->blk, m->smem});
+        }
+    } else {
         rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
         if (rc) return rc;
+        for (uint32_t c = 0; c < check_every; ++c) round_chain.push_back({m->f_prop, grid, m->blk, m->smem});
     }
     uint64_t n = 0;
     uint32_t word = 0;
@@ -760,9 +774,10 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     LaunchGraph lg;
     for (uint64_t round = 0;; ++round) {
         if (compact) {
-            if (hyk_generic_compact_active(p->status, lanes->n_lanes, list, act, stream))
-                return fail(HYK_ERR_CUDA, "launch of the lane compaction kernel failed");
-            HYK_CU(drv().cuMemcpyDtoHAsync(&word, (CUdeviceptr)act, sizeof word, s));
+            rc = launch(m, m->f_azero, 1, 32, 0, k, stream);
+            if (!rc) rc = launch(m, m->f_alist, std::min<uint64_t>(4096, (lanes->n_lanes + 255) / 256), 256, 0, k, stream);
+            if (rc) return rc;
+            HYK_CU(drv().cuMemcpyDtoHAsync(&word, (CUdeviceptr)k.act_count, sizeof word, s));
             HYK_CU(drv().cuStreamSynchronize(s));
             if (word == 0) break;
         } else {
@@ -772,17 +787,17 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
         }
         if (graphs && round >= 1) {
             if (!lg.x) {
-                rc = build_graph(m, m->f_prop, grid, m->blk, m->smem, k, check_every, lg);
+                rc = build_graph(m, round_chain, k, lg);
                 if (rc) return rc;
             }
             HYK_CU(drv().cuGraphLaunch(lg.x, s));
             n += check_every;
             continue;
         }
-        for (uint32_t c = 0; c < check_every; ++c) {
-            rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
+        for (const LaunchSpec &ls : round_chain) {
+            rc = launch(m, ls.f, ls.grid, ls.blk, ls.smem, k, stream);
             if (rc) return rc;
-            ++n;
+            if (ls.f == m->f_prop) ++n;
         }
     }
     if (iters) *iters = n;
