@@ -41,8 +41,8 @@ T_END = 200.0
 TOL = 1e-15
 
 # DRAM traffic of one persistent Kepler launch per lane, from ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum = 2.84 MB for 2^14 orbits).
-KEPLER_DRAM_BYTES_PER_LANE = 2.84e6 / 16384
+# (dram__bytes_read.sum + dram__bytes_write.sum = 2.65 MB for 2^14 orbits).
+KEPLER_DRAM_BYTES_PER_LANE = 2.65e6 / 16384
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -812,7 +812,7 @@ def main():
                 "unit": "TFLOP/s",
                 "frac": achieved / peak,
                 # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum of one
-                # 2^14-orbit launch (2.84 MB, one load and one store of each lane's state and
+                # 2^14-orbit launch (2.65 MB, one load and one store of each lane's state and
                 # bookkeeping), scaled by the lanes of this launch (the traffic is per lane)
                 "traffic": KEPLER_DRAM_BYTES_PER_LANE * n,
                 "traffic_source": "ncu capture of a 2^14-orbit launch, scaled by lanes",
