@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2048)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="kepler", choices=["kepler", "kepler-f32", "serve", "pendulum", "cr3bp-adjoint", "oss", "forms"],
+    ap.add_argument("--workload", default="kepler", choices=["kepler", "kepler-f32", "serve", "pendulum", "cr3bp-adjoint", "oss", "forms",
+                             "occupancy"],
                     help="kepler: the headline metric; serve: the Poisson request stream (p50/p99 latency); "
                          "pendulum: 4096 trajectories through ensemble_propagate_until; "
                          "cr3bp-adjoint: 65536 trajectories forward plus discrete adjoint")
@@ -643,6 +644,44 @@ def run_forms(args):
                   flush=True)
 
 
+def run_occupancy(args):
+    """Lane form with its coefficients in shared memory at every block size
+    from 32 to 256 lanes: 2^18 Kepler orbits propagated from t = 0 to 20, at
+    tol 1e-9 (order 12) and 1e-15 (order 19); one JSON line per block size
+    (resident warps per SM against trajectory-steps/s)."""
+    import torch
+
+    import hyk
+    from hyk import workloads as W
+
+    n = 1 << 18
+    st = W.kepler_ics(n, seed=1)
+    for tol in (1e-9, TOL):
+        for blk in (32, 64, 96, 128, 160, 192, 224, 256):
+            try:
+                ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=tol, block_lanes=blk)
+            except Exception as e:  # noqa: BLE001 - a block too large for shared memory
+                print(json.dumps({"tol": tol, "block_lanes": blk, "skipped": str(e)[:120]}), flush=True)
+                continue
+            info = ta.module_info
+            ta.propagate_until(1.0)
+            ta.set_time(0.0)
+            ta.state[:] = st
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            ta.propagate_until(20.0)
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            steps = int(ta.propagate_res_tensors["n_steps"].sum().item())
+            print(json.dumps({"tol": tol, "order": ta.order, "block_lanes": info["block_lanes"],
+                              "ctas_per_sm": info["ctas_per_sm"],
+                              "warps_per_sm": info["ctas_per_sm"] * info["block_lanes"] / 32,
+                              "smem_per_lane": info["smem_per_lane"], "regs": info["regs_per_thread"],
+                              "ms": ms, "trajectory_steps_per_s": steps / ms * 1e3}), flush=True)
+
+
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
@@ -652,7 +691,7 @@ def main():
     if args.workload != "kepler":
         if rank == 0:
             {"serve": run_serve, "pendulum": run_pendulum, "cr3bp-adjoint": run_cr3bp_adjoint, "oss": run_oss,
-             "forms": run_forms, "kepler-f32": run_kepler_f32}[args.workload](args)
+             "forms": run_forms, "kepler-f32": run_kepler_f32, "occupancy": run_occupancy}[args.workload](args)
         return
     import numpy as np
     import torch
