@@ -203,7 +203,7 @@ class taylor_adaptive:
 
     @property
     def tstate(self):
-        return self._b.tstate[:, 0]
+        return _owned(np.asarray(self._b.tstate[:, 0]), self)
 
     def __getattr__(self, name):
         # order, tol, dim, sys, decomposition, compact_mode, high_accuracy,
@@ -254,11 +254,37 @@ class taylor_adaptive:
         return self._b.get_mindex(i)
 
     def eval_taylor_map(self, inputs):
+        """The Taylor map at the displacements ``inputs`` (shape (n_vargs,));
+        returns ``tstate`` (reference: heyoka/taylor_expose_integrator.cpp,
+        checks as in heyoka/_test_var_integrator.py:68-110)."""
+        b = self._b
+        if b._vsys is None:
+            raise ValueError("The integrator is not variational")
+        m = len(b._vsys.vargs)
+        overlap = ValueError("The array of inputs provided for the evaluation of a Taylor map may overlap with the "
+                             "internal state of the integrator")
+        if isinstance(inputs, torch.Tensor):
+            if inputs.device.type == "cuda" and inputs.untyped_storage().data_ptr() == \
+                    b._state.untyped_storage().data_ptr():
+                raise overlap
+            inputs = inputs.detach().cpu().numpy()
+        if isinstance(inputs, np.ndarray) and np.shares_memory(inputs, b._tstate_buf()):
+            raise overlap
         a = np.asarray(inputs)
+        if isinstance(inputs, np.ndarray) and np.issubdtype(a.dtype, np.integer):
+            raise TypeError("Invalid dtype detected for the inputs of a Taylor map evaluation: the expected dtype is "
+                            "{}, but the dtype is {} instead".format(np.dtype(b._np_dt).name, a.dtype))
+        if isinstance(inputs, np.ndarray) and not inputs.flags.c_contiguous:
+            raise ValueError("Invalid inputs array detected in a Taylor map evaluation: the array is not C-style "
+                             "contiguous, please consider using numpy.ascontiguousarray() to turn it into one")
         if a.ndim != 1:
-            raise ValueError("The array of inputs provided for the evaluation of a Taylor map must be "
-                             "one-dimensional, but it has {} dimensions".format(a.ndim))
-        return self._b.eval_taylor_map(a.reshape(-1, 1))[:, 0]
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map has {} dimensions, but "
+                             "it must have 1 dimension instead".format(a.ndim))
+        if a.size != m:
+            raise ValueError("The array of inputs provided for the evaluation of a Taylor map has {} elements, but it "
+                             "must have {} elements instead".format(a.size, m))
+        b.eval_taylor_map(a.astype(b._np_dt).reshape(-1, 1))
+        return self.tstate
 
     # ------------------------------------------------------------ stepping
     def step(self, max_delta_t=None, write_tc=False):

@@ -91,3 +91,49 @@ def test_initial_time_variational_integrator_bitwise(oracle):
     o = oracle.Oracle(vs.sys, full0, pars=pars, time=t0, order=ta.order, mode=1)
     o.propagate_until(3.0)
     assert np.array_equal(np.asarray(ta.state), o.state)
+
+
+def test_reference_scalar_variational_integrator():
+    """heyoka/_test_var_integrator.py test_scalar (:14-110): a scalar
+    integrator of a second-order variational system, tstate that keeps the
+    integrator alive, the variable ordering, eval_taylor_map and its errors."""
+    x, v = hyk.make_vars("x", "v")
+    orig_sys = [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
+    vsys = hyk.var_ode_sys(orig_sys, hyk.var_args.vars, order=2)
+    ta = hyk.taylor_adaptive(vsys, [0.2, 0.3], pars=[0.4], time=0.5, compact_mode=True)
+    assert ta.dim > 2 and ta.n_orig_sv == 2 and ta.is_variational
+    assert ta.vorder == 2 and ta.vargs == [x, v]
+    rc = getrefcount(ta)
+    ts = ta.tstate
+    assert getrefcount(ta) == rc + 1
+    assert ts.shape == (2,) and np.all(ts == [0.0, 0.0])
+    with pytest.raises(ValueError):
+        ta.tstate[0] = 0.5
+    assert ta.get_vslice(order=0) == slice(0, 2, None)
+    assert ta.get_vslice(order=0, component=1) == slice(1, 2, None)
+    assert ta.get_vslice(order=1) == slice(2, 6, None)
+    assert ta.get_vslice(order=1, component=1) == slice(4, 6, None)
+    assert ta.get_mindex(0) == [0, 0, 0] and ta.get_mindex(1) == [1, 0, 0]
+    assert ta.get_mindex(2) == [0, 1, 0] and ta.get_mindex(3) == [0, 0, 1]
+    assert ta.get_mindex(4) == [1, 1, 0] and ta.get_mindex(i=5) == [1, 0, 1]
+    ta.propagate_until(3.0)
+    ts2 = ta.eval_taylor_map([0.0, 0.0])
+    assert getrefcount(ta) == rc + 2
+    assert np.shares_memory(ts, ts2) and np.all(ts2 == np.asarray(ta.state[:2].cpu()))
+    ts2 = ta.eval_taylor_map(np.array([0.0, 0.0]))
+    assert np.shares_memory(ts, ts2) and np.all(ts2 == np.asarray(ta.state[:2].cpu()))
+    with pytest.raises(TypeError, match="Invalid dtype detected for the inputs of a Taylor map evaluation:"):
+        ta.eval_taylor_map(np.array([0.0, 0.0], dtype=np.int32))
+    with pytest.raises(ValueError, match="Invalid inputs array detected in a Taylor map evaluation: the array is not "
+                                         "C-style contiguous, please "):
+        ta.eval_taylor_map(np.array([0.0, 0.0, 0.0, 0.0])[::2])
+    with pytest.raises(ValueError, match="The array of inputs provided for the evaluation of a Taylor map has 2 "
+                                         "dimensions, "):
+        ta.eval_taylor_map(np.array([[0.0, 0.0], [0.0, 0.0]]))
+    with pytest.raises(ValueError, match="The array of inputs provided for the evaluation of a Taylor map has 4 "
+                                         "elements, "):
+        ta.eval_taylor_map(np.array([0.0, 0.0, 0.0, 0.0]))
+    with pytest.raises(ValueError, match="may overlap"):
+        ta.eval_taylor_map(ta.state[:2])
+    with pytest.raises(ValueError, match="may overlap"):
+        ta.eval_taylor_map(ta.tstate)
