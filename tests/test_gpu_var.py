@@ -137,3 +137,17 @@ def test_reference_scalar_variational_integrator():
         ta.eval_taylor_map(ta.state[:2])
     with pytest.raises(ValueError, match="may overlap"):
         ta.eval_taylor_map(ta.tstate)
+
+
+def test_reference_taylor_map_size_check():
+    """heyoka/_test_var_integrator.py test_size_check_bug: the inputs of a
+    Taylor map are sized by the variational arguments (here 3: x, v and the
+    parameter), not by the original state variables."""
+    x, v = hyk.make_vars("x", "v")
+    orig_sys = [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
+    vsys = hyk.var_ode_sys(orig_sys, hyk.var_args.vars | hyk.var_args.params, order=2)
+    ta = hyk.taylor_adaptive(vsys, [0.2, 0.3], pars=[0.4], time=0.5, compact_mode=True)
+    assert np.all(ta.state[:2] == ta.eval_taylor_map([0.0, 0.0, 0.0]))
+    ta = hyk.taylor_adaptive_batch(vsys, [[0.2, 0.21], [0.3, 0.31]], pars=[[0.4, 0.41]], time=[0.5, 0.51],
+                                   compact_mode=True)
+    assert np.all(ta.state[:2] == ta.eval_taylor_map([[0.0, 0.0], [0.0, 0.0], [0.0, 0.0]]))
