@@ -197,6 +197,8 @@ class LaneArray(torch.Tensor):
         if isinstance(value, torch.Tensor):
             return value.to(device=self.device, dtype=self.dtype)
         a = _to_fp_array(value, "value", np.float32 if self.dtype == torch.float32 else np.float64)
+        if not a.flags.writeable:  # a read-only view (tstate, d_output, ...): torch wants its own copy
+            a = a.copy()
         return torch.as_tensor(a, device=self.device)
 
     def __setitem__(self, idx, value):
