@@ -283,8 +283,10 @@ int hyk_prop_init(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int mode);
 
 /* Advance every unfinished lane until it is done or stopped.
- * PLAIN mode launches one step kernel per iteration and reads one word back
- * every `check_every` launches to detect completion (synchronises `stream`).
+ * PLAIN mode launches one step kernel per iteration (with a large enough
+ * workspace, over a list of the unfinished lanes made before each launch)
+ * and reads one word back every `check_every` launches to detect completion
+ * (synchronises `stream`).
  * PERSISTENT mode runs one persistent launch.  `workspace` is device memory
  * of hyk_propagate_workspace_size() bytes.  On return, `*iters` (may be NULL)
  * holds the number of step launches made (PLAIN) or 1 (PERSISTENT). */
