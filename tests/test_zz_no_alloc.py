@@ -74,13 +74,19 @@ def _propagate(L, mod, st, tf, dev, noalloc, mode):
     return results
 
 
+@pytest.mark.parametrize("n", [300, 5000])
 @pytest.mark.parametrize("mode", [_lib.HYK_MODE_PERSISTENT, _lib.HYK_MODE_PLAIN])
-def test_noalloc_matches_workspace_entry_point(libhyk, mode):
+def test_noalloc_matches_workspace_entry_point(libhyk, mode, n):
+    """With 300 lanes the plain form's lane list fits the no-allocation scratch
+    (it steps the listed unfinished lanes); with 5000 it steps the lanes in
+    place, as the 256-byte workspace of the other entry point makes it do."""
     assert torch.cuda.is_available(), "this test needs a CUDA device"
     dev = torch.device("cuda", 0)
     dec = taylor_decompose(W.kepler_sys())
     mod = get_module(dec, order_from_tol(1e-15), 0)
-    st = W.kepler_ics(5000, seed=21)
+    assert int(libhyk.hyk_propagate_workspace_size(mod.handle, n, _lib.HYK_MODE_PLAIN)) == 256 + 8 * n
+    assert int(libhyk.hyk_propagate_workspace_size(mod.handle, n, _lib.HYK_MODE_PERSISTENT)) == 256
+    st = W.kepler_ics(n, seed=21)
     ref = _propagate(libhyk, mod, st, 6.0, dev, noalloc=False, mode=mode)
     got = _propagate(libhyk, mod, st, 6.0, dev, noalloc=True, mode=mode)
     for (s0, t0, a0), (s1, t1, a1) in zip(ref, got):
