@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="kepler", choices=["kepler", "kepler-f32", "serve", "pendulum", "cr3bp-adjoint", "oss", "forms",
-                             "occupancy"],
+                             "occupancy", "plain"],
                     help="kepler: the headline metric; serve: the Poisson request stream (p50/p99 latency); "
                          "pendulum: 4096 trajectories through ensemble_propagate_until; "
                          "cr3bp-adjoint: 65536 trajectories forward plus discrete adjoint")
@@ -646,6 +646,42 @@ def run_forms(args):
                   flush=True)
 
 
+def run_plain(args):
+    """The plain form (one launch per step, over the unfinished lanes listed
+    before each launch) against the persistent kernel, in each system's
+    default kernel form: 2^20 Kepler orbits to t = 20, 65536 CR3BP
+    trajectories to t = 50 and 65536 outer-solar-system members to end times
+    log-uniform in [1e3, 1e5] days; best of two calls, one JSON line per
+    (system, mode)."""
+    import torch
+
+    import hyk
+    from hyk import workloads as W
+
+    cr_st, cr_mu = W.cr3bp_ics(65536, seed=3)
+    oss_st, oss_t = W.oss_ics(65536, seed=2)
+    cases = [("kepler", W.kepler_sys(), W.kepler_ics(1 << 20, seed=1), None, 20.0),
+             ("cr3bp", W.cr3bp_sys(), cr_st, cr_mu, 50.0),
+             ("oss", W.oss_sys(), oss_st, None, oss_t)]
+    for name, sys_, st, pars, tf in cases:
+        for mode in ("persistent", "plain"):
+            ta = hyk.taylor_adaptive_batch(sys_, st, pars=pars, tol=TOL, prop_mode=mode)
+            info = ta.module_info
+            best = 1e30
+            for _ in range(2):
+                ta.set_time(0.0)
+                ta.state[:] = st
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                ta.propagate_until(tf)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            steps = int(ta.propagate_res_tensors["n_steps"].sum().item())
+            print(json.dumps({"system": name, "mode": mode, "team_size": info["team_size"],
+                              "jets": "global" if info["smem_per_lane"] == 0 else "shared", "s": best,
+                              "trajectory_steps": steps, "trajectory_steps_per_s": steps / best}), flush=True)
+
+
 def run_occupancy(args):
     """Lane form with its coefficients in shared memory at every block size
     from 32 to 256 lanes: 2^18 Kepler orbits propagated from t = 0 to 20, at
@@ -693,7 +729,8 @@ def main():
     if args.workload != "kepler":
         if rank == 0:
             {"serve": run_serve, "pendulum": run_pendulum, "cr3bp-adjoint": run_cr3bp_adjoint, "oss": run_oss,
-             "forms": run_forms, "kepler-f32": run_kepler_f32, "occupancy": run_occupancy}[args.workload](args)
+             "forms": run_forms, "kepler-f32": run_kepler_f32, "occupancy": run_occupancy,
+             "plain": run_plain}[args.workload](args)
         return
     import numpy as np
     import torch
