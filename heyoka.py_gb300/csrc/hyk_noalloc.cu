@@ -44,6 +44,9 @@ extern "C" __attribute__((visibility("hidden"))) int hyk_noalloc_scratch(int dev
         const cudaError_t e = cudaGetSymbolAddress(&p, g_hyk_noalloc_scratch);
         if (e != cudaSuccess) {
             std::snprintf(err, errlen, "cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+            // Clear the runtime's sticky last error, so that a later runtime
+            // call of this library does not report this failure as its own.
+            (void)cudaGetLastError();
             return -2;
         }
         g_addr[device] = p;

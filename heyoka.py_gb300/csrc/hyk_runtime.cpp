@@ -579,12 +579,37 @@ struct LaunchSpec {
     size_t smem;
 };
 
-static int build_graph(hyk_module *m, const std::vector<LaunchSpec> &chain, KParams &k, LaunchGraph &lg) {
+// The launches of one round of the plain propagation after the round's first
+// listing: with a lane list, [step, (zero, list, step) x (per_round - 1)];
+// without one, per_round step launches.  Generated on demand (no container),
+// so the direct-launch path keeps no heap storage.
+struct PlainRound {
+    bool compact;
+    uint32_t per_round;
+    uint64_t grid, lgrid;
+    uint32_t size() const { return compact ? 1 + 3 * (per_round - 1) : per_round; }
+    LaunchSpec at(const hyk_module *m, uint32_t i) const {
+        if (compact && i > 0) {
+            switch ((i - 1) % 3) {
+            case 0:
+                return {m->f_azero, 1, 32, 0};
+            case 1:
+                return {m->f_alist, lgrid, 256, 0};
+            default:
+                break;
+            }
+        }
+        return {m->f_prop, grid, m->blk, m->smem};
+    }
+};
+
+static int build_graph(hyk_module *m, const PlainRound &round, KParams &k, LaunchGraph &lg) {
     k.jets = reinterpret_cast<double *>(m->jets);
     HYK_CU(drv().cuGraphCreate(&lg.g, 0));
     void *args[] = {&k};
     CUgraphNode prev = nullptr;
-    for (const LaunchSpec &ls : chain) {
+    for (uint32_t i = 0; i < round.size(); ++i) {
+        const LaunchSpec ls = round.at(m, i);
         const uint64_t grid = launch_grid(m, ls.f, ls.grid);
         if (grid == 0 || grid > 0x7fffffffULL) return fail(HYK_ERR_INVALID, "too many lanes for one launch");
         CUDA_KERNEL_NODE_PARAMS np;
@@ -707,8 +732,12 @@ size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int m
     return kWsCounters;
 }
 
-int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
-                  size_t workspace_bytes, uint32_t check_every, uint64_t *iters, void *stream) {
+// hyk_propagate and hyk_propagate_noalloc.  use_graphs: the plain form
+// replays its rounds as a CUDA graph (hyk_propagate); without it every
+// launch is made directly, so that nothing is created or instantiated
+// (hyk_propagate_noalloc, whose callers must not allocate).
+static int propagate_impl(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
+                          size_t workspace_bytes, uint32_t check_every, uint64_t *iters, void *stream, bool use_graphs) {
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (iters) *iters = 0;
@@ -742,40 +771,32 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     // reads from device memory), so warps are not left half idle by lanes
     // that finished; the word read back is the list's length.  Without it,
     // every launch covers all lanes and the word is the number of finished
-    // lanes.  From the second round on, a round's launches are one CUDA graph
-    // (built once per call and replayed: the launch parameters do not change).
+    // lanes.  With use_graphs, from the second round on a round's launches are
+    // one CUDA graph (built once per call and replayed: the launch parameters
+    // do not change); otherwise every launch is made directly.
     if (check_every == 0) check_every = 16;
     k.persistent = 0;
     k.iters_per_launch = 1;
     const bool compact = plain_compacts(m, lanes->n_lanes, workspace_bytes);
     uint64_t grid = lane_blocks(m, lanes->n_lanes);
-    std::vector<LaunchSpec> round_chain;  // the launches of one round after its first listing
+    PlainRound chain{compact, check_every, grid, std::min<uint64_t>(4096, (lanes->n_lanes + 255) / 256)};
     if (compact) {
         k.lane_order = reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(workspace) + kWsCounters);
         k.n_order = 0;
         k.act_count = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(workspace) + 12);
-        grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm);
-        const uint64_t lgrid = std::min<uint64_t>(4096, (lanes->n_lanes + 255) / 256);
-        for (uint32_t c = 0; c < check_every; ++c) {
-            if (c) {
-                round_chain.push_back({m->f_azero, 1, 32, 0});
-                round_chain.push_back({m->f_alist, lgrid, 256, 0});
-            }
-            round_chain.push_back({m->f_prop, grid, m->blk, m->smem});
-        }
+        chain.grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm);
     } else {
         rc = hyk_generic_count_finished(p->status, lanes->n_lanes, k.finished, stream);
         if (rc) return rc;
-        for (uint32_t c = 0; c < check_every; ++c) round_chain.push_back({m->f_prop, grid, m->blk, m->smem});
     }
     uint64_t n = 0;
     uint32_t word = 0;
-    const bool graphs = check_every > 1 && !std::getenv("HYK_PLAIN_NO_GRAPH");
+    const bool graphs = use_graphs && check_every > 1;
     LaunchGraph lg;
-    for (uint64_t round = 0;; ++round) {
+    for (uint64_t r = 0;; ++r) {
         if (compact) {
             rc = launch(m, m->f_azero, 1, 32, 0, k, stream);
-            if (!rc) rc = launch(m, m->f_alist, std::min<uint64_t>(4096, (lanes->n_lanes + 255) / 256), 256, 0, k, stream);
+            if (!rc) rc = launch(m, m->f_alist, chain.lgrid, 256, 0, k, stream);
             if (rc) return rc;
             HYK_CU(drv().cuMemcpyDtoHAsync(&word, (CUdeviceptr)k.act_count, sizeof word, s));
             HYK_CU(drv().cuStreamSynchronize(s));
@@ -785,16 +806,17 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
             HYK_CU(drv().cuStreamSynchronize(s));
             if ((uint64_t)word >= lanes->n_lanes) break;
         }
-        if (graphs && round >= 1) {
+        if (graphs && r >= 1) {
             if (!lg.x) {
-                rc = build_graph(m, round_chain, k, lg);
+                rc = build_graph(m, chain, k, lg);
                 if (rc) return rc;
             }
             HYK_CU(drv().cuGraphLaunch(lg.x, s));
             n += check_every;
             continue;
         }
-        for (const LaunchSpec &ls : round_chain) {
+        for (uint32_t i = 0; i < chain.size(); ++i) {
+            const LaunchSpec ls = chain.at(m, i);
             rc = launch(m, ls.f, ls.grid, ls.blk, ls.smem, k, stream);
             if (rc) return rc;
             if (ls.f == m->f_prop) ++n;
@@ -804,11 +826,17 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
     return 0;
 }
 
+int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
+                  size_t workspace_bytes, uint32_t check_every, uint64_t *iters, void *stream) {
+    return propagate_impl(m, lanes, p, mode, workspace, workspace_bytes, check_every, iters, stream, true);
+}
+
 // Propagation without a caller workspace: the counters hyk_propagate keeps in
 // its workspace come from libhyk's file-scope device scratch array
 // (hyk_noalloc.cu).  Nothing here allocates: the scratch address is looked up
-// once per device, the counters are cleared by hyk_propagate itself at the
-// start of every call, and the rest is hyk_propagate unchanged.
+// once per device, the counters are cleared at the start of every call, and
+// the plain form launches every kernel directly (no CUDA graph is created or
+// instantiated, no host container is filled).
 int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, uint32_t check_every,
                           uint64_t *iters, void *stream) {
     if (!m) return fail(HYK_ERR_INVALID, "null module");
@@ -821,7 +849,7 @@ int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
     // batch is small enough, and the plain form steps the lanes in place
     // otherwise.
     if (kWsCounters > cap) return fail(HYK_ERR_INVALID, "hyk_propagate_noalloc: the scratch array is too small");
-    return hyk_propagate(m, lanes, p, mode, ws, cap, check_every, iters, stream);
+    return propagate_impl(m, lanes, p, mode, ws, cap, check_every, iters, stream, false);
 }
 
 int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,

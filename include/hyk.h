@@ -308,8 +308,12 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
  * first call before any stream capture.  Every call clears the counters it
  * needs before using them, so a call never sees the previous call's values,
  * but all calls share the one array: calls that overlap on the GPU (other
- * streams, other threads) race and give wrong results.  It allocates nothing
- * and calls no allocating CUDA or library routine. */
+ * streams, other threads) race and give wrong results.  It allocates no
+ * device memory and calls no allocating CUDA or library routine: the PLAIN
+ * mode makes every launch directly (hyk_propagate replays its rounds as a
+ * CUDA graph, which this entry point never creates or instantiates), and on
+ * success no host memory is allocated either (an error message is the only
+ * host allocation). */
 #define HYK_NOALLOC_SCRATCH_BYTES 4096
 int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode,
                           uint32_t check_every, uint64_t *iters, void *stream);

@@ -328,7 +328,7 @@ def test_pin_arithmetic_module_close_to_oracle_pin(oracle):
     o = oracle.Oracle(sys_, st, order=ta.order, mode=0)
     r = o.propagate_until(tf)
     rel = np.max(np.abs(np.asarray(ta.state) - o.state), axis=0) / np.max(np.abs(o.state), axis=0)
-    assert rel.max() < 1e-11
+    assert rel.max() <= 1e-12
     assert np.mean(res_arrays(ta)["n_steps"] == r["n_steps"]) >= 0.99
 
 

@@ -8,6 +8,8 @@ the reference's exact operation order, which is not observable, moves the
 last bits), printed 8-digit states exactly.
 """
 
+import os
+
 import numpy as np
 import pytest
 
@@ -225,7 +227,7 @@ def test_non_finite_state(oracle):
 
 
 def test_quad_reference_error_kepler(oracle):
-    """Error of the double-precision run against a binary128 run at tol 1e-32."""
+    """Error of the double-precision runs against a binary128 run at tol 1e-32."""
     from hyk import workloads as W
 
     st = W.kepler_ics(8)
@@ -234,6 +236,30 @@ def test_quad_reference_error_kepler(oracle):
     d.propagate_until(10.0)
     q.propagate_until(10.0)
     assert np.max(traj_rel_err(d.state, q.state)) < 1e-12
+
+
+def test_binary128_fixture_kepler_benchmark_orbits(oracle):
+    """The binary128 states of 1024 benchmark orbits (tests/golden/
+    kepler_t200_quad_1024.npz, made by make_kepler_quad.py): a re-run of the
+    first 16 at tol 1e-28 (order 33) agrees with them to 1e-15 at t = 50 and
+    t = 200, and
+    on the first 256 orbits the gpu and the reference (pin) arithmetic are
+    equally far from them at t = 200 (the fixture's use in the GPU tests)."""
+    from hyk import workloads as W
+
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "kepler_t200_quad_1024.npz"))
+    st = np.ascontiguousarray(W.kepler_ics(1 << 20, seed=1)[:, fx["idx"]])
+    q = oracle.Oracle(W.kepler_sys(), st[:, :16], order=order_from_tol(1e-28), prec=1, mode=0)
+    for t in (50.0, 200.0):
+        q.propagate_until(t)
+        assert np.max(traj_rel_err(q.state, fx["state_t{:g}".format(t)][:, :16])) <= 1e-15
+    err = {}
+    for mode in (0, 1):
+        o = oracle.Oracle(W.kepler_sys(), st[:, :256], order=19, mode=mode)
+        o.propagate_until(200.0)
+        err[mode] = traj_rel_err(o.state, fx["state_t200"][:, :256])
+    assert err[1].max() <= 1.5 * err[0].max() and np.median(err[1]) <= 1.25 * np.median(err[0])
+    assert err[0].max() > 1e-12  # the reference arithmetic's own error at this horizon
 
 
 def test_high_accuracy_oracle_close_to_quad(oracle):

@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 import hyk
+import systems
 from hyk import _lib, workloads as W
 from hyk.decompose import taylor_decompose
 
@@ -37,32 +38,15 @@ def _team_host(libhyk, sys_, order, team=2):
 
 
 def _mixed():
-    x, y = hyk.make_vars("x", "y")
-    t, p = hyk.time, hyk.par
-    return [
-        (x, hyk.exp(-y) * hyk.log(x) + hyk.sqrt(y) / x + hyk.cos(t) * p[1] + p[0] / y + x * t + 0.5 * t),
-        (y, p[0] / (x + 2.0) - x**-1.5 * p[1] + hyk.sin(x) * y + hyk.square(x - y) + t * y - (3.0 - x)
-         + hyk.exp(t) * 1e-3 + y**2.5 + (x - t) / 7.0 + 2.0 - t),
-    ]
+    return systems.mixed()
 
 
 def _consts():
-    # time-constant operations (only an order-0 value) feeding every kind of operation
-    x, y = hyk.make_vars("x", "y")
-    p = hyk.par
-    c1, c2 = 1.0 - p[0], hyk.exp(p[1])
-    return [
-        (x, c1 * y + c2 * hyk.sin(x) + hyk.sqrt(p[0] + 2.0) - (p[0] * 3.0) / (x + 4.0) + y / (p[1] + 1.0)),
-        (y, -x * hyk.sin(p[1]) + hyk.cos(p[0] * x) + (c1 - y) ** 2.0 + hyk.log(c2 + x * x) - c1),
-    ]
+    return systems.consts()
 
 
 def _var2():
-    from hyk import var
-
-    x, v = hyk.make_vars("x", "v")
-    orig = [(x, v), (v, hyk.cos(hyk.time) - hyk.par[0] * v - hyk.sin(x))]
-    return var.var_ode_sys(orig, var.var_args.vars | var.var_args.params, order=2)
+    return systems.var2()
 
 
 CASES = {

@@ -95,3 +95,23 @@ def test_noalloc_matches_workspace_entry_point(libhyk, mode, n):
         for k in ("n_steps", "n_iter", "min_h", "max_h", "outcome", "status"):
             assert np.array_equal(a0[k], a1[k]), k
         assert np.all(a1["n_steps"] > 0)
+
+
+def test_noalloc_scratch_per_device(libhyk):
+    """Every GPU that loads the library holds its own copy of the scratch
+    array, and its address is looked up on that device.  With two GPUs, a
+    call on device 1 after one on device 0 must still reproduce hyk_propagate
+    on both (a device-0 address used on device 1 would not)."""
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two visible GPUs")
+    dec = taylor_decompose(W.kepler_sys())
+    st = W.kepler_ics(300, seed=22)
+    for ordinal in (0, 1):
+        dev = torch.device("cuda", ordinal)
+        mod = get_module(dec, order_from_tol(1e-15), ordinal)
+        for mode in (_lib.HYK_MODE_PERSISTENT, _lib.HYK_MODE_PLAIN):
+            ref = _propagate(libhyk, mod, st, 6.0, dev, noalloc=False, mode=mode)
+            got = _propagate(libhyk, mod, st, 6.0, dev, noalloc=True, mode=mode)
+            for (s0, t0, a0), (s1, t1, a1) in zip(ref, got):
+                assert np.array_equal(s0, s1) and np.array_equal(t0, t1)
+                assert np.array_equal(a0["n_steps"], a1["n_steps"])
