@@ -1889,4 +1889,35 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
     return true;
 }
 
+// Recurrences of one system in the reference's arithmetic (no fused
+// multiply-adds, true divisions, the C library's elementary functions) over
+// an element type chosen by the including translation unit: `hyk_real` may
+// be a vector of lanes (GCC vector extension), in which case every operation
+// acts on a batch of trajectories at once and the includer provides the
+// element-wise pow/exp/log/sqrt/sincos for that type.  This is the per-system
+// part of the compiled CPU stepper that stands in for the reference's
+// LLVM-compiled batch stepper in timing comparisons; nothing on the GPU path
+// uses it.
+bool generate_host_batch(const Dec &d, uint32_t order, std::string &src, std::string &err) {
+    PrecisionScope ps(false);
+    if (order < 2) {
+        err = "the Taylor order must be at least 2";
+        return false;
+    }
+    if (!d.ev.empty()) {
+        err = "the compiled CPU stepper does not support events";
+        return false;
+    }
+    Gen g(d, order, true, false);
+    std::ostringstream h;
+    h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
+      << "\n#define HYK_STRIDE 1\n#define HYK_NSLOT " << g.nslot << "\n#define HYK_PAR_SLOT " << g.par_slot << "\n";
+    h << "#define HYK_SX(i, n) S[((i) * (HYK_ORDER + 1) + (n)) * HYK_STRIDE]\n#define HYK_PAR(k) S[(HYK_PAR_SLOT + (k)) * HYK_STRIDE]\n";
+    g.emit_jets();
+    h << g.o.str();
+    h << "#define HYK_FLOPS_PER_STEP " << lit(g.flops) << "\n";
+    src = h.str();
+    return true;
+}
+
 }  // namespace hyk

@@ -56,4 +56,8 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
 bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team = false,
                    bool f32 = false);
 
+// The recurrences in the reference's arithmetic over an element type chosen
+// by the includer (a vector of lanes for the compiled CPU stepper).
+bool generate_host_batch(const Dec &d, uint32_t order, std::string &src, std::string &err);
+
 }  // namespace hyk

@@ -912,6 +912,13 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     // slot stride of a 152-SM grid.
     const uint32_t team = cfg ? cfg->team_size : 0;
     const bool f32 = cfg && (cfg->flags & HYK_CFG_FLOAT32);
+    if (verbose == 4) {  // recurrences for the compiled CPU stepper (reference arithmetic, any element type)
+        std::string hs;
+        if (!hyk::generate_host_batch(d, order, hs, err)) return fail(HYK_ERR_UNSUPPORTED, err);
+        if (hs.size() + 1 > log_len || !log) return fail(HYK_ERR_INVALID, "log buffer too small for the generated source");
+        std::snprintf(log, log_len, "%s", hs.c_str());
+        return 0;
+    }
     if (team > 1 && verbose == 3) {  // host translation unit of the team form
         std::string hs;
         if (!hyk::generate_host(d, order, false, hs, err, true, f32)) return fail(HYK_ERR_UNSUPPORTED, err);

@@ -363,8 +363,11 @@ int hyk_fp32_peak(int device, double millis, double *flops_per_s);
  * sm_103a.  `log` receives the NVRTC log (ptxas register and spill
  * statistics when `verbose` is 1; the generated source, without compiling,
  * when `verbose` is 2; a host C++ translation unit of the same recurrences,
- * for CPU checks, when `verbose` is 3); `n_slot` the shared-memory doubles
- * per lane, `flops` the algorithmic flops per step. */
+ * for CPU checks, when `verbose` is 3; the recurrences in the reference's
+ * arithmetic over an element type the includer defines, the per-system part
+ * of the compiled CPU stepper used as a timing baseline, when `verbose` is
+ * 4); `n_slot` the shared-memory doubles per lane, `flops` the algorithmic
+ * flops per step. */
 int hyk_codegen_check(const hyk_decomp_t *d, uint32_t order, const hyk_config_t *cfg, int verbose, char *log,
                       size_t log_len, uint32_t *n_slot, double *flops);
 
