@@ -267,9 +267,23 @@ struct Gen {
     // the pinned arithmetic and the adjoint keep the full recurrences.
     std::vector<char> cst;
 
-    Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false)
+    // Cold state rows (coldrows mode): a state variable whose coefficients no
+    // recurrence reads at a later order (it enters the right-hand sides only
+    // through sums and differences, or not at all: the velocities of
+    // Kepler, N-body and CR3BP) is read again only by the step size, the
+    // state update and the coefficient outputs.  Its orders 1..p then live
+    // in a global buffer of the module (row crow[i], slot crow[i] * p + n - 1,
+    // slot stride HYK_CSTRIDE), and only its order 0 in shared memory, so
+    // that more lanes fit the shared memory of an SM.
+    bool coldrows = false;
+    std::vector<int> crow;
+    std::vector<char> hread;
+    uint32_t ncold = 0;
+
+    Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false, bool cold_rows = false)
         : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint),
           split((uint64_t)dd.n_ops * order > 3000), evx(!dd.ev.empty()) {
+        coldrows = cold_rows && !adjoint && !evx;
         base.resize(NU);
         negf.assign(NU, 0);
         alias.assign(NU, 0);
@@ -312,6 +326,7 @@ struct Gen {
     void analyse() {
         hist.assign(NU, 0);
         needka.assign(NU, 0);
+        hread.assign(NU, 0);
         for (uint32_t i = 0; i < N; ++i) hist[i] = 1;
         for (uint32_t k = 0; k < d.n_ops; ++k) {
             const uint32_t u = N + k;
@@ -319,7 +334,7 @@ struct Gen {
             const auto &op = d.ops[k];
             const Ref A = res(op.a), B = res(op.b);
             auto H = [&](const Ref &r) {
-                if (r.kind == HYK_ARG_U) hist[r.u] = 1;
+                if (r.kind == HYK_ARG_U) hist[r.u] = hread[r.u] = 1;
             };
             auto K = [&](const Ref &r) {
                 if (r.kind == HYK_ARG_U && !cst[r.u]) needka[r.u] = 1;
@@ -386,10 +401,17 @@ struct Gen {
         // then the parameters.
         slot.assign(NU, -1);
         kslot.assign(NU, -1);
+        crow.assign(N, -1);
+        ncold = 0;
         uint32_t s = 0;
         for (uint32_t i = 0; i < N; ++i) {
             slot[i] = (int)s;
-            s += p + 1;
+            if (coldrows && !hread[i]) {
+                crow[i] = (int)ncold++;
+                s += 1;  // order 0 only
+            } else {
+                s += p + 1;
+            }
         }
         // The adjoint module keeps every history up to order p-1.
         const bool ext = adj || evx;
@@ -463,7 +485,7 @@ struct Gen {
     // Coefficient of order j of u-variable u (not an alias) while emitting block n.
     std::string ucoef(uint32_t u, uint32_t j, uint32_t n) const {
         if (j == n) return vname(u, j);
-        if (!hist[u] || slot[u] < 0) {
+        if (!hist[u] || slot[u] < 0 || (u < N && crow[u] >= 0 && j > 0)) {
             std::fprintf(stderr, "hyk codegen: missing history for u%u\n", u);
             std::abort();
         }
@@ -765,18 +787,49 @@ struct Gen {
         }
     }
 
+    // State variable i, order n in the jets code: shared memory, or for a
+    // cold row (n >= 1) the module's global buffer.
+    std::string sx(uint32_t i, uint32_t n) const {
+        if (coldrows && crow[i] >= 0 && n > 0)
+            return "HYK_CX(" + std::to_string(crow[i] * p + n - 1) + ")";
+        return "HYK_SX(" + std::to_string(i) + ", " + std::to_string(n) + ")";
+    }
+
+    // The template's access to state coefficients (HYK_SX): a function of
+    // the variable and the order that knows each variable's place.
+    void emit_sx_access(std::ostream &h) const {
+        if (!coldrows) return;
+        h << "#define HYK_COLDROWS 1\n#define HYK_NCOLD " << ncold << "\n";
+        h << "extern \"C\" { __constant__ hyk_real *hyk_cold_base; }\n";
+        h << "#define HYK_CX(k) hyk_cold_g[(hyk_u64)(k) * HYK_CSTRIDE]\n";
+        h << "static __device__ __forceinline__ hyk_real *hyk_cold_ptr() {\n"
+             "    return hyk_cold_base + ((hyk_u64)blockIdx.x * HYK_TPB + threadIdx.x);\n}\n";
+        h << "template <typename R>\nstatic __device__ __forceinline__ R *hyk_sxp(R *S, int i, int n) {\n    switch (i) {\n";
+        for (uint32_t i = 0; i < N; ++i) {
+            h << "    case " << i << ": return ";
+            if (crow[i] >= 0)
+                h << "n == 0 ? S + " << slot[i] << " * HYK_STRIDE : hyk_cold_ptr() + (hyk_u64)(" << crow[i] * p
+                  << " + n - 1) * HYK_CSTRIDE;\n";
+            else
+                h << "S + (" << slot[i] << " + n) * HYK_STRIDE;\n";
+        }
+        h << "    default: return S;\n    }\n}\n";
+        h << "#define HYK_SX(i, n) (*hyk_sxp(S, (i), (n)))\n";
+    }
+
     void emit_jets() {
+        const char *coldg = coldrows ? "    hyk_real *__restrict__ hyk_cold_g = hyk_cold_ptr();\n" : "";
         if (!split) {
-            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n";
+            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n" << coldg;
             for (uint32_t i = 0; i < N; ++i) o << "    const hyk_real " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
         }
         const uint32_t last = evx ? p : p - 1;  // order p: the event functions' cone only
         for (uint32_t n = 0; n <= last; ++n) {
             if (split) {
                 o << "static __device__ __noinline__ void hyk_jets_o" << n
-                  << "(hyk_real *__restrict__ S, const hyk_real t0) {\n";
+                  << "(hyk_real *__restrict__ S, const hyk_real t0) {\n" << coldg;
                 for (uint32_t i = 0; i < N; ++i) {
-                    o << "    const hyk_real " << vname(i, n) << " = HYK_SX(" << i << ", " << n << ");\n";
+                    o << "    const hyk_real " << vname(i, n) << " = " << sx(i, n) << ";\n";
                     // The same product the previous order formed (k_i_0 is never read).
                     if (needka[i] && n >= 1)
                         o << "    const hyk_real " << kname(i, n) << " = " << lit((double)n) << " * " << vname(i, n)
@@ -805,7 +858,7 @@ struct Gen {
                 const Ref r = res(d.rhs[i]);
                 const std::string f = cf(r, n, n);
                 def(i, n + 1, f.empty() ? lit(0.0) : divn(f, n + 1));
-                o << "    HYK_SX(" << i << ", " << (n + 1) << ") = " << vname(i, n + 1) << ";\n";
+                o << "    " << sx(i, n + 1) << " = " << vname(i, n + 1) << ";\n";
                 if (needka[i]) {
                     o << "    const hyk_real " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
                       << vname(i, n + 1) << ";\n";
@@ -1666,8 +1719,9 @@ const char *kEvents =
 
 }  // namespace
 
-uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin) {
-    Gen g(d, order, pin, adjoint);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin, bool cold_rows, uint32_t *n_cold) {
+    Gen g(d, order, pin, adjoint, cold_rows);
+    if (n_cold) *n_cold = g.ncold;
     return g.nslot;
 }
 
@@ -1677,7 +1731,7 @@ struct PrecisionScope {
 };
 
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc, bool f32) {
+              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc, bool f32, uint64_t cold_stride) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1687,7 +1741,7 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
         return false;
     }
     PrecisionScope prec(f32);
-    Gen g(d, order, pin_arith, adjoint);
+    Gen g(d, order, pin_arith, adjoint, cold_stride != 0 && gmem_stride == 0);
     const double p = (double)order;
     const double rhofac = rhofac_of(order);
     std::ostringstream h;
@@ -1710,8 +1764,10 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     }
     if (adjoint) h << "#define HYK_ADJOINT 1\n";
     h << "#define HYK_HIGH_ACC " << (high_acc ? 1 : 0) << "\n";
+    if (g.coldrows) h << "#define HYK_CSTRIDE " << cold_stride << "ULL\n";
     h << kDmath << "\n";
     h << kCommon << "\n";
+    g.emit_sx_access(h);
     g.emit_events(h);
     if (!d.ev.empty()) h << kEvents << "\n";
     h << kTemplate << "\n";
@@ -1732,6 +1788,7 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
     full.insert(pos, body + "\n");
     out.src = std::move(full);
     out.n_slot = g.nslot;
+    out.n_cold = g.coldrows ? g.ncold : 0;
     out.par_slot = g.par_slot;
     // Per-step flops: recurrences + Horner (2 per coefficient) + step size
     // (two pow and the norm arithmetic) + double-length time update.

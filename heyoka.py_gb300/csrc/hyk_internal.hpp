@@ -25,20 +25,26 @@ struct GenOut {
     std::string src;          // complete NVRTC translation unit
     uint32_t n_slot = 0;      // shared-memory doubles per lane
     uint32_t par_slot = 0;    // first parameter slot
+    uint32_t n_cold = 0;      // cold state rows (orders 1..p in the module's global buffer)
     double flops = 0;         // algorithmic FP64 flops per step per lane
 };
 
 // Shared-memory slots per lane for a decomposition at a given order (the
 // block size does not change it).
-uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pin = false);
+// cold_rows: the layout with cold state rows (their orders 1..p in a global
+// buffer, only order 0 in shared memory); *n_cold receives their number.
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pin = false, bool cold_rows = false,
+                     uint32_t *n_cold = nullptr);
 
 // adjoint: also emit the reverse sweep hyk_jets_bw() and the adjoint kernel
 // (and keep every history up to order p-1 for it).
 // gmem_stride != 0: Taylor coefficients in a global-memory buffer with that
 // slot stride (the number of threads of the fixed grid) instead of shared memory.
+// cold_stride != 0: the cold-state-row layout, the global rows with that slot
+// stride (the number of threads of the fixed grid).
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
               std::string &err, bool adjoint = false, uint64_t gmem_stride = 0, bool high_acc = false,
-              bool f32 = false);
+              bool f32 = false, uint64_t cold_stride = 0);
 
 // Team form (several threads per trajectory): slot count and the share of
 // busy threads over the rounds of one order for teams of 1, 2, 4, ..., 32.

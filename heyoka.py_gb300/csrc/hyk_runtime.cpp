@@ -48,7 +48,7 @@ thread_local std::string g_err;
 // driver entry point goes through this table.
 #define HYK_STR2(x) #x
 #define HYK_STR(x) HYK_STR2(x)
-#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy) X(cuModuleGetGlobal) X(cuMemcpyHtoD)
 
 struct DriverApi {
 #define HYK_DECL(f) decltype(&::f) f = nullptr;
@@ -140,6 +140,8 @@ struct KParams {
     uint64_t ev_cap;
     double *ev_last;
     int32_t *ev_sign;
+    uint64_t *stop_iter;
+    uint64_t stop_group;
     int persistent;
 };
 
@@ -236,6 +238,9 @@ struct hyk_module {
     bool f32 = false;            // single precision
     bool gmem = false;           // Taylor coefficients in a global buffer (large systems)
     uint64_t gmem_threads = 0;   // threads of the fixed grid in that mode
+    uint32_t ncold = 0;          // cold state rows in the global buffer (0: none)
+    uint64_t cold_threads = 0;   // threads of the fixed grid the cold rows are sized for
+    int cold_ctas = 0;           // CTAs per SM of that grid
     CUdeviceptr jets = 0;        // the module's coefficient buffer (gmem mode)
     std::string src, log;
     uint32_t blk = 0, nslot = 0;
@@ -352,33 +357,76 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (blk == 0) blk = 128;
         const uint32_t ctas = m->cfg.persist_ctas ? m->cfg.persist_ctas : (blk <= 128 ? 2 : 1);
         m->gmem_threads = (uint64_t)dv.n_sm * ctas * blk;
-    } else if (blk == 0) {
+    } else {
         // Pick the block size maximising resident lanes per SM under the
         // shared-memory budget (1 KiB per CTA is reserved by the hardware),
         // capped at 256 per CTA and at 512 lanes per SM in double precision
         // (the FP64 pipe saturates with far fewer warps) or 768 in single
         // precision (more warps hide the dependent-issue latency of the
         // FP32 pipe).
+        // The double-precision lane kernels use (nearly) all 255 registers a
+        // thread can have, so at most 256 threads share an SM's 64K registers.
         const uint32_t lane_cap = f32 ? 768u : 512u;
+        const uint32_t reg_threads = f32 ? 1024u : 256u;
+        auto pick = [&](size_t lbytes, uint32_t &b_out, uint32_t &lanes_out) {
+            b_out = 0;
+            lanes_out = 0;
+            for (uint32_t b = 32; b <= 256; b += 32) {
+                const size_t per_cta = b * lbytes;
+                if (per_cta > (size_t)dv.smem_optin) break;
+                uint32_t ctas = (uint32_t)((size_t)dv.smem_per_sm / (per_cta + 1024));
+                ctas = std::min(ctas, reg_threads / b);
+                uint32_t lanes = std::min<uint32_t>(ctas * b, lane_cap);
+                if (lanes >= lanes_out) {
+                    lanes_out = lanes;
+                    b_out = b;
+                }
+            }
+        };
         uint32_t best = 0, best_lanes = 0;
-        for (uint32_t b = 32; b <= 256; b += 32) {
-            const size_t per_cta = b * lane_bytes;
-            if (per_cta > (size_t)dv.smem_optin) break;
-            uint32_t ctas = (uint32_t)((size_t)dv.smem_per_sm / (per_cta + 1024));
-            uint32_t lanes = std::min<uint32_t>(ctas * b, lane_cap);
-            if (lanes >= best_lanes) {
-                best_lanes = lanes;
-                best = b;
+        pick(lane_bytes, best, best_lanes);
+        // Cold state rows: when the state variables that no recurrence reads
+        // at a later order move their orders 1..p to a global buffer of the
+        // module, more lanes may fit (Kepler at order 19: 99 slots instead of
+        // 156, eight warps per SM instead of five).  A sub-partition with a
+        // single warp leaves its FP64 pipe idle while that warp waits on
+        // shared-memory loads and other latencies; two warps keep it busy.
+        uint32_t ncold = 0;
+        const uint32_t cslots = adjoint || !m->d.ev.empty() || (m->cfg.flags & HYK_CFG_NO_COLD_ROWS)
+                                    ? nslot
+                                    : hyk::count_slots(m->d, order, adjoint, pin, true, &ncold);
+        if (ncold > 0 && cslots < nslot) {
+            uint32_t cb = 0, clanes = 0;
+            pick((size_t)cslots * real_bytes, cb, clanes);
+            if (blk) {  // the caller's block size: cold rows whenever they fit more of its CTAs
+                const size_t hot = (size_t)blk * nslot * real_bytes, cold = (size_t)blk * cslots * real_bytes;
+                const uint32_t ch = hot > (size_t)dv.smem_optin ? 0 : (uint32_t)((size_t)dv.smem_per_sm / (hot + 1024));
+                const uint32_t cc = cold > (size_t)dv.smem_optin ? 0 : (uint32_t)((size_t)dv.smem_per_sm / (cold + 1024));
+                cb = blk;
+                clanes = std::min(cc, reg_threads / blk) > std::min(ch, reg_threads / blk) ? std::min(cc, reg_threads / blk) * blk : 0;
+                best_lanes = 0;
+            }
+            if (clanes > best_lanes && clanes >= 32 * 4) {
+                best = cb;
+                best_lanes = clanes;
+                nslot = cslots;
+                lane_bytes = (size_t)nslot * real_bytes;
+                m->ncold = ncold;
+                m->cold_ctas = (int)std::min<size_t>((size_t)dv.smem_per_sm / ((size_t)cb * lane_bytes + 1024),
+                                                     reg_threads / cb);
+                m->cold_threads = (uint64_t)dv.n_sm * (uint64_t)m->cold_ctas * cb;
             }
         }
-        if (best == 0) {
-            if (lane_bytes * 32 > (size_t)dv.smem_optin)
-                return fail(HYK_ERR_UNSUPPORTED, "the system needs " + std::to_string(lane_bytes) +
-                                                     " bytes of Taylor coefficients per lane; at most " +
-                                                     std::to_string(dv.smem_optin / 32) + " fit the shared memory");
-            best = 32;
+        if (blk == 0) {
+            if (best == 0) {
+                if (lane_bytes * 32 > (size_t)dv.smem_optin)
+                    return fail(HYK_ERR_UNSUPPORTED, "the system needs " + std::to_string(lane_bytes) +
+                                                         " bytes of Taylor coefficients per lane; at most " +
+                                                         std::to_string(dv.smem_optin / 32) + " fit the shared memory");
+                best = 32;
+            }
+            blk = best;
         }
-        blk = best;
     }
     if (blk % 32 != 0 || blk > 1024) return fail(HYK_ERR_INVALID, "block_lanes must be a multiple of 32, <= 1024");
     m->blk = blk;
@@ -393,10 +441,10 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32, m->gmem))
             return fail(HYK_ERR_INVALID, err);
     } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
-                              high_acc, f32)) {
+                              high_acc, f32, m->ncold ? m->cold_threads : 0)) {
         return fail(HYK_ERR_INVALID, err);
     }
-    if (g.n_slot != nslot) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
+    if (g.n_slot != nslot || g.n_cold != m->ncold) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
     m->src = g.src;
     m->flops = g.flops;
 
@@ -438,6 +486,16 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
 
     HYK_CU(drv().cuModuleLoadData(&m->mod, cubin.data()));
     if (m->gmem && !m->team) HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->gmem_threads * lane_bytes));
+    if (m->ncold) {
+        // The cold rows' buffer and its address in the module's constant
+        // hyk_cold_base (read by every kernel thread of the module).
+        HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->cold_threads * m->ncold * order * real_bytes));
+        CUdeviceptr cb = 0;
+        size_t cbytes = 0;
+        HYK_CU(drv().cuModuleGetGlobal(&cb, &cbytes, m->mod, "hyk_cold_base"));
+        if (cbytes != sizeof(CUdeviceptr)) return fail(HYK_ERR_INVALID, "internal: hyk_cold_base size");
+        HYK_CU(drv().cuMemcpyHtoD(cb, &m->jets, sizeof(CUdeviceptr)));
+    }
     HYK_CU(drv().cuModuleGetFunction(&m->f_step, m->mod, "hyk_step_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_prop, m->mod, "hyk_prop_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
@@ -472,6 +530,9 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         const int want = (int)(m->gmem_threads / ((uint64_t)dv.n_sm * blk));
         if (m->ctas_per_sm < want) return fail(HYK_ERR_UNSUPPORTED, "the global-memory grid cannot be resident");
         m->ctas_per_sm = want;
+    } else if (m->ncold) {
+        // Launches never exceed the grid the cold rows are sized for.
+        m->ctas_per_sm = std::min(m->ctas_per_sm, m->cold_ctas);
     }
     if (adjoint) {
         HYK_CU(drv().cuModuleGetFunction(&m->f_adj, m->mod, "hyk_adjoint_kernel"));
@@ -546,7 +607,7 @@ static uint64_t lane_blocks(const hyk_module *m, uint64_t n) {
 // Grid of a launch of f: in global-memory mode every kernel but the
 // initialisation runs on the fixed grid the coefficient buffer is sized for.
 static uint64_t launch_grid(const hyk_module *m, CUfunction f, uint64_t grid) {
-    if (m->gmem && f != m->f_init) grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * m->ctas_per_sm);
+    if ((m->gmem || m->ncold) && f != m->f_init) grid = std::min<uint64_t>(grid, (uint64_t)m->dv->n_sm * m->ctas_per_sm);
     return grid;
 }
 
@@ -703,6 +764,8 @@ static int fill_prop(hyk_module *m, KParams &k, const hyk_lanes_t *lanes, const 
     k.ck_h = p->ck_h;
     k.ck_cap = p->ck_capacity;
     if (p->ck_x && (!p->ck_t || !p->ck_h)) return fail(HYK_ERR_INVALID, "the checkpoint tape needs ck_x, ck_t and ck_h");
+    k.stop_iter = p->stop_iter;
+    k.stop_group = p->stop_group;
     return fill_events(m, k, p);
 }
 
@@ -927,6 +990,12 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     }
     const uint32_t slots = hyk::count_slots(d, order, adjoint, pin);
     const uint64_t gstride = (uint64_t)slots * (f32 ? 4 : 8) * 32 > 227u * 1024 ? 152ull * blk : 0;
+    // The cold-state-row layout (as the runtime may pick it), with the rows
+    // sized for one CTA per SM of a 152-SM GPU.
+    uint32_t ncold = 0;
+    if (!gstride && !adjoint && d.ev.empty() && !(cfg && (cfg->flags & HYK_CFG_NO_COLD_ROWS)))
+        hyk::count_slots(d, order, adjoint, pin, true, &ncold);
+    const uint64_t cstride = ncold ? 152ull * blk : 0;
     hyk::GenOut g;
     const bool high_acc = cfg && (cfg->flags & HYK_CFG_HIGH_ACCURACY);
     if (team > 1) {
@@ -934,7 +1003,7 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : (tg ? 128 : 32), sizeof(KParams),
                                 g, err, high_acc, f32, tg))
             return fail(HYK_ERR_UNSUPPORTED, err);
-    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32)) {
+    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32, cstride)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (n_slot) *n_slot = g.n_slot;

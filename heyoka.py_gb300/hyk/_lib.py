@@ -40,6 +40,7 @@ HYK_CFG_ADJOINT = 2
 HYK_CFG_HIGH_ACCURACY = 4
 HYK_CFG_GLOBAL_JETS = 8
 HYK_CFG_FLOAT32 = 16
+HYK_CFG_NO_COLD_ROWS = 32
 
 LANE_DONE, LANE_STOPPED, LANE_CAPACITY, LANE_EVENT = 1, 2, 4, 8
 OC_EV_OVERFLOW = -4294967310
@@ -122,6 +123,8 @@ class hyk_prop_t(ctypes.Structure):
         ("ev_capacity", c_u64),
         ("ev_last", c_vp),
         ("ev_sign", c_vp),
+        ("stop_iter", c_vp),
+        ("stop_group", c_u64),
     ]
 
 

@@ -19,13 +19,14 @@ class Module:
 
     def __init__(self, dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False,
                  team_size: int = 0, persist_ctas: int = 0, high_accuracy: bool = False, global_jets: bool = False,
-                 float32: bool = False):
+                 float32: bool = False, cold_rows: bool = True):
         L = _lib.load()
         self.dec, self.order, self.device = dec, int(order), int(device)
         self._cdec, self._keep = dec.as_c()
         flags = (_lib.HYK_CFG_PIN_ARITH if pin_arith else 0) | (_lib.HYK_CFG_HIGH_ACCURACY if high_accuracy else 0)
         flags |= _lib.HYK_CFG_GLOBAL_JETS if global_jets else 0
         flags |= _lib.HYK_CFG_FLOAT32 if float32 else 0
+        flags |= 0 if cold_rows else _lib.HYK_CFG_NO_COLD_ROWS
         self.float32 = bool(float32)
         cfg = _lib.hyk_config_t(int(block_lanes), int(persist_ctas), flags, int(team_size))
         h = ctypes.c_void_p()
@@ -82,14 +83,14 @@ class Module:
 
 def get_module(dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False,
                team_size: int = 0, persist_ctas: int = 0, high_accuracy: bool = False,
-               global_jets: bool = False, float32: bool = False) -> Module:
+               global_jets: bool = False, float32: bool = False, cold_rows: bool = True) -> Module:
     key = (dec.digest(), int(order), int(device), int(block_lanes), bool(pin_arith), int(team_size), int(persist_ctas),
-           bool(high_accuracy), bool(global_jets), bool(float32))
+           bool(high_accuracy), bool(global_jets), bool(float32), bool(cold_rows))
     with _cache_lock:
         m = _modules.get(key)
         if m is None:
             m = Module(dec, order, device, block_lanes, pin_arith, team_size, persist_ctas, high_accuracy, global_jets,
-                       float32)
+                       float32, cold_rows)
             _modules[key] = m
         return m
 

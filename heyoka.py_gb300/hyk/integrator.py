@@ -244,6 +244,8 @@ class taylor_adaptive_batch:
         persist_ctas=0,
         global_jets=False,
         autotune=False,
+        batch_semantics="reference",
+        cold_rows=True,
         **kwargs,
     ):
         llvm = {"opt_level": 3, "force_avx512": False, "slp_vectorize": False, "fast_math": False,
@@ -358,7 +360,7 @@ class taylor_adaptive_batch:
             self._autotune = r
         self._mod_opts = dict(block_lanes=int(block_lanes), pin_arith=bool(pin_arith), team_size=int(team_size),
                               persist_ctas=int(persist_ctas), high_accuracy=self._high_accuracy,
-                              global_jets=bool(global_jets), float32=f32)
+                              global_jets=bool(global_jets), float32=f32, cold_rows=bool(cold_rows))
         self._mod = get_module(self._dec, self._order, self._dev, **self._mod_opts)
         # propagate_grid's own measured choice, when the autotuner found a
         # different one (its modules share the bookkeeping layout)
@@ -371,6 +373,9 @@ class taylor_adaptive_batch:
             self._mod_grid = get_module(self._dec, self._order, self._dev, **self._mod_grid_opts)
         self._prop_mode = prop_mode
         self._schedule = schedule
+        if batch_semantics not in ("reference", "lane"):
+            raise ValueError("batch_semantics must be 'reference' or 'lane', not {!r}".format(batch_semantics))
+        self._batch_semantics = batch_semantics
         self._compact_mode = bool(compact_mode)
         self._B = B
         fr = dict(dtype=self._tdt, device=self._tdev)
@@ -915,8 +920,58 @@ class taylor_adaptive_batch:
         }
         return p
 
+    def _ev_has_callbacks(self):
+        return bool(self._nt_events) or any(e.callback is not None for e in self._t_events)
+
     def _run(self, tf_hi, tf_lo, max_steps, md, grid=None, write_tc=False, c_output=False, group=None,
              lane_order=None, callback=None, group_callbacks=None):
+        """A propagation of every lane to (tf_hi, tf_lo), with the batch rules
+        of ``batch_semantics``.
+
+        "reference" (the default): a state that becomes non-finite stops every
+        lane of its batch (of its ensemble iteration, with ``group``) at that
+        iteration, with err_nf_state for the lane concerned and the outcome of
+        its last step for the others, as the reference's batch propagate loop
+        does (heyoka/expose_batch_integrators.cpp:279-314); event callbacks run
+        after each batch step.  The one-launch-per-step and the stepped forms
+        step the lanes in lockstep, so the stop is exact in one pass; the
+        persistent form lets lanes run ahead, so after a pass in which a
+        state became non-finite the initial state is restored and the
+        propagation runs again with every lane stopping at the iteration the
+        first pass found.  "lane": a non-finite state stops only its lane, and
+        event callbacks run when the propagation returns."""
+        ref = self.__dict__.get("_batch_semantics", "reference") == "reference"
+        stepped_ev = ref and self._ev is not None and self._ev_has_callbacks()
+        if not ref:
+            return self._run_once(tf_hi, tf_lo, max_steps, md, grid, write_tc, c_output, group, lane_order, callback,
+                                  group_callbacks, None, False)
+        B = self._B
+        G = B if group is None else int(group)
+        stop = torch.full((B // G,), -1, dtype=torch.int64, device=self._tdev)  # all ones: no stop
+        if stepped_ev or bool(_callbacks(callback)) or bool(group_callbacks):
+            # one batch step per launch: a launch in which a state became
+            # non-finite is taken again with the stop words it left (_run_once)
+            return self._run_once(tf_hi, tf_lo, max_steps, md, grid, write_tc, c_output, group, lane_order, callback,
+                                  group_callbacks, (stop, G), stepped_ev)
+        snap = (self._state.clone(), self._thi.clone(), self._tlo.clone(),
+                None if self._ev is None else {k: self._ev[k].clone() for k in ("count", "last", "sign")})
+        res = self._run_once(tf_hi, tf_lo, max_steps, md, grid, write_tc, c_output, group, lane_order, callback,
+                             group_callbacks, (stop, G), False)
+        if bool((stop != -1).any()):
+            # a state became non-finite: run again from the initial state, every
+            # lane of the group taking the failing iteration uncounted and stopping
+            self._state.copy_(snap[0])
+            self._thi.copy_(snap[1])
+            self._tlo.copy_(snap[2])
+            if snap[3] is not None:
+                for k, v in snap[3].items():
+                    self._ev[k].copy_(v)
+            res = self._run_once(tf_hi, tf_lo, max_steps, md, grid, write_tc, c_output, group, lane_order, callback,
+                                 group_callbacks, (stop, G), False)
+        return res
+
+    def _run_once(self, tf_hi, tf_lo, max_steps, md, grid, write_tc, c_output, group, lane_order, callback,
+                  group_callbacks, stop, stepped_ev):
         """Initialise and run a propagation of every lane to (tf_hi, tf_lo).
 
         With step callbacks the persistent kernel runs one step per lane per
@@ -939,7 +994,7 @@ class taylor_adaptive_batch:
             for cb in cl:
                 if hasattr(cb, "pre_hook"):
                     cb.pre_hook(view)
-        stepped = cbs or gcbs  # one batch step per launch
+        stepped = cbs or gcbs or stepped_ev  # one batch step per launch
         if max_steps < 0:
             raise ValueError("max_steps must be non-negative")
         B, ne, order = self._B, self.dim, self._order
@@ -972,6 +1027,8 @@ class taylor_adaptive_batch:
                 None if last_tc is None else last_tc.data_ptr(), p["status"].data_ptr(),
                 None if lane_order is None else lane_order.data_ptr(),
                 0 if lane_order is None else lane_order.numel(), None, None, None, 0, 1 if stepped else 0,
+                None, None, None, None, 0, None, None,
+                None if stop is None else stop[0].data_ptr(), 0 if stop is None or stop[1] == B else stop[1],
             ))
 
         lanes = lanes_struct(self._state, self._pars, self._thi, self._tlo)
@@ -997,10 +1054,29 @@ class taylor_adaptive_batch:
                 ws_bytes = int(L.hyk_propagate_workspace_size(mod.handle, B, mode))
                 ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self._tdev)
             while True:
+                redo = None
+                if stop is not None and stepped:
+                    # the step's inputs, to take it again if a state becomes non-finite in it
+                    redo = (stop[0].clone(), self._state.clone(), self._thi.clone(), self._tlo.clone(),
+                            {k: v.clone() for k, v in p.items() if v is not None},
+                            None if self._ev is None else {k: self._ev[k].clone() for k in ("count", "last", "sign")})
                 _lib.check(
                     L.hyk_propagate(mod.handle, lanes, d, mode, ws.data_ptr(), ws_bytes, 16, None, s),
                     "hyk_propagate",
                 )
+                if redo is not None and bool((stop[0] != redo[0]).any()):
+                    self._state.copy_(redo[1])
+                    self._thi.copy_(redo[2])
+                    self._tlo.copy_(redo[3])
+                    for k, v in redo[4].items():
+                        p[k].copy_(v)
+                    if redo[5] is not None:
+                        for k, v in redo[5].items():
+                            self._ev[k].copy_(v)
+                    _lib.check(
+                        L.hyk_propagate(mod.handle, lanes, d, mode, ws.data_ptr(), ws_bytes, 16, None, s),
+                        "hyk_propagate",
+                    )
                 if ev is not None:
                     ev[1].record(torch.cuda.current_stream(self._dev))
                 if not c_output and self._ev is None and not stepped:
@@ -1064,7 +1140,13 @@ class taylor_adaptive_batch:
         self._finish_prop(p, group, last_tc)
         res = {"grid_out": grid_out}
         if c_output:
-            res["c_output"] = self._make_c_output(p, tcs, thi, tlo, t0h, t0l)
+            nrec = p["n_iter"]
+            if stop is not None and bool((stop[0] != -1).any()):
+                # the lanes stopped at their group's failing iteration took it uncounted
+                hit = (stop[0] != -1).repeat_interleave(stop[1])
+                unc = hit & ((p["status"] & _lib.LANE_STOPPED) != 0) & (p["outcome"] != int(taylor_outcome.err_nf_state))
+                nrec = torch.where(unc | (hit & (p["outcome"] == int(taylor_outcome.err_nf_state))), nrec - 1, nrec)
+            res["c_output"] = self._make_c_output(p, tcs, thi, tlo, t0h, t0l, nrec)
         return res
 
     def _lpt_order(self, tf_hi, tf_lo):
@@ -1105,11 +1187,11 @@ class taylor_adaptive_batch:
             self._final_tc_mask = early | (p["n_iter"] == 0)
         self._prop = p
 
-    def _make_c_output(self, p, tcs, thi, tlo, t0h, t0l):
+    def _make_c_output(self, p, tcs, thi, tlo, t0h, t0l, nrec=None):
         from .c_output import continuous_output_batch
 
         B = self._B
-        nit = p["n_iter"]
+        nit = p["n_iter"] if nrec is None else nrec
         K = int(nit.max().item()) if B else 0
         ne, order = self.dim, self._order
         fr = dict(dtype=self._tdt, device=self._tdev)

@@ -131,6 +131,11 @@ typedef struct hyk_config {
 #define HYK_CFG_GLOBAL_JETS 8u   /* one thread per trajectory with the Taylor coefficients in global memory
                                     (chosen automatically for systems that leave fewer than two warps
                                     per SM in shared memory) */
+#define HYK_CFG_NO_COLD_ROWS 32u /* lane form: keep every state variable's coefficients in shared memory.
+                                    By default the variables that no recurrence reads at a later order
+                                    keep orders 1..p in a module-owned global buffer when that lets more
+                                    lanes share an SM (the module's calls must then be ordered on one
+                                    stream, as with HYK_CFG_GLOBAL_JETS) */
 
 typedef struct hyk_module_info {
     uint32_t n_eq, n_pars, order, n_u;
@@ -260,6 +265,23 @@ typedef struct hyk_prop {
     uint64_t ev_capacity;
     double *ev_last;
     int32_t *ev_sign;
+    /* optional: the reference's whole-batch stop on a non-finite state
+     * (heyoka/expose_batch_integrators.cpp:279-314 returns err_nf_state for
+     * the lane whose state became non-finite and stops every lane of the
+     * batch at that iteration).  Device words of "iterations at which to
+     * stop", one per group of stop_group lanes (stop_group 0: one word for
+     * all lanes), initialised by the caller (UINT64_MAX: no stop).  A lane
+     * whose state becomes non-finite at its iteration k lowers its group's
+     * word to k (atomic minimum); a lane that has made as many iterations as
+     * its group's word stops before its next one (HYK_LANE_STOPPED, its
+     * outcome that of its last step).  The one-launch-per-step form steps the
+     * unfinished lanes in lockstep, so one call gives the reference's result;
+     * the persistent form runs lanes ahead of one another, so after a call
+     * that lowered a word the caller restores the initial state and calls
+     * again with the words as they were left.  NULL: every lane stops only
+     * itself (per-lane semantics). */
+    uint64_t *stop_iter;
+    uint64_t stop_group;
 } hyk_prop_t;
 
 #define HYK_LANE_DONE 1u     /* reached the final time */
@@ -359,8 +381,9 @@ int hyk_fp64_peak(int device, double millis, double *flops_per_s);
 int hyk_fp32_peak(int device, double millis, double *flops_per_s);
 
 /* Build check without a GPU: generate the module source for `d` at `order`
- * (block size cfg->block_lanes, default 128) and compile it with NVRTC for
- * sm_103a.  `log` receives the NVRTC log (ptxas register and spill
+ * (block size cfg->block_lanes, default 128; the lane form with cold state
+ * rows unless cfg->flags has HYK_CFG_NO_COLD_ROWS) and compile it with NVRTC
+ * for sm_103a.  `log` receives the NVRTC log (ptxas register and spill
  * statistics when `verbose` is 1; the generated source, without compiling,
  * when `verbose` is 2; a host C++ translation unit of the same recurrences,
  * for CPU checks, when `verbose` is 3; the recurrences in the reference's

@@ -1134,14 +1134,16 @@ int hyko_step(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, uint32
 }
 
 // Batch propagation (until/for/grid) of B lanes.  With c_output != 0 the
-// per-iteration Taylor coefficients (n_iter, n_eq, order+1, B) and end times
-// (n_iter+1, B) are returned in malloc'ed buffers (free with hyko_free).
+// per-iteration Taylor coefficients (c_n, n_eq, order+1, B) and end times
+// (c_n+1, B) are returned in malloc'ed buffers (free with hyko_free); c_n is
+// n_iter, or n_iter - 1 when a non-finite state stopped the batch (the
+// failing iteration is not recorded).
 int hyko_propagate(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, uint32_t B, double *state,
                    const double *pars, double *t_hi, double *t_lo, const double *tf_hi, const double *tf_lo,
                    uint64_t max_steps, const double *max_dt, const double *grid, uint64_t n_grid,
                    double *grid_out, int c_output, double **c_tcs, double **c_thi, double **c_tlo,
                    uint64_t *n_iter, int64_t *outcome, double *min_h, double *max_h, uint64_t *n_steps,
-                   double *last_h, double *last_tc) {
+                   double *last_h, double *last_tc, uint64_t *c_n) {
     Dec d;
     if (!load_dec(dd, d)) return HYK_ERR_INVALID;
     if (order < 2 || B == 0) {
@@ -1163,6 +1165,7 @@ int hyko_propagate(const hyk_decomp_t *dd, uint32_t order, int prec, int mode, u
         *c_tcs = dup(vt);
         *c_thi = dup(vh);
         *c_tlo = dup(vl);
+        if (c_n) *c_n = vh.size() / B - 1;
     }
     return r;
 }

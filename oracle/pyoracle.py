@@ -51,7 +51,7 @@ def lib():
         L.hyko_propagate.argtypes = [
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
             pd, pd, pd, pd, pd, pd, ctypes.c_uint64, pd, pd, ctypes.c_uint64, pd,
-            ctypes.c_int, P(pd), P(pd), P(pd), pu64, pi64, pd, pd, pu64, pd, pd,
+            ctypes.c_int, P(pd), P(pd), P(pd), pu64, pi64, pd, pd, pu64, pd, pd, pu64,
         ]
         L.hyko_ensemble_until.argtypes = [
             P(hyk_decomp_t), ctypes.c_uint32, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
@@ -146,6 +146,7 @@ class Oracle:
         mn, mx, lh = np.zeros(B), np.zeros(B), np.zeros(B)
         ns = np.zeros(B, dtype=np.uint64)
         nit = ctypes.c_uint64(0)
+        cn = ctypes.c_uint64(0)
         md = None if max_delta_t is None else _f64(np.broadcast_to(max_delta_t, (B,))).copy()
         gout = None
         if grid is not None:
@@ -158,7 +159,7 @@ class Oracle:
             _p(tf), _p(tfl), int(max_steps), _p(md),
             _p(grid), 0 if grid is None else grid.shape[0], _p(gout),
             int(bool(c_output)), ctypes.byref(c_t), ctypes.byref(c_h), ctypes.byref(c_l),
-            ctypes.byref(nit), _p(oc, pi64), _p(mn), _p(mx), _p(ns, pu64), _p(lh), _p(ltc),
+            ctypes.byref(nit), _p(oc, pi64), _p(mn), _p(mx), _p(ns, pu64), _p(lh), _p(ltc), ctypes.byref(cn),
         )
         self._err(rc)
         self.last_h = lh
@@ -166,7 +167,7 @@ class Oracle:
             self.tc = ltc
         res = {"outcome": oc, "min_h": mn, "max_h": mx, "n_steps": ns, "n_iter": nit.value, "grid": gout}
         if c_output:
-            n = nit.value
+            n = cn.value
             res["c_tcs"] = np.ctypeslib.as_array(c_t, shape=(max(n, 1) * ne * (p + 1) * B,))[
                 : n * ne * (p + 1) * B
             ].reshape(n, ne, p + 1, B).copy()

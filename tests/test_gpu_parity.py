@@ -261,9 +261,12 @@ def test_zero_duration_and_errors():
 
 
 def test_non_finite_state_stops_lane(oracle):
+    """With batch_semantics="lane" a non-finite state stops only its lane (the
+    default, the reference's whole-batch stop, is tested in
+    test_gpu_batch_semantics.py)."""
     x, v = hyk.make_vars("x", "v")
     sys_ = [(x, v), (v, hyk.log(x))]
-    ta = hyk.taylor_adaptive_batch(sys_, [[-1.0, 1.0], [0.0, 0.0]])
+    ta = hyk.taylor_adaptive_batch(sys_, [[-1.0, 1.0], [0.0, 0.0]], batch_semantics="lane")
     ta.propagate_until(0.5)
     res = ta.propagate_res
     assert res[0][0] == hyk.taylor_outcome.err_nf_state
