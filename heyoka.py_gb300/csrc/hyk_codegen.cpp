@@ -215,6 +215,15 @@ std::string precision_header(bool pin) {
     } else {
         h += "#define HYK_F32 0\n";
         h += "#define HYK_FMA(a, b, c) __fma_rn((a), (b), (c))\n";
+        // x * y, x + y and x - y as fused multiply-adds (same bits); the
+        // constants -0 and 1 come from volatile loads of module globals, so
+        // that the compiler cannot turn the fused operations back into plain ones.
+        h += "__device__ double hyk_nz_g = -0.0, hyk_one_g = 1.0;\n";
+        h += "#define HYK_FMAOPS_CONSTS const double hyk_nz = *(volatile double *)&hyk_nz_g, "
+             "hyk_one = *(volatile double *)&hyk_one_g;\n";
+        h += "#define HYK_MUL(a, b) __fma_rn((a), (b), hyk_nz)\n";
+        h += "#define HYK_ADD(a, b) __fma_rn((a), hyk_one, (b))\n";
+        h += "#define HYK_SUB(a, b) __fma_rn((b), -hyk_one, (a))\n";
         h += "#define HYK_DM_EXP hyk_dm_exp\n#define HYK_DM_LOG hyk_dm_log\n#define HYK_DM_SINCOS hyk_dm_sincos\n"
              "#define HYK_DM_POW hyk_dm_pow\n#define HYK_DM_RHO hyk_dm_rho\n";
     }
@@ -556,6 +565,21 @@ struct Gen {
         if (pin) return "(" + c + " + " + x + " * " + y + ")";
         return "HYK_FMA(" + x + ", " + y + ", " + c + ")";
     }
+    // Products, sums and differences of the gpu arithmetic in double
+    // precision: fused multiply-adds with an addend of -0 (x * y) or a factor
+    // of 1 (x + y, x - y).  They give exactly the bits of the plain
+    // operations, and the FP64 pipe of this GPU issues fused multiply-adds
+    // faster than plain multiplications and additions.
+    bool fmaops() const { return !pin && !g_f32; }
+    std::string mul(const std::string &x, const std::string &y) const {
+        return fmaops() ? "HYK_MUL(" + x + ", " + y + ")" : "(" + x + " * " + y + ")";
+    }
+    std::string add(const std::string &x, const std::string &y) const {
+        return fmaops() ? "HYK_ADD(" + x + ", " + y + ")" : "(" + x + " + " + y + ")";
+    }
+    std::string sub(const std::string &x, const std::string &y) const {
+        return fmaops() ? "HYK_SUB(" + x + ", " + y + ")" : "(" + x + " - " + y + ")";
+    }
 
     struct Acc {
         std::string name;
@@ -564,7 +588,7 @@ struct Gen {
     void term(Acc &a, const std::string &x, const std::string &y) {
         if (x.empty() || y.empty()) return;
         if (a.first) {
-            o << "    hyk_real " << a.name << " = " << x << " * " << y << ";\n";
+            o << "    hyk_real " << a.name << " = " << mul(x, y) << ";\n";
             a.first = false;
             flops += 1;
         } else {
@@ -575,7 +599,7 @@ struct Gen {
     std::string divn(const std::string &x, uint32_t n) {
         flops += 1;
         if (pin) return "(" + x + " / " + lit((double)n) + ")";
-        return "(" + x + " * " + lit(recip((double)n)) + ")";
+        return mul(x, lit(recip((double)n)));
     }
     std::string inv0(uint32_t u) const { return "i" + std::to_string(u); }
     // After defining 1/b_0 at order 0: keep it for the later order functions.
@@ -593,7 +617,7 @@ struct Gen {
         const uint32_t lim = (adj || evx) ? p : p - 1;  // stored orders: 0..lim-1
         if (u >= N && hist[u] && n + 1 <= lim) o << "    " << smem((uint32_t)slot[u] + n) << " = " << vname(u, n) << ";\n";
         if (needka[u] && n >= 1) {
-            o << "    const hyk_real " << kname(u, n) << " = " << lit((double)n) << " * " << vname(u, n) << ";\n";
+            o << "    const hyk_real " << kname(u, n) << " = " << mul(lit((double)n), vname(u, n)) << ";\n";
             flops += 1;
             if (kslot[u] >= 0 && n + 1 <= lim) o << "    " << smem((uint32_t)kslot[u] + n - 1) << " = " << kname(u, n) << ";\n";
         }
@@ -613,7 +637,7 @@ struct Gen {
             const std::string a = cf(A, n, n), b = cf(B, n, n);
             const bool add = op.op == HYK_OP_ADD;
             if (!a.empty() && !b.empty()) {
-                def(u, n, "(" + a + (add ? " + " : " - ") + b + ")");
+                def(u, n, add ? this->add(a, b) : sub(a, b));
                 flops += 1;
             } else if (!a.empty())
                 def(u, n, a);
@@ -648,10 +672,10 @@ struct Gen {
             for (uint32_t j = 1; j <= n; ++j)
                 if (nz(B, j)) term(s, cf(B, j, n), ucoef(u, n - j, n));
             const std::string av = an.empty() ? z : an;
-            const std::string num = s.first ? av : "(" + av + " - " + acc + ")";
+            const std::string num = s.first ? av : sub(av, acc);
             if (!s.first) flops += 1;
             flops += 1;
-            def(u, n, pin ? "(" + num + " / " + b0 + ")" : "(" + num + " * " + inv0(u) + ")");
+            def(u, n, pin ? "(" + num + " / " + b0 + ")" : mul(num, inv0(u)));
             break;
         }
         case HYK_OP_SQUARE: {
@@ -659,7 +683,7 @@ struct Gen {
             for (uint32_t j = 0; 2 * j < n; ++j)
                 if (nz(A, j) && nz(A, n - j)) term(s, cf(A, j, n), cf(A, n - j, n));
             if (!s.first) {
-                o << "    " << acc << " = " << acc << " + " << acc << ";\n";
+                o << "    " << acc << " = " << add(acc, acc) << ";\n";
                 flops += 1;
             }
             if (n % 2 == 0 && nz(A, n / 2)) term(s, cf(A, n / 2, n), cf(A, n / 2, n));
@@ -678,14 +702,14 @@ struct Gen {
             Acc s{acc};
             for (uint32_t j = 1; 2 * j < n; ++j) term(s, ucoef(u, j, n), ucoef(u, n - j, n));
             if (!s.first) {
-                o << "    " << acc << " = " << acc << " + " << acc << ";\n";
+                o << "    " << acc << " = " << add(acc, acc) << ";\n";
                 flops += 1;
             }
             if (n % 2 == 0) term(s, ucoef(u, n / 2, n), ucoef(u, n / 2, n));
             const std::string av = an.empty() ? z : an;
-            const std::string num = s.first ? av : "(" + av + " - " + acc + ")";
+            const std::string num = s.first ? av : sub(av, acc);
             flops += s.first ? 1 : 2;
-            def(u, n, pin ? "(" + num + " / (2.0 * " + ucoef(u, 0, n) + "))" : "(" + num + " * " + inv0(u) + ")");
+            def(u, n, pin ? "(" + num + " / (2.0 * " + ucoef(u, 0, n) + "))" : mul(num, inv0(u)));
             break;
         }
         case HYK_OP_POW: {
@@ -704,7 +728,7 @@ struct Gen {
                 if (anj.empty()) continue;
                 const double coef = powcoef(n, j, alpha);
                 const std::string t = "t" + std::to_string(u) + "_" + std::to_string(n) + "_" + std::to_string(j);
-                o << "    const hyk_real " << t << " = " << lit(coef) << " * " << anj << ";\n";
+                o << "    const hyk_real " << t << " = " << mul(lit(coef), anj) << ";\n";
                 flops += 1;
                 term(s, t, ucoef(u, j, n));
             }
@@ -716,7 +740,7 @@ struct Gen {
             if (pin)
                 def(u, n, "(" + acc + " / (" + lit((double)n) + " * " + a0 + "))");
             else
-                def(u, n, "((" + acc + " * " + lit(recip((double)n)) + ") * " + inv0(u) + ")");
+                def(u, n, mul(mul(acc, lit(recip((double)n))), inv0(u)));
             break;
         }
         case HYK_OP_EXP: {
@@ -749,11 +773,11 @@ struct Gen {
             const std::string av = an.empty() ? z : an;
             std::string num = av;
             if (!s.first) {
-                num = "(" + av + " - " + divn(acc, n) + ")";
+                num = sub(av, divn(acc, n));
                 flops += 1;
             }
             flops += 1;
-            def(u, n, pin ? "(" + num + " / " + a0 + ")" : "(" + num + " * " + inv0(u) + ")");
+            def(u, n, pin ? "(" + num + " / " + a0 + ")" : mul(num, inv0(u)));
             break;
         }
         case HYK_OP_SIN:
@@ -818,7 +842,8 @@ struct Gen {
     }
 
     void emit_jets() {
-        const char *coldg = coldrows ? "    hyk_real *__restrict__ hyk_cold_g = hyk_cold_ptr();\n" : "";
+        std::string coldg = coldrows ? "    hyk_real *__restrict__ hyk_cold_g = hyk_cold_ptr();\n" : "";
+        if (fmaops()) coldg += "    HYK_FMAOPS_CONSTS\n";
         if (!split) {
             o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n" << coldg;
             for (uint32_t i = 0; i < N; ++i) o << "    const hyk_real " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
@@ -832,8 +857,7 @@ struct Gen {
                     o << "    const hyk_real " << vname(i, n) << " = " << sx(i, n) << ";\n";
                     // The same product the previous order formed (k_i_0 is never read).
                     if (needka[i] && n >= 1)
-                        o << "    const hyk_real " << kname(i, n) << " = " << lit((double)n) << " * " << vname(i, n)
-                          << ";\n";
+                        o << "    const hyk_real " << kname(i, n) << " = " << mul(lit((double)n), vname(i, n)) << ";\n";
                 }
                 if (!pin && n >= 1)
                     for (uint32_t u = N; u < NU; ++u)
@@ -860,8 +884,8 @@ struct Gen {
                 def(i, n + 1, f.empty() ? lit(0.0) : divn(f, n + 1));
                 o << "    " << sx(i, n + 1) << " = " << vname(i, n + 1) << ";\n";
                 if (needka[i]) {
-                    o << "    const hyk_real " << kname(i, n + 1) << " = " << lit((double)(n + 1)) << " * "
-                      << vname(i, n + 1) << ";\n";
+                    o << "    const hyk_real " << kname(i, n + 1) << " = " << mul(lit((double)(n + 1)), vname(i, n + 1))
+                      << ";\n";
                     flops += 1;
                     if (kslot[i] >= 0 && n + 1 + ((adj || evx) ? 1u : 2u) <= p)
                         o << "    " << smem((uint32_t)kslot[i] + n) << " = " << kname(i, n + 1) << ";\n";
