@@ -388,6 +388,9 @@ struct Gen {
             }
         }
         if (adj) {
+            // The reverse sweep reads every operation's coefficients.
+            for (uint32_t u = N; u < NU; ++u)
+                if (!alias[u]) hist[u] = 1;
             // Values the reverse sweep reads besides the forward histories:
             // the factor multiplied by a parameter (for the parameter's
             // adjoint), the quotient by a parameter, and the logarithm.
@@ -469,20 +472,20 @@ struct Gen {
             }
         }
         if (adj) {
-            // Adjoint accumulators: orders 0..p of every history, of every j*a_j.
+            // Reverse sweep (gather form): per operation the history of its
+            // adjoint factor at orders 1..p-1 (slot hslot[u] + n - 1), and one
+            // slot per state variable for its adjoint at the order above.
             abase = s;
             aslot.assign(NU, -1);
             akslot.assign(NU, -1);
-            for (uint32_t u = 0; u < NU; ++u)
-                if (hist[u] && !alias[u]) {
-                    aslot[u] = (int)s;
-                    s += p + 1;
-                }
-            for (uint32_t u = 0; u < NU; ++u)
-                if (needka[u] && !alias[u]) {
-                    akslot[u] = (int)s;
-                    s += p + 1;
-                }
+            for (uint32_t k = 0; k < d.n_ops; ++k) {
+                const uint32_t u = N + k;
+                const int o = d.ops[k].op;
+                if (alias[u] || o == HYK_OP_ADD || o == HYK_OP_SUB || o == HYK_OP_NEG || p < 2) continue;
+                aslot[u] = (int)s;
+                s += p - 1;
+            }
+            for (uint32_t i = 0; i < N; ++i) akslot[i] = (int)s++;
         }
         nslot = s;
     }
@@ -959,152 +962,240 @@ struct Gen {
         }
         return (r.kind == HYK_ARG_TIME && j == 1) ? "1.0" : "0.0";
     }
-    std::string aref(uint32_t u, uint32_t j) const { return smem((uint32_t)aslot[u] + j); }
-    std::string akref(uint32_t u, uint32_t j) const { return smem((uint32_t)akslot[u] + j); }
-    std::string gname(uint32_t u, uint32_t n) const { return "g" + std::to_string(u) + "_" + std::to_string(n); }
-    // adjoint(r, order j) += x * y
-    void acc(const Ref &r, uint32_t j, uint32_t n, const std::string &x, const std::string &y) {
+    // ------------------------------------------------------------------
+    // Reverse sweep in gather form.  The orders are walked downwards; at
+    // order m the operations are walked in reverse.  ub<u> (a register of the
+    // order's function) collects the adjoint of coefficient m of u: every
+    // consumer of u adds its whole contribution to order m at once, as a sum
+    // over the orders n >= m of the consumer's adjoint factor (its history,
+    // aslot, read back from memory; order m itself from the register) times a
+    // forward coefficient.  An operation whose recurrence reads its own lower
+    // orders gathers those terms the same way before its adjoint is complete.
+    // Nothing is accumulated in memory: every slot is written once.
+    std::string ub(uint32_t u) const { return "ub" + std::to_string(u); }
+    std::string hfac(uint32_t u) const { return "hf" + std::to_string(u); }
+    // The adjoint factor of u at order n while emitting order m (n >= m).
+    std::string hval(uint32_t u, uint32_t n, uint32_t m) const {
+        if (n == m) return hfac(u);
+        return smem((uint32_t)aslot[u] + n - 1);
+    }
+    // ub(r) += e (r a variable, or a parameter at order 0).
+    // (as fused multiply-adds, which the FP64 pipe issues fastest; scale:
+    // ub(r) += scale * e).
+    void contrib(const Ref &r, uint32_t m, const std::string &e, const std::string &scale = "") {
+        std::string f = scale.empty() ? "hyk_one" : scale;
+        if (r.neg) f = "(-" + f + ")";
         if (r.kind == HYK_ARG_U) {
-            const uint32_t u = (uint32_t)r.u;
-            const std::string xx = r.neg ? "(-" + x + ")" : x;
-            std::string t;
-            if (hist[u])
-                t = aref(u, j);
-            else {
-                if (j != n) {
-                    std::fprintf(stderr, "hyk codegen: adjoint of a non-stored value at another order (u%u)\n", u);
-                    std::abort();
-                }
-                t = gname(u, n);
-            }
-            o << "    " << t << " = __fma_rn(" << xx << ", " << y << ", " << t << ");\n";
-        } else if (r.kind == HYK_ARG_PAR && j == 0) {
-            o << "    pb[" << r.par << "] = __fma_rn(" << x << ", " << y << ", pb[" << r.par << "]);\n";
+            o << "    " << ub((uint32_t)r.u) << " = __fma_rn(" << f << ", " << e << ", " << ub((uint32_t)r.u) << ");\n";
+        } else if (r.kind == HYK_ARG_PAR && m == 0) {
+            o << "    pb[" << r.par << "] = __fma_rn(" << f << ", " << e << ", pb[" << r.par << "]);\n";
         }
     }
-    void acck(const Ref &r, uint32_t j, const std::string &x, const std::string &y) {
-        if (r.kind != HYK_ARG_U) return;
-        const std::string xx = r.neg ? "(-" + x + ")" : x;
-        o << "    " << akref((uint32_t)r.u, j) << " = __fma_rn(" << xx << ", " << y << ", " << akref((uint32_t)r.u, j)
-          << ");\n";
+    // A sum of products as one fused multiply-add chain; "" when empty.
+    int gcount = 0;
+    std::string gsum(const std::vector<std::pair<std::string, std::string>> &t) {
+        if (t.empty()) return "";
+        const std::string a = "gs" + std::to_string(gcount++);
+        o << "    double " << a << " = __fma_rn(" << t[0].first << ", " << t[0].second << ", hyk_nz);\n";
+        for (size_t k = 1; k < t.size(); ++k)
+            o << "    " << a << " = __fma_rn(" << t[k].first << ", " << t[k].second << ", " << a << ");\n";
+        return a;
     }
+    // The adjoint factor at order m is final: keep it for the lower orders.
+    void keep(uint32_t u, uint32_t m) {
+        if (m >= 1) o << "    " << smem((uint32_t)aslot[u] + m - 1) << " = " << hfac(u) << ";\n";
+    }
+    // Whether an argument receives an adjoint at order m (a variable, or a
+    // parameter at order 0).
+    static bool wants(const Ref &r, uint32_t m) { return r.kind == HYK_ARG_U || (r.kind == HYK_ARG_PAR && m == 0); }
 
-    void emit_op_bw(uint32_t k, uint32_t n) {
+    void emit_op_bw(uint32_t k, uint32_t m) {
         const auto &op = d.ops[k];
         const uint32_t u = N + k;
         if (alias[u]) return;
         const Ref A = res(op.a), B = res(op.b);
         const Ref self{HYK_ARG_U, (int)u, false, 0, -1};
-        // A function of a constant is constant: nothing flows back above order 0.
         const bool unary_fn = op.op == HYK_OP_SQRT || op.op == HYK_OP_POW || op.op == HYK_OP_EXP ||
                               op.op == HYK_OP_LOG || op.op == HYK_OP_SIN || op.op == HYK_OP_COS;
-        if (unary_fn && n >= 1 && !varying(A)) return;
-        const std::string G = "G" + std::to_string(u) + "_" + std::to_string(n);
-        std::string gsrc = hist[u] ? aref(u, n) : gname(u, n);
-        if (needka[u] && n >= 1) gsrc = "__fma_rn(" + lit((double)n) + ", " + akref(u, n) + ", " + gsrc + ")";
-        o << "    const double " << G << " = " << gsrc << ";\n";
-        const std::string W = "W" + std::to_string(u) + "_" + std::to_string(n);
-        const std::string inv = "i" + std::to_string(u);
+        // A function of a constant is constant: nothing flows back above order 0.
+        if (unary_fn && m >= 1 && !varying(A)) return;
+        const std::string G = ub(u), H = hfac(u), inv = "i" + std::to_string(u);
+        std::vector<std::pair<std::string, std::string>> t;
         switch (op.op) {
         case HYK_OP_ADD:
-            if (nz(A, n)) acc(A, n, n, G, "1.0");
-            if (nz(B, n)) acc(B, n, n, G, "1.0");
+            if (nz(A, m)) contrib(A, m, G);
+            if (nz(B, m)) contrib(B, m, G);
             break;
         case HYK_OP_SUB:
-            if (nz(A, n)) acc(A, n, n, G, "1.0");
-            if (nz(B, n)) acc(B, n, n, G, "(-1.0)");
+            if (nz(A, m)) contrib(A, m, G);
+            if (nz(B, m)) contrib(B, m, G, "(-hyk_one)");
             break;
         case HYK_OP_NEG:
-            if (nz(A, n)) acc(A, n, n, G, "(-1.0)");
+            if (nz(A, m)) contrib(A, m, G, "(-hyk_one)");
             break;
-        case HYK_OP_MUL:
-            for (uint32_t j = 0; j <= n; ++j)
-                if (nz(A, j) && nz(B, n - j)) {
-                    acc(A, j, n, G, val(B, n - j));
-                    acc(B, n - j, n, G, val(A, j));
-                }
-            break;
-        case HYK_OP_DIV:
-            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
-            if (nz(A, n)) acc(A, n, n, W, "1.0");
-            for (uint32_t j = 1; j <= n; ++j)
-                if (nz(B, j)) {
-                    acc(B, j, n, "(-" + W + ")", val(self, n - j));
-                    acc(self, n - j, n, "(-" + W + ")", val(B, j));
-                }
-            acc(B, 0, n, "(-" + W + ")", val(self, n));
-            break;
-        case HYK_OP_SQUARE:
-            for (uint32_t j = 0; j <= n; ++j)
-                if (nz(A, j) && nz(A, n - j)) acc(A, j, n, "(2.0 * " + G + ")", val(A, n - j));
-            break;
-        case HYK_OP_SQRT:
-            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
-            if (nz(A, n)) acc(A, n, n, W, "1.0");
-            if (n >= 1) {
-                for (uint32_t j = 1; j < n; ++j) acc(self, j, n, "(-2.0 * " + W + ")", val(self, n - j));
-                acc(self, 0, n, "(-2.0 * " + W + ")", val(self, n));
-            }
-            break;
-        case HYK_OP_POW: {
-            const double alpha = op.b.num;
-            if (n == 0) {
-                acc(A, 0, 0, "(" + G + " * " + lit(alpha) + ")", "(" + val(self, 0) + " * " + inv + ")");
-                break;
-            }
-            o << "    const double " << W << " = (" << G << " * " << inv << ") * " << lit(1.0 / (double)n) << ";\n";
-            for (uint32_t j = 0; j < n; ++j) {
-                if (!nz(A, n - j)) continue;
-                const double coef = (double)n * alpha - (double)j * (alpha + 1.0);
-                const std::string wc = "(" + W + " * " + lit(coef) + ")";
-                acc(A, n - j, n, wc, val(self, j));
-                acc(self, j, n, wc, val(A, n - j));
-            }
-            acc(A, 0, n, "(-" + G + " * " + inv + ")", val(self, n));
+        case HYK_OP_MUL: {
+            // c_n = sum_j a_j b_{n-j}: abar_m += sum_{n>=m} cbar_n b_{n-m}, and symmetrically.
+            o << "    const double " << H << " = " << G << ";\n";
+            keep(u, m);
+            if (nz(A, m) && wants(A, m))
+                for (uint32_t n = m; n < p; ++n)
+                    if (nz(B, n - m)) t.push_back({hval(u, n, m), val(B, n - m)});
+            const std::string sa = gsum(t);
+            if (!sa.empty()) contrib(A, m, sa);
+            t.clear();
+            if (nz(B, m) && wants(B, m))
+                for (uint32_t n = m; n < p; ++n)
+                    if (nz(A, n - m)) t.push_back({hval(u, n, m), val(A, n - m)});
+            const std::string sb = gsum(t);
+            if (!sb.empty()) contrib(B, m, sb);
             break;
         }
-        case HYK_OP_EXP:
-            if (n == 0) {
-                acc(A, 0, 0, G, val(self, 0));
+        case HYK_OP_DIV: {
+            // c_n = (a_n - sum_{j>=1} b_j c_{n-j}) / b_0, w_n = cbar_n / b_0:
+            // cbar_m -= sum_{n>m} w_n b_{n-m}; abar_m += w_m; bbar_m -= sum_{n>=m} w_n c_{n-m}.
+            for (uint32_t n = m + 1; n < p; ++n)
+                if (nz(B, n - m)) t.push_back({hval(u, n, m), val(B, n - m)});
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = " << G << " - " << ss << ";\n";
+            o << "    const double " << H << " = __fma_rn(" << G << ", " << inv << ", hyk_nz);\n";
+            keep(u, m);
+            if (nz(A, m)) contrib(A, m, H);
+            t.clear();
+            if (nz(B, m) && wants(B, m))
+                for (uint32_t n = m; n < p; ++n) t.push_back({hval(u, n, m), val(self, n - m)});
+            const std::string sb = gsum(t);
+            if (!sb.empty()) contrib(B, m, sb, "(-hyk_one)");
+            break;
+        }
+        case HYK_OP_SQUARE: {
+            o << "    const double " << H << " = " << G << ";\n";
+            keep(u, m);
+            if (nz(A, m) && wants(A, m))
+                for (uint32_t n = m; n < p; ++n)
+                    if (nz(A, n - m)) t.push_back({hval(u, n, m), val(A, n - m)});
+            const std::string sa = gsum(t);
+            if (!sa.empty()) contrib(A, m, sa, "2.0");
+            break;
+        }
+        case HYK_OP_SQRT: {
+            // c_n = (a_n - sum_{0<j<n} c_j c_{n-j}) / (2 c_0), w_n = cbar_n / (2 c_0):
+            // cbar_m -= 2 sum_{n>m} w_n c_{n-m}; abar_m += w_m.
+            for (uint32_t n = m + 1; n < p; ++n) t.push_back({hval(u, n, m), val(self, n - m)});
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = __fma_rn(-2.0, " << ss << ", " << G << ");\n";
+            o << "    const double " << H << " = __fma_rn(" << G << ", " << inv << ", hyk_nz);\n";
+            keep(u, m);
+            if (nz(A, m)) contrib(A, m, H);
+            break;
+        }
+        case HYK_OP_POW: {
+            // c_n = (1/(n a_0)) sum_{j<n} (n al - j (al+1)) a_{n-j} c_j, w_n = cbar_n / (n a_0):
+            // cbar_m += sum_{n>m} w_n coef(n, m) a_{n-m};
+            // abar_m += sum_{n>=m} w_n coef(n, n-m) c_{n-m} (m >= 1);
+            // abar_0 += al cbar_0 c_0 / a_0 - sum_{n>=1} n w_n c_n.
+            const double alpha = op.b.num;
+            for (uint32_t n = m + 1; n < p; ++n)
+                if (nz(A, n - m)) {
+                    const double coef = (double)n * alpha - (double)m * (alpha + 1.0);
+                    t.push_back({hval(u, n, m), "__fma_rn(" + lit(coef) + ", " + val(A, n - m) + ", hyk_nz)"});
+                }
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = " << G << " + " << ss << ";\n";
+            t.clear();
+            if (m == 0) {
+                for (uint32_t n = 1; n < p; ++n) t.push_back({hval(u, n, m), "__fma_rn(" + lit(-(double)n) + ", " + val(self, n) + ", hyk_nz)"});
+                const std::string s0 = gsum(t);
+                std::string e = "(" + G + " * " + lit(alpha) + ") * (" + val(self, 0) + " * " + inv + ")";
+                if (!s0.empty()) e = "(" + e + " + " + s0 + ")";
+                contrib(A, 0, e);
                 break;
             }
-            o << "    const double " << W << " = " << G << " * " << lit(1.0 / (double)n) << ";\n";
-            for (uint32_t j = 1; j <= n; ++j)
-                if (knz(A, j)) {
-                    acck(A, j, W, val(self, n - j));
-                    acc(self, n - j, n, W, kval(A, j));
-                }
+            o << "    const double " << H << " = (" << G << " * " << inv << ") * " << lit(1.0 / (double)m) << ";\n";
+            keep(u, m);
+            for (uint32_t n = m; n < p; ++n) {
+                const double coef = (double)n * alpha - (double)(n - m) * (alpha + 1.0);
+                t.push_back({hval(u, n, m), "__fma_rn(" + lit(coef) + ", " + val(self, n - m) + ", hyk_nz)"});
+            }
+            const std::string sa = gsum(t);
+            if (!sa.empty()) contrib(A, m, sa);
             break;
-        case HYK_OP_LOG:
-            if (n == 0) {
-                acc(A, 0, 0, G, inv);
+        }
+        case HYK_OP_EXP: {
+            // c_n = (1/n) sum_{j=1}^{n} (j a_j) c_{n-j}, w_n = cbar_n / n:
+            // cbar_m += sum_{n>m} w_n (n-m) a_{n-m}; abar_m += m sum_{n>=m} w_n c_{n-m} (m >= 1);
+            // abar_0 += cbar_0 c_0.
+            for (uint32_t n = m + 1; n < p; ++n)
+                if (knz(A, n - m)) t.push_back({hval(u, n, m), kval(A, n - m)});
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = " << G << " + " << ss << ";\n";
+            t.clear();
+            if (m == 0) {
+                contrib(A, 0, "(" + G + " * " + val(self, 0) + ")");
                 break;
             }
-            o << "    const double " << W << " = " << G << " * " << inv << ";\n";
-            if (nz(A, n)) acc(A, n, n, W, "1.0");
-            if (varying(A))
-                for (uint32_t j = 1; j < n; ++j) {
-                    if (!nz(A, n - j)) continue;
-                    const std::string t = "(-" + W + " * " + lit(1.0 / (double)n) + ")";
-                    acck(self, j, t, val(A, n - j));
-                    acc(A, n - j, n, t, kval(self, j));
-                }
-            acc(A, 0, n, "(-" + G + " * " + inv + ")", val(self, n));
+            o << "    const double " << H << " = __fma_rn(" << G << ", " << lit(1.0 / (double)m) << ", hyk_nz);\n";
+            keep(u, m);
+            if (knz(A, m))
+                for (uint32_t n = m; n < p; ++n) t.push_back({hval(u, n, m), val(self, n - m)});
+            const std::string sa = gsum(t);
+            if (!sa.empty()) contrib(A, m, sa, lit((double)m));
             break;
+        }
+        case HYK_OP_LOG: {
+            // c_n = (a_n - (1/n) sum_{0<j<n} (j c_j) a_{n-j}) / a_0, w_n = cbar_n / a_0:
+            // cbar_m -= m sum_{n>m} (w_n / n) a_{n-m};
+            // abar_m += w_m - sum_{n>m} (w_n / n) (n-m) c_{n-m} (m >= 1);
+            // abar_0 += cbar_0 / a_0 - sum_{n>=1} w_n c_n.
+            if (m >= 1 && varying(A))
+                for (uint32_t n = m + 1; n < p; ++n)
+                    if (nz(A, n - m)) t.push_back({hval(u, n, m), "__fma_rn(" + lit(1.0 / (double)n) + ", " + val(A, n - m) + ", hyk_nz)"});
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = __fma_rn(" << lit(-(double)m) << ", " << ss << ", " << G << ");\n";
+            t.clear();
+            if (m == 0) {
+                for (uint32_t n = 1; n < p; ++n) t.push_back({hval(u, n, m), val(self, n)});
+                const std::string s0 = gsum(t);
+                std::string e = "(" + G + " * " + inv + ")";
+                if (!s0.empty()) e = "(" + e + " - " + s0 + ")";
+                contrib(A, 0, e);
+                break;
+            }
+            o << "    const double " << H << " = __fma_rn(" << G << ", " << inv << ", hyk_nz);\n";
+            keep(u, m);
+            std::string e = H;
+            if (varying(A)) {
+                for (uint32_t n = m + 1; n < p; ++n)
+                    t.push_back({hval(u, n, m), "__fma_rn(" + lit(1.0 / (double)n) + ", " + kval(self, n - m) + ", hyk_nz)"});
+                const std::string sa = gsum(t);
+                if (!sa.empty()) e = "(" + H + " - " + sa + ")";
+            }
+            if (nz(A, m)) contrib(A, m, e);
+            break;
+        }
         case HYK_OP_SIN:
         case HYK_OP_COS: {
-            const Ref P{HYK_ARG_U, op.aux, false, 0, -1};
+            // s_n = (1/n) sum (j a_j) c_{n-j}, c_n = -(1/n) sum (j a_j) s_{n-j};
+            // w_n = sigma ubar_n / n (sigma = +1 sin, -1 cos):
+            // ubar_m += sum_{n>m} wP_n (n-m) a_{n-m} (wP the partner's factors);
+            // abar_m += m sum_{n>=m} w_n P_{n-m} (m >= 1); abar_0 += sigma ubar_0 P_0.
+            const uint32_t partner = (uint32_t)op.aux;
             const bool is_sin = op.op == HYK_OP_SIN;
-            if (n == 0) {
-                acc(A, 0, 0, is_sin ? G : "(-" + G + ")", val(P, 0));
+            const Ref P{HYK_ARG_U, (int)partner, false, 0, -1};
+            for (uint32_t n = m + 1; n < p; ++n)
+                if (knz(A, n - m)) t.push_back({hval(partner, n, m), kval(A, n - m)});
+            const std::string ss = gsum(t);
+            if (!ss.empty()) o << "    " << G << " = " << G << " + " << ss << ";\n";
+            t.clear();
+            if (m == 0) {
+                contrib(A, 0, "(" + std::string(is_sin ? "" : "-") + G + " * " + val(P, 0) + ")");
                 break;
             }
-            o << "    const double " << W << " = " << G << " * " << lit((is_sin ? 1.0 : -1.0) / (double)n) << ";\n";
-            for (uint32_t j = 1; j <= n; ++j)
-                if (knz(A, j)) {
-                    acck(A, j, W, val(P, n - j));
-                    acc(P, n - j, n, W, kval(A, j));
-                }
+            o << "    const double " << H << " = __fma_rn(" << G << ", " << lit((is_sin ? 1.0 : -1.0) / (double)m) << ", hyk_nz);\n";
+            keep(u, m);
+            if (knz(A, m))
+                for (uint32_t n = m; n < p; ++n) t.push_back({hval(u, n, m), val(P, n - m)});
+            const std::string sa = gsum(t);
+            if (!sa.empty()) contrib(A, m, sa, lit((double)m));
             break;
         }
         default:
@@ -1128,38 +1219,42 @@ struct Gen {
 
     // One function per order keeps each compiled block small (compile time
     // grows faster than linearly with the size of a straight-line block).
+    // Order m: the state variables' adjoints start from the Horner update
+    // (lam_i h^m); the right-hand sides receive x̄_{m+1} / (m+1) (x̄_{m+1} kept
+    // in slot akslot[i] by order m+1); then the operations in reverse order.
     void emit_bw() {
-        for (uint32_t n = 0; n < p; ++n) {
-            o << "static __device__ __noinline__ void hyk_bw_o" << n
-              << "(double *__restrict__ S, const double t0, double *__restrict__ pb) {\n";
-            o << "    (void)t0;\n";
+        for (uint32_t m = 0; m < p; ++m) {
+            gcount = 0;
+            o << "static __device__ __noinline__ void hyk_bw_o" << m
+              << "(double *__restrict__ S, const double t0, const double h, double *__restrict__ lam, "
+                 "double *__restrict__ pb) {\n";
+            o << "    (void)t0;\n    HYK_FMAOPS_CONSTS\n    (void)hyk_nz;\n";
             emit_inverses(true);
-            for (uint32_t k = 0; k < d.n_ops; ++k) {
-                const uint32_t u = N + k;
-                if (!alias[u] && !hist[u]) o << "    double " << gname(u, n) << " = 0.0;\n";
-            }
+            o << "    double hm = 1.0;\n";
+            for (uint32_t q = 0; q < m; ++q) o << "    hm = hm * h;\n";
+            for (uint32_t i = 0; i < N; ++i) o << "    double " << ub(i) << " = lam[" << i << "] * hm;\n";
+            for (uint32_t k = 0; k < d.n_ops; ++k)
+                if (!alias[N + k]) o << "    double " << ub(N + k) << " = 0.0;\n";
             for (uint32_t ii = N; ii-- > 0;) {
-                const uint32_t i = ii;
-                if (needka[i])
-                    o << "    " << aref(i, n + 1) << " = __fma_rn(" << lit((double)(n + 1)) << ", " << akref(i, n + 1) << ", "
-                      << aref(i, n + 1) << ");\n";
-                const Ref r = res(d.rhs[i]);
-                if (nz(r, n)) acc(r, n, n, aref(i, n + 1), lit(1.0 / (double)(n + 1)));
+                const Ref r = res(d.rhs[ii]);
+                if (nz(r, m)) contrib(r, m, smem((uint32_t)akslot[ii]), lit(1.0 / (double)(m + 1)));
             }
-            for (uint32_t kk = d.n_ops; kk-- > 0;) emit_op_bw(kk, n);
+            for (uint32_t kk = d.n_ops; kk-- > 0;) emit_op_bw(kk, m);
+            for (uint32_t i = 0; i < N; ++i) {
+                if (m > 0)
+                    o << "    " << smem((uint32_t)akslot[i]) << " = " << ub(i) << ";\n";
+                else
+                    o << "    lam[" << i << "] = " << ub(i) << ";\n";
+            }
             o << "}\n";
         }
         o << "static __device__ __noinline__ void hyk_jets_bw(double *__restrict__ S, const double t0, const double h, "
              "double *__restrict__ lam, double *__restrict__ pb) {\n";
-        o << "#pragma unroll 1\n    for (int s = " << abase << "; s < " << nslot << "; ++s) S[s * HYK_STRIDE] = 0.0;\n";
-        // Horner update x_new_i = sum_n x_i^[n] h^n
+        // x̄_p comes from the Horner update only
         o << "    double hp = 1.0;\n";
-        for (uint32_t n = 0; n <= p; ++n) {
-            for (uint32_t i = 0; i < N; ++i) o << "    " << aref(i, n) << " = lam[" << i << "] * hp;\n";
-            if (n < p) o << "    hp = hp * h;\n";
-        }
-        for (uint32_t nn = p; nn-- > 0;) o << "    hyk_bw_o" << nn << "(S, t0, pb);\n";
-        for (uint32_t i = 0; i < N; ++i) o << "    lam[" << i << "] = " << aref(i, 0) << ";\n";
+        for (uint32_t q = 0; q < p; ++q) o << "    hp = hp * h;\n";
+        for (uint32_t i = 0; i < N; ++i) o << "    " << smem((uint32_t)akslot[i]) << " = lam[" << i << "] * hp;\n";
+        for (uint32_t mm = p; mm-- > 0;) o << "    hyk_bw_o" << mm << "(S, t0, h, lam, pb);\n";
         o << "}\n";
     }
 };

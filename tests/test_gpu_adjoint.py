@@ -110,3 +110,28 @@ def test_forward_matches_integrator(libhyk):
     ta = hyk.taylor_adaptive_batch(W.cr3bp_sys(), st, pars=mu, tol=1e-15)
     ta.propagate_until(5.0)
     assert np.array_equal(xf.detach().cpu().numpy(), np.asarray(ta.state))
+
+
+def test_cr3bp_gradient_vs_variational_equations_t50_256(libhyk, oracle):
+    """The benchmark configuration's horizon: 256 seeded trajectories of the
+    65536-trajectory CR3BP ensemble (mu per lane) to t = 50; the adjoint's
+    gradient of loss = sum |r(50) - r*|^2 with respect to the initial state
+    and mu against the first-order variational equations."""
+    st, mu = W.cr3bp_ics(1 << 16, seed=3)
+    idx = np.sort(np.random.default_rng(123).choice(1 << 16, 256, replace=False))
+    st, mu = np.ascontiguousarray(st[:, idx]), np.ascontiguousarray(mu[:, idx])
+    target = st[:3] + np.random.default_rng(3).normal(0.0, 1e-2, (3, 256))
+    tf = 50.0
+    _, gx, gp = _loss_grad(W.cr3bp_sys(), st, mu, tf, target)
+    vs = var.var_ode_sys(W.cr3bp_sys(), var.var_args.vars | var.var_args.params)
+    full = np.concatenate([st, vs.initial_variational_state(256)])
+    o = oracle.Oracle(vs.sys, full, pars=mu, order=19, mode=1)
+    o.propagate_until(tf)
+    xf = o.state[:6]
+    J = o.state[6:].reshape(6, 7, 256)
+    g = np.zeros((6, 256))
+    g[:3] = 2 * (xf[:3] - target)
+    grad = np.einsum("ial,il->al", J, g)
+    rel_x = np.max(np.abs(grad[:6] - gx), axis=0) / np.max(np.abs(grad[:6]), axis=0)
+    rel_p = np.abs(grad[6] - gp[0]) / np.abs(grad[6])
+    assert rel_x.max() < 1e-8 and rel_p.max() < 1e-8, (rel_x.max(), rel_p.max())
