@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=1024, help="serve: the most steps per lane in one slice")
     ap.add_argument("--quantum-ms", type=float, default=2.0, help="serve: target duration of a slice")
+    ap.add_argument("--serve-mode", default="resident", choices=["resident", "slice"],
+                    help="serve: resident kernels fed from a device ring, or time slices relaunched by the host")
     ap.add_argument("--members", type=int, default=65536, help="oss, cr3bp-adjoint: trajectories")
     ap.add_argument("--autotune", action="store_true",
                     help="oss: pick the kernel configuration by measurement (hyk.autotune, cached per system)")
@@ -349,7 +351,8 @@ def run_serve(args):
 
     systems = {"pendulum": (W.pendulum_sys(), 1e-15), "kepler": (W.kepler_sys(), 1e-15), "cr3bp": (W.cr3bp_sys(), 1e-15)}
     reqs = serve_stream(args.rate, args.duration)
-    srv = serve.Server(systems, hbm_budget=4 << 30, slice_iters=args.slice, quantum_ms=args.quantum_ms)
+    srv = serve.Server(systems, hbm_budget=4 << 30, slice_iters=args.slice, quantum_ms=args.quantum_ms,
+                       mode=args.serve_mode)
     srv.run(serve_stream(50.0, 0.2, seed=99), realtime=False)  # warm-up: compile, first launches
     for p in srv.pools.values():
         p.lane_steps = 0
@@ -388,6 +391,7 @@ def run_serve(args):
             "workload": "serve: Poisson {:g} req/s for {:g} s, size round(logU[1,4096]), system U{{pendulum,kepler,cr3bp}}, "
                         "horizon logU[1,1000], tol 1e-15".format(args.rate, args.duration),
             "requests": len(reqs),
+            "mode": args.serve_mode,
             "slice_iters_max": args.slice,
             "quantum_ms": args.quantum_ms,
             "pool_capacity": {k: p.C for k, p in srv.pools.items()},

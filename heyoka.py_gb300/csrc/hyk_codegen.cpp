@@ -896,7 +896,9 @@ struct Gen {
             }
             // Values of earlier orders are re-read from shared memory: the
             // warp barrier keeps the compiler from carrying them in registers.
-            o << "    __syncwarp();\n";
+            // It joins the threads that run the recurrences together (the
+            // serving kernel's idle threads wait elsewhere).
+            o << "    HYK_WARP_SYNC();\n";
             if (split) o << "}\n";
         }
         if (split) {
@@ -1994,7 +1996,7 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
              "#define __forceinline__ inline\n#define __restrict__\n"
              "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
              "static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }\n"
-             "static inline void __syncwarp() {}\n";
+             "static inline void __syncwarp() {}\n#define HYK_WARP_SYNC()\n";
         h << kDmath << "\n";
         h << (f32 ? "typedef float hyk_real;\n" : "typedef double hyk_real;\n") << precision_header(false);
         h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
@@ -2028,7 +2030,7 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
          "#define __forceinline__ inline\n#define __restrict__\n"
          "static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }\n"
              "static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }\n"
-         "static inline void __syncwarp() {}\n";
+         "static inline void __syncwarp() {}\n#define HYK_WARP_SYNC()\n";
     h << kDmath << "\n";
     h << (f32 ? "typedef float hyk_real;\n" : "typedef double hyk_real;\n") << precision_header(false);
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order

@@ -48,7 +48,7 @@ thread_local std::string g_err;
 // driver entry point goes through this table.
 #define HYK_STR2(x) #x
 #define HYK_STR(x) HYK_STR2(x)
-#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy) X(cuModuleGetGlobal) X(cuMemcpyHtoD)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy) X(cuModuleGetGlobal) X(cuMemcpyHtoD) X(cuMemcpy2DAsync)
 
 struct DriverApi {
 #define HYK_DECL(f) decltype(&::f) f = nullptr;
@@ -142,6 +142,16 @@ struct KParams {
     int32_t *ev_sign;
     uint64_t *stop_iter;
     uint64_t stop_group;
+    uint64_t *ring;
+    uint64_t ring_mask;
+    uint64_t *ring_head;
+    const uint64_t *ring_tail;
+    const uint32_t *serve_stop;
+    const int64_t *owner;
+    uint32_t *done_count;
+    uint64_t *inflight;
+    uint32_t *serve_status;
+    uint64_t idle_ns, max_wait_ns;
     int persistent;
 };
 
@@ -233,6 +243,7 @@ struct hyk_module {
     CUmodule mod = nullptr;
     CUfunction f_step = nullptr, f_prop = nullptr, f_init = nullptr, f_adj = nullptr;
     CUfunction f_azero = nullptr, f_alist = nullptr;  // the plain form's list of unfinished lanes
+    CUfunction f_serve = nullptr;                     // the serving kernel (lane form)
     int adj_ctas_per_sm = 0;
     uint32_t team = 0;           // threads per trajectory (team form); 0 = lane form
     bool f32 = false;            // single precision
@@ -501,6 +512,12 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     HYK_CU(drv().cuModuleGetFunction(&m->f_init, m->mod, "hyk_prop_init_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_azero, m->mod, "hyk_act_zero_kernel"));
     HYK_CU(drv().cuModuleGetFunction(&m->f_alist, m->mod, "hyk_act_list_kernel"));
+    if (!m->team) {
+        HYK_CU(drv().cuModuleGetFunction(&m->f_serve, m->mod, "hyk_serve_kernel"));
+        HYK_CU(drv().cuFuncSetAttribute(m->f_serve, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
+        HYK_CU(drv().cuFuncSetAttribute(m->f_serve, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT,
+                                        m->gmem ? 0 : 100));
+    }
     for (CUfunction f : {m->f_step, m->f_prop}) {
         HYK_CU(drv().cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)m->smem));
         // Global-memory coefficients: no shared memory, the whole unified
@@ -913,6 +930,58 @@ int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
     // otherwise.
     if (kWsCounters > cap) return fail(HYK_ERR_INVALID, "hyk_propagate_noalloc: the scratch array is too small");
     return propagate_impl(m, lanes, p, mode, ws, cap, check_every, iters, stream, false);
+}
+
+int hyk_serve(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, const hyk_serve_t *sv, void *stream) {
+    int rc = check_lanes(m, lanes);
+    if (rc) return rc;
+    if (!m->f_serve) return fail(HYK_ERR_UNSUPPORTED, "serving with a device work queue needs a lane-form module");
+    if (!sv || !sv->ring || !sv->head || !sv->tail || !sv->stop || !sv->owner || !sv->done_count || !sv->inflight ||
+        !sv->status)
+        return fail(HYK_ERR_INVALID, "null serving-queue pointer");
+    if (sv->ring_capacity == 0 || (sv->ring_capacity & (sv->ring_capacity - 1)))
+        return fail(HYK_ERR_INVALID, "the ring capacity must be a power of two");
+    if (sv->max_wait_ns == 0) return fail(HYK_ERR_INVALID, "max_wait_ns must be positive (every wait is bounded)");
+    if (lanes->n_lanes == 0) return 0;
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    KParams k;
+    rc = fill_prop(m, k, lanes, p);
+    if (rc) return rc;
+    if (k.grid || k.tc_out || k.ck_x || !m->d.ev.empty())
+        return fail(HYK_ERR_UNSUPPORTED, "the serving kernel propagates without grids, coefficient output, tapes or events");
+    k.persistent = 1;
+    k.iters_per_launch = ~0ULL;
+    k.ring = sv->ring;
+    k.ring_mask = sv->ring_capacity - 1;
+    k.ring_head = sv->head;
+    k.ring_tail = sv->tail;
+    k.serve_stop = sv->stop;
+    k.owner = sv->owner;
+    k.done_count = sv->done_count;
+    k.inflight = sv->inflight;
+    k.serve_status = sv->status;
+    k.idle_ns = sv->idle_ns;
+    k.max_wait_ns = sv->max_wait_ns;
+    uint64_t grid = (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm;
+    if (sv->grid_ctas) grid = std::min<uint64_t>(grid, sv->grid_ctas);
+    return launch(m, m->f_serve, grid, m->blk, m->smem, k, stream);
+}
+
+int hyk_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height, void *stream) {
+    if (width == 0 || height == 0) return 0;
+    if (!dst || !src || dpitch < width || spitch < width) return fail(HYK_ERR_INVALID, "invalid 2D copy");
+    CUDA_MEMCPY2D c;
+    std::memset(&c, 0, sizeof c);
+    c.srcMemoryType = CU_MEMORYTYPE_UNIFIED;
+    c.srcDevice = (CUdeviceptr)src;
+    c.srcPitch = spitch;
+    c.dstMemoryType = CU_MEMORYTYPE_UNIFIED;
+    c.dstDevice = (CUdeviceptr)dst;
+    c.dstPitch = dpitch;
+    c.WidthInBytes = width;
+    c.Height = height;
+    HYK_CU(drv().cuMemcpy2DAsync(&c, (CUstream)stream));
+    return 0;
 }
 
 int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,

@@ -128,6 +128,26 @@ class hyk_prop_t(ctypes.Structure):
     ]
 
 
+class hyk_serve_t(ctypes.Structure):
+    _fields_ = [
+        ("ring", c_vp),
+        ("ring_capacity", c_u64),
+        ("head", c_vp),
+        ("tail", c_vp),
+        ("stop", c_vp),
+        ("owner", c_vp),
+        ("done_count", c_vp),
+        ("inflight", c_vp),
+        ("status", c_vp),
+        ("idle_ns", c_u64),
+        ("max_wait_ns", c_u64),
+        ("grid_ctas", c_u32),
+    ]
+
+
+HYK_SERVE_IDLE, HYK_SERVE_STOP, HYK_SERVE_TIMEOUT = 1, 2, 4
+
+
 # Every function the header declares, with its ctypes signature.
 SIGNATURES = {
     "hyk_module_create": (c_int, [P(hyk_decomp_t), c_u32, P(hyk_config_t), c_int, P(c_vp)]),
@@ -148,6 +168,8 @@ SIGNATURES = {
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_fp32_peak": (c_int, [c_int, c_d, P(c_d)]),
     "hyk_dmath_eval": (c_int, [c_int, c_vp, c_vp, c_vp, c_u64, c_vp]),
+    "hyk_serve": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), P(hyk_serve_t), c_vp]),
+    "hyk_memcpy2d": (c_int, [c_vp, ctypes.c_size_t, c_vp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, c_vp]),
     "hyk_codegen_check": (
         c_int,
         [P(hyk_decomp_t), c_u32, P(hyk_config_t), c_int, ctypes.c_char_p, ctypes.c_size_t, P(c_u32), P(c_d)],

@@ -368,6 +368,376 @@ class LanePool:
         return bool(self.active or self.inflight or self.gathers)
 
 
+def _next_pow2(n):
+    r = 1
+    while r < n:
+        r <<= 1
+    return r
+
+
+class _Ranges:
+    """First-fit allocator of contiguous lane ranges (a request's lanes are
+    contiguous, so that admitting and gathering it are 2D copies)."""
+
+    def __init__(self, n):
+        self.free = [(0, n)]  # sorted (start, length)
+        self.n_free = n
+
+    def alloc(self, n):
+        for k, (s, ln) in enumerate(self.free):
+            if ln >= n:
+                if ln == n:
+                    del self.free[k]
+                else:
+                    self.free[k] = (s + n, ln - n)
+                self.n_free -= n
+                return s
+        return -1
+
+    def release(self, s, n):
+        import bisect
+
+        k = bisect.bisect_left(self.free, (s, 0))
+        self.free.insert(k, (s, n))
+        # merge with the neighbours
+        if k + 1 < len(self.free) and self.free[k][0] + self.free[k][1] == self.free[k + 1][0]:
+            self.free[k] = (s, self.free[k][1] + self.free[k + 1][1])
+            del self.free[k + 1]
+        if k > 0 and self.free[k - 1][0] + self.free[k - 1][1] == self.free[k][0]:
+            self.free[k - 1] = (self.free[k - 1][0], self.free[k - 1][1] + self.free[k][1])
+            del self.free[k]
+        self.n_free += n
+
+
+@dataclass
+class _RActive:
+    req: Request
+    start: int
+    admitted: float
+    retiring: bool = False
+
+
+class ResidentPool:
+    """Device lanes of one ODE system served by one resident kernel
+    (``hyk_serve``) that takes newly admitted lanes from a device ring while
+    it runs, so that a request never waits for a slice boundary or a
+    relaunch.
+
+    Admission copies a request's rows (state, parameters, time, final time,
+    bookkeeping, owner, status) into a contiguous range of the pool's tables
+    and then appends the range's lane indices to the ring and advances its
+    tail; retirement reads the per-request finished-lane counters the kernel
+    keeps and copies a finished request's range back.  All of it is done by
+    stream-ordered copies (``hyk_memcpy2d``) on an I/O stream: the kernel
+    holds the pool's share of the SMs, so no other kernel could start.  The
+    kernel's waits are bounded: with nothing to do for ``idle_ms`` it returns
+    (HYK_SERVE_IDLE) and the pool launches it again with the next admission;
+    once any thread has returned, the pool stops the launch (its idle threads
+    leave, threads holding lanes finish them) and starts a fresh one, so the
+    queue is never served by a thinned-out grid."""
+
+    def __init__(self, name, sys, tol, capacity, device, grid_share=1.0, idle_ms=20.0, max_wait_ms=60000.0,
+                 max_requests=1 << 16):
+        self.name = name
+        self.dec = taylor_decompose(sys)
+        self.order = order_from_tol(tol)
+        self.dev = torch.device(device)
+        self.mod = get_module(self.dec, self.order, self.dev.index)
+        info = self.mod.info_dict()
+        if info["team_size"] != 1:
+            raise _lib.HykError("the resident serving pool needs a lane-form module")
+        self.grid_ctas = max(1, int(info["n_sm"] * info["ctas_per_sm"] * grid_share))
+        self.C = int(capacity)
+        ne, npar, C = self.dec.n_eq, self.dec.n_pars, self.C
+        b = ne + npar
+        self.R = {"thi": b, "tlo": b + 1, "tf": b + 2, "rem_hi": b + 3, "rem_lo": b + 4, "min_h": b + 5,
+                  "max_h": b + 6, "last_h": b + 7}
+        self.RF = b + 8
+        f = dict(device=self.dev)
+        self.F = torch.zeros((self.RF, C), dtype=torch.float64, **f)
+        self.I = torch.zeros((4, C), dtype=torch.int64, **f)  # outcome, n_steps, n_iter, owner
+        self.I[3].fill_(-1)
+        self.status = torch.full((C,), _DONE, dtype=torch.int32, **f)
+        self.ring_cap = _next_pow2(max(C, 2))
+        self.ring = torch.zeros(self.ring_cap, dtype=torch.int64, **f)
+        # device words: head, tail, inflight (u64); stop, status (u32)
+        self.words = torch.zeros(3, dtype=torch.int64, **f)
+        self.flags = torch.zeros(2, dtype=torch.int32, **f)
+        self.done = torch.zeros(int(max_requests) + 1, dtype=torch.int32, **f)
+        self.tail_h = 0
+        self.ranges = _Ranges(C)
+        self.active: dict = {}
+        self.kstream = torch.cuda.Stream(self.dev)
+        self.io = torch.cuda.Stream(self.dev)
+        self.kernel_ev = None  # completion of the running launch
+        self.draining = False
+        self.idle_ns = int(idle_ms * 1e6)
+        self.max_wait_ns = int(max_wait_ms * 1e6)
+        self.lane_steps = 0
+        self.keep = deque()  # (event, pinned buffers) alive until their copies are done
+        self.poll_ev = None
+        self.poll_host = None
+        self.gathers: deque = deque()
+        self.top_rid = 0
+
+    @property
+    def n_free(self):
+        return self.ranges.n_free
+
+    def reserve_requests(self, n):
+        """Room for request indices below n in the finished-lane counters (a
+        running launch is drained first; its counts are carried over)."""
+        if n + 1 > self.done.numel():
+            if self.kernel_ev is not None:
+                self.stop_kernel(wait=True)
+            torch.cuda.synchronize(self.dev)
+            new = torch.zeros(n + 1, dtype=torch.int32, device=self.dev)
+            self._copy(new.data_ptr(), 4, self.done.data_ptr(), 4, self.done.numel() * 4, 1)
+            self.io.synchronize()
+            self.done = new
+
+    def _copy(self, dst, dpitch, src, spitch, width, height, stream=None):
+        L = _lib.load()
+        st = self.io if stream is None else stream
+        if height == 1:
+            dpitch = spitch = width  # one row: the pitches do not matter
+        with torch.cuda.device(self.dev):
+            _lib.check(L.hyk_memcpy2d(dst, dpitch, src, spitch, width, height,
+                                      ctypes.c_void_p(st.cuda_stream)), "hyk_memcpy2d")
+
+    def _free_keep(self):
+        while self.keep and self.keep[0][0].query():
+            self.keep.popleft()
+
+    def admit(self, reqs, now):
+        """Admit the longest prefix of `reqs` whose requests each find a
+        contiguous range of free lanes; returns how many were admitted."""
+        self._free_keep()
+        ne, npar, RF, R, C = self.dec.n_eq, self.dec.n_pars, self.RF, self.R, self.C
+        k = 0
+        starts = []
+        while k < len(reqs):
+            st = self.ranges.alloc(reqs[k].state.shape[1])
+            if st < 0:
+                break
+            starts.append(st)
+            k += 1
+        if k == 0:
+            return 0
+        self.top_rid = max(self.top_rid, max(r.rid for r in reqs[:k]) + 1)
+        self.reserve_requests(self.top_rid)
+        bufs = []
+        order_h = []
+        for r, st in zip(reqs[:k], starts):
+            n = r.state.shape[1]
+            blk = np.empty((RF, n))
+            blk[:ne] = r.state
+            if npar:
+                blk[ne: ne + npar] = np.asarray(r.pars, dtype=np.float64).reshape(npar, n)
+            t0 = np.full(n, float(r.t0))
+            tf = np.full(n, float(r.t_final))
+            blk[R["thi"]], blk[R["tlo"]], blk[R["tf"]] = t0, 0.0, tf
+            # remaining time = tf - t0 in double-length arithmetic (the
+            # operations of the propagation initialisation kernel)
+            sm = tf - t0
+            bb = sm - tf
+            e = (tf - (sm - bb)) + (-t0 - bb)
+            e = e + 0.0
+            hi = sm + e
+            lo = e - (hi - sm)
+            blk[R["rem_hi"]], blk[R["rem_lo"]] = hi, lo
+            blk[R["min_h"]], blk[R["max_h"]], blk[R["last_h"]] = np.inf, 0.0, 0.0
+            ints = np.zeros((4, n), dtype=np.int64)
+            ints[0] = -4294967299
+            ints[3] = r.rid
+            stat = np.where((hi == 0) & (lo == 0), _lib.LANE_DONE, 0).astype(np.int32)
+            hb = torch.from_numpy(blk).pin_memory()
+            hi_ = torch.from_numpy(ints).pin_memory()
+            hs = torch.from_numpy(stat).pin_memory()
+            bufs += [hb, hi_, hs]
+            self._copy(self.F.data_ptr() + st * 8, C * 8, hb.data_ptr(), n * 8, n * 8, RF)
+            self._copy(self.I.data_ptr() + st * 8, C * 8, hi_.data_ptr(), n * 8, n * 8, 4)
+            self._copy(self.status.data_ptr() + st * 4, C * 4, hs.data_ptr(), n * 4, n * 4, 1)
+            order_h.append(np.arange(st, st + n, dtype=np.int64))
+            self.active[r.rid] = _RActive(r, st, now)
+        # the lane indices into the ring, then the new tail
+        lanes = torch.from_numpy(np.concatenate(order_h)).pin_memory()
+        bufs.append(lanes)
+        m = lanes.numel()
+        pos = self.tail_h % self.ring_cap
+        first = min(m, self.ring_cap - pos)
+        self._copy(self.ring.data_ptr() + pos * 8, 8, lanes.data_ptr(), 8, first * 8, 1)
+        if first < m:
+            self._copy(self.ring.data_ptr(), 8, lanes.data_ptr() + first * 8, 8, (m - first) * 8, 1)
+        self.tail_h += m
+        tail = torch.tensor([self.tail_h], dtype=torch.int64).pin_memory()
+        bufs.append(tail)
+        self._copy(self.words.data_ptr() + 8, 8, tail.data_ptr(), 8, 8, 1)
+        ev = torch.cuda.Event()
+        ev.record(self.io)
+        self.keep.append((ev, bufs))
+        self.ensure_kernel()
+        return k
+
+    def _launch(self):
+        L = _lib.load()
+        a = {"rem_hi": self.F[self.R["rem_hi"]], "rem_lo": self.F[self.R["rem_lo"]], "outcome": self.I[0],
+             "min_h": self.F[self.R["min_h"]], "max_h": self.F[self.R["max_h"]], "n_steps": self.I[1],
+             "n_iter": self.I[2], "last_h": self.F[self.R["last_h"]], "status": self.status}
+        d = _lib.hyk_prop_t(
+            self.F[self.R["tf"]].data_ptr(), None, None, 0, None, 0, None, None, None, None, 0,
+            a["rem_hi"].data_ptr(), a["rem_lo"].data_ptr(), a["outcome"].data_ptr(), a["min_h"].data_ptr(),
+            a["max_h"].data_ptr(), a["n_steps"].data_ptr(), a["n_iter"].data_ptr(), None, a["last_h"].data_ptr(),
+            None, a["status"].data_ptr(), None, 0, None, None, None, 0, 0,
+        )
+        ne = self.dec.n_eq
+        lanes = lanes_struct(self.F[:ne], self.F[ne: ne + self.dec.n_pars], self.F[self.R["thi"]],
+                             self.F[self.R["tlo"]])
+        sv = _lib.hyk_serve_t(
+            self.ring.data_ptr(), self.ring_cap, self.words.data_ptr(), self.words.data_ptr() + 8,
+            self.flags.data_ptr(), self.I[3].data_ptr(), self.done.data_ptr(), self.words.data_ptr() + 16,
+            self.flags.data_ptr() + 4, self.idle_ns, self.max_wait_ns, self.grid_ctas,
+        )
+        # a fresh launch starts with the stop flag and the status word clear
+        # (a copy: another pool's launch may hold every other SM)
+        zero = torch.zeros(2, dtype=torch.int32).pin_memory()
+        self._copy(self.flags.data_ptr(), 8, zero.data_ptr(), 8, 8, 1)
+        zev = torch.cuda.Event()
+        zev.record(self.io)
+        self.keep.append((zev, [zero]))
+        with torch.cuda.device(self.dev):
+            self.kstream.wait_stream(self.io)
+            _lib.check(L.hyk_serve(self.mod.handle, lanes, d, sv, ctypes.c_void_p(self.kstream.cuda_stream)),
+                       "hyk_serve")
+            ev = torch.cuda.Event()
+            ev.record(self.kstream)
+        self.kernel_ev = ev
+        self.draining = False
+
+    def kernel_running(self):
+        return self.kernel_ev is not None and not self.kernel_ev.query()
+
+    def ensure_kernel(self):
+        """Launch the kernel unless a launch that still takes work is running."""
+        if self.kernel_running() and not self.draining:
+            return
+        if self.kernel_running():
+            return  # a draining launch ends soon; poll() starts the next one
+        self._launch()
+
+    def stop_kernel(self, wait=False):
+        if self.kernel_ev is None:
+            return
+        one = torch.ones(1, dtype=torch.int32).pin_memory()
+        self._copy(self.flags.data_ptr(), 4, one.data_ptr(), 4, 4, 1)
+        ev = torch.cuda.Event()
+        ev.record(self.io)
+        self.keep.append((ev, [one]))
+        self.draining = True
+        if wait:
+            self.kernel_ev.synchronize()
+
+    def poll(self, now_fn, block=False):
+        """Read the finished-lane counters (and the kernel's status word)
+        without waiting for the kernel; gather the finished requests; return
+        the results whose copies have completed."""
+        out = []
+        if self.poll_ev is not None and (block or self.poll_ev.query()):
+            self.poll_ev.synchronize()
+            counts, flags = self.poll_host
+            self.poll_ev = None
+            cn = counts.numpy()
+            done = [rid for rid, a in self.active.items()
+                    if not a.retiring and rid < cn.size and cn[rid] >= a.req.state.shape[1]]
+            if done:
+                self._gather(done)
+            if int(flags.numpy()[1]) != 0 and self.kernel_running() and not self.draining:
+                self.stop_kernel()  # threads are leaving: end this launch, start a fresh one
+        if self.poll_ev is None and self.active:
+            n = self.top_rid
+            counts = torch.empty(n, dtype=torch.int32).pin_memory()
+            flags = torch.empty(2, dtype=torch.int32).pin_memory()
+            self._copy(counts.data_ptr(), n * 4, self.done.data_ptr(), n * 4, n * 4, 1)
+            self._copy(flags.data_ptr(), 8, self.flags.data_ptr(), 8, 8, 1)
+            self.poll_ev = torch.cuda.Event()
+            self.poll_ev.record(self.io)
+            self.poll_host = (counts, flags)
+        if self.kernel_ev is not None and self.kernel_ev.query() and (self.draining or self.tail_pending()):
+            if self.tail_pending():
+                self._launch()
+            else:
+                self.draining = False
+        while self.gathers and (block or self.gathers[0][0].query()):
+            ev, host, acts = self.gathers.popleft()
+            ev.synchronize()
+            out.extend(self._results(host, acts, now_fn()))
+        return out
+
+    def tail_pending(self):
+        """Whether admitted lanes may still wait in the ring for a kernel."""
+        return any(not a.retiring for a in self.active.values())
+
+    def _gather(self, done):
+        acts = [self.active[rid] for rid in done]
+        RF, C = self.RF, self.C
+        for a in acts:
+            a.retiring = True
+        host = []
+        for a in acts:
+            n = a.req.state.shape[1]
+            hf = torch.empty((RF, n), dtype=torch.float64).pin_memory()
+            hi = torch.empty((3, n), dtype=torch.int64).pin_memory()
+            self._copy(hf.data_ptr(), n * 8, self.F.data_ptr() + a.start * 8, C * 8, n * 8, RF)
+            self._copy(hi.data_ptr(), n * 8, self.I.data_ptr() + a.start * 8, C * 8, n * 8, 3)
+            host.append((hf, hi))
+        ev = torch.cuda.Event()
+        ev.record(self.io)
+        self.gathers.append((ev, host, acts))
+
+    def _results(self, host, acts, t):
+        ne, R = self.dec.n_eq, self.R
+        out = []
+        for (hf, hi), act in zip(host, acts):
+            h, ints = hf.numpy(), hi.numpy()
+            ns = ints[1].copy()
+            out.append(Result(act.req.rid, self.name, h[:ne].copy(), h[R["thi"]].copy(), ints[0].copy(), ns,
+                              h[R["min_h"]].copy(), h[R["max_h"]].copy(), arrival=act.req.arrival,
+                              admitted=act.admitted, finished=t))
+            self.lane_steps += int(ns.sum())
+            self.ranges.release(act.start, act.req.state.shape[1])
+            del self.active[act.req.rid]
+        return out
+
+    def busy(self):
+        return bool(self.active or self.gathers)
+
+    # the slice interface of LanePool (the resident kernel needs no slices)
+    inflight: deque = deque()
+
+    def depth(self):
+        return 0
+
+    def launch_slice(self):
+        return False
+
+    def close(self):
+        """Stop the kernel (its idle threads return at once) and wait for it.
+        The kernel reads the pool's ring and words while it runs, so it must
+        end before they are freed: Server.run closes its resident pools when
+        the stream is served, and a pool also closes itself when collected."""
+        if self.kernel_ev is not None:
+            self.stop_kernel(wait=True)
+        self.kernel_ev = None
+        self.io.synchronize()
+
+    def __del__(self):
+        try:
+            if self.__dict__.get("kernel_ev") is not None:
+                self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
 class Server:
     """Continuous-batching server over a set of ODE systems.
 
@@ -376,13 +746,23 @@ class Server:
     per lane in one slice; ``quantum_ms``: the target duration of a slice."""
 
     def __init__(self, systems, hbm_budget=2 << 30, slice_iters=1024, device="cuda:0", max_lanes=1 << 21,
-                 quantum_ms=2.0):
+                 quantum_ms=2.0, mode="resident"):
+        if mode not in ("resident", "slice"):
+            raise ValueError("mode must be 'resident' or 'slice'")
         self.pools = {}
+        self.mode = mode
         for name, (sys, tol) in systems.items():
             dec = taylor_decompose(sys)
             bpl = (dec.n_eq + dec.n_pars + 16) * 8
             cap = int(min(max_lanes, hbm_budget // bpl))  # lanes that fit the pool's HBM budget
-            self.pools[name] = LanePool(name, sys, tol, cap, device, slice_iters, quantum_ms * 1e-3)
+            pool = None
+            if mode == "resident":
+                # one resident kernel per system, each on an equal share of the SMs
+                try:
+                    pool = ResidentPool(name, sys, tol, cap, device, grid_share=1.0 / len(systems))
+                except _lib.HykError:
+                    pool = None  # a team-form system: time slices
+            self.pools[name] = pool or LanePool(name, sys, tol, cap, device, slice_iters, quantum_ms * 1e-3)
 
     def run(self, requests, realtime=True):
         """Serve `requests` (with arrival times in seconds); returns the results
@@ -440,7 +820,14 @@ class Server:
                     big = [r for q in waiting.values() for r in q][0]
                     raise RuntimeError("request {} needs more lanes ({}) than its pool holds ({})".format(
                         big.rid, big.state.shape[1], self.pools[big.system].C))
+        self.close()
         return results
+
+    def close(self):
+        """End every resident kernel (none outlives a run)."""
+        for p in self.pools.values():
+            if isinstance(p, ResidentPool):
+                p.close()
 
     def trajectory_steps(self):
         return sum(p.lane_steps for p in self.pools.values())

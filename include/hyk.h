@@ -340,6 +340,60 @@ int hyk_propagate(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, 
 int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode,
                           uint32_t check_every, uint64_t *iters, void *stream);
 
+/* Serving with a device work queue: one launch of a resident kernel that
+ * integrates the lanes the caller appends to a device ring while it runs
+ * (continuous batching without a relaunch per batch).  No counterpart in the
+ * reference (heyoka.py has no server); it serves the same propagate_until
+ * semantics per lane as hyk_propagate.  Lane form modules only.
+ *   lanes, p: the pool's lane arrays and bookkeeping (as for hyk_propagate;
+ *            n_lanes = the pool's capacity).  A lane is made ready by the
+ *            caller writing its state, time, final time, bookkeeping
+ *            (rem_hi/lo = final time - time, outcome, min_h = inf, max_h = 0,
+ *            n_steps = n_iter = 0, status = 0) and owner, then its index at
+ *            ring[tail % ring_capacity], then *tail = tail + 1, in that order
+ *            on one stream (device copies only: while the kernel runs no
+ *            other kernel can start on the SMs it holds).
+ *   ring, ring_capacity (a power of two): the ring of lane indices;
+ *   head: device word, the next ring position to take (advanced by the
+ *         kernel; the caller initialises it once);
+ *   tail: device word, the positions filled so far (advanced by the caller);
+ *   stop: device word; non-zero makes idle threads return;
+ *   owner: (ld) the request of each lane, an index into done_count;
+ *   done_count: per request, the lanes finished so far (incremented by the
+ *         kernel after the lane's results are stored and fenced);
+ *   inflight: device word, lanes being integrated (0 before the first launch);
+ *   status: device word receiving the HYK_SERVE_* reasons threads returned for;
+ *   idle_ns: a thread without work returns after this long with an empty
+ *         ring and no lane in flight; max_wait_ns: after this long waiting in
+ *         any case (every wait of the kernel is bounded);
+ *   grid_ctas: CTAs to launch (0: the GPU's resident capacity; a share of it
+ *         lets the pools of several systems run their kernels side by side). */
+typedef struct hyk_serve {
+    uint64_t *ring;
+    uint64_t ring_capacity;
+    uint64_t *head;
+    const uint64_t *tail;
+    const uint32_t *stop;
+    const int64_t *owner;
+    uint32_t *done_count;
+    uint64_t *inflight;
+    uint32_t *status;
+    uint64_t idle_ns;
+    uint64_t max_wait_ns;
+    uint32_t grid_ctas;
+} hyk_serve_t;
+#define HYK_SERVE_IDLE 1u    /* returned idle: empty ring, nothing in flight for idle_ns */
+#define HYK_SERVE_STOP 2u    /* returned because *stop was set */
+#define HYK_SERVE_TIMEOUT 4u /* a thread waited max_wait_ns for work while others still ran */
+int hyk_serve(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, const hyk_serve_t *s, void *stream);
+
+/* Stream-ordered copy of `height` rows of `width` bytes between host and
+ * device memory (pitches in bytes; either side may be host or device
+ * memory): a copy-engine transfer, never a kernel, so that it runs while a
+ * resident kernel holds the SMs (the serving pool's admissions and result
+ * gathers). */
+int hyk_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height, void *stream);
+
 /* Discrete adjoint of a taped propagation (module created with
  * HYK_CFG_ADJOINT).  For every lane, runs backwards over its n_steps[lane]
  * taped steps: recomputes the step's Taylor coefficients from the taped

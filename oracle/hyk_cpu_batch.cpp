@@ -80,6 +80,7 @@ typedef hyk_v hyk_real;
 #define __forceinline__ inline
 #define __restrict__ __restrict
 static inline void __syncwarp() {}
+#define HYK_WARP_SYNC()
 static inline double hyk_inf() { return HUGE_VAL; }
 
 #define HYK_STR2(x) #x

@@ -6,7 +6,7 @@ import pytest
 import torch
 
 import hyk
-from hyk import serve, workloads as W
+from hyk import _lib, serve, workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -36,13 +36,17 @@ def make_requests(seed=0, n=24):
     return reqs
 
 
-def test_alone_equals_mix_and_batch(libhyk):
+@pytest.mark.parametrize("mode", ["resident", "slice"])
+def test_alone_equals_mix_and_batch(libhyk, mode):
     assert torch.cuda.is_available()
     reqs = make_requests()
-    mix = {r.rid: r for r in serve.Server(systems(), hbm_budget=64 << 20, slice_iters=16).run(reqs, realtime=False)}
+    srv = serve.Server(systems(), hbm_budget=64 << 20, slice_iters=16, mode=mode)
+    if mode == "resident":
+        assert all(isinstance(p, serve.ResidentPool) for p in srv.pools.values())
+    mix = {r.rid: r for r in srv.run(reqs, realtime=True)}
     assert len(mix) == len(reqs)
     for r in reqs[:6]:
-        alone = serve.Server(systems(), hbm_budget=64 << 20, slice_iters=5).run([r], realtime=False)[0]
+        alone = serve.Server(systems(), hbm_budget=64 << 20, slice_iters=5, mode=mode).run([r], realtime=False)[0]
         m = mix[r.rid]
         assert np.array_equal(alone.state, m.state) and np.array_equal(alone.n_steps, m.n_steps)
         assert np.array_equal(alone.min_h, m.min_h) and np.array_equal(alone.max_h, m.max_h)
@@ -55,12 +59,61 @@ def test_alone_equals_mix_and_batch(libhyk):
         assert np.all(m.outcome == int(hyk.taylor_outcome.time_limit))
 
 
-def test_admission_waits_for_capacity(libhyk):
+@pytest.mark.parametrize("mode", ["resident", "slice"])
+def test_admission_waits_for_capacity(libhyk, mode):
     # a pool with room for 100 lanes: requests wait until lanes free up
     reqs = [serve.Request("kepler", W.kepler_ics(60, seed=i), 5.0, arrival=0.0, rid=i) for i in range(5)]
-    srv = serve.Server({"kepler": (W.kepler_sys(), 1e-15)}, hbm_budget=100 * (6 + 16) * 8, slice_iters=8)
+    srv = serve.Server({"kepler": (W.kepler_sys(), 1e-15)}, hbm_budget=100 * (6 + 16) * 8, slice_iters=8, mode=mode)
     assert srv.pools["kepler"].C == 100
     res = srv.run(reqs, realtime=False)
     assert sorted(r.rid for r in res) == list(range(5))
     st = serve.latency_stats(res)
     assert st["n"] == 5 and st["p99_ms"] >= st["p50_ms"] > 0
+
+
+def _pool(**kw):
+    return serve.ResidentPool("kepler", W.kepler_sys(), 1e-15, 4096, "cuda:0", **kw)
+
+
+def _flags(pool):
+    return pool.flags.cpu().numpy()
+
+
+def test_serve_kernel_returns_when_idle(libhyk):
+    """The resident kernel's bounded wait: with an empty ring it returns after
+    idle_ns on its own, reporting HYK_SERVE_IDLE."""
+    pool = _pool(idle_ms=1.0, max_wait_ms=5000.0)
+    pool._launch()
+    pool.kernel_ev.synchronize()
+    assert _flags(pool)[1] & _lib.HYK_SERVE_IDLE
+    assert int(pool.words[2].item()) == 0  # nothing in flight
+
+
+def test_serve_kernel_stop(libhyk):
+    """With the stop word set no thread waits: the launch returns at once."""
+    pool = _pool(idle_ms=60000.0, max_wait_ms=60000.0)
+    pool._launch()
+    pool.stop_kernel(wait=True)
+    assert _flags(pool)[1] & _lib.HYK_SERVE_STOP
+
+
+def test_serve_kernel_timeout_while_a_lane_runs(libhyk):
+    """A thread that waits max_wait_ns for work returns (HYK_SERVE_TIMEOUT)
+    even while another thread still integrates a lane; that lane finishes,
+    is counted, and equals a batch propagation of the same trajectory."""
+    pool = _pool(idle_ms=60000.0, max_wait_ms=20.0)
+    st = W.kepler_ics(1, seed=77)
+    req = serve.Request("kepler", st, 500.0, rid=0)
+    pool.reserve_requests(1)
+    assert pool.admit([req], 0.0) == 1
+    pool.kernel_ev.synchronize()
+    flags = _flags(pool)
+    assert flags[1] & _lib.HYK_SERVE_TIMEOUT
+    assert int(pool.done[0].item()) == 1
+    res = []
+    while not res:
+        res = pool.poll(lambda: 0.0, block=True)
+    ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=1e-15)
+    ta.propagate_until(500.0)
+    assert np.array_equal(res[0].state, np.asarray(ta.state))
+    assert np.array_equal(res[0].n_steps, ta.propagate_res_tensors["n_steps"].cpu().numpy())
