@@ -210,6 +210,8 @@ std::string precision_header(bool pin) {
     if (g_f32) {
         h += "#define HYK_F32 1\n";
         h += "#define HYK_FMA(a, b, c) __fmaf_rn((a), (b), (c))\n";
+        h += "#define HYK_FMAOPS_CONSTS\n#define HYK_MUL(a, b) ((a) * (b))\n#define HYK_ADD(a, b) ((a) + (b))\n"
+             "#define HYK_SUB(a, b) ((a) - (b))\n";
         h += "#define HYK_DM_EXP hyk_dmf_exp\n#define HYK_DM_LOG hyk_dmf_log\n#define HYK_DM_SINCOS hyk_dmf_sincos\n"
              "#define HYK_DM_POW hyk_dmf_pow\n#define HYK_DM_RHO hyk_dmf_rho\n";
     } else {
@@ -1443,6 +1445,40 @@ struct TeamGen {
             }
         }
         std::sort(supd.begin(), supd.end(), [](const Group &x, const Group &y) { return x.key < y.key; });
+        // Slots of the operations in group order (the layout of the
+        // constructor, reordered): the members of a group take consecutive
+        // regions of odd stride, so that the threads of a round (consecutive
+        // members) find their coefficients in distinct shared-memory banks,
+        // and so do the groups that read them in the same member order.
+        {
+            uint32_t s = N * XS;
+            for (auto &lv : levels)
+                for (auto &gr : lv)
+                    for (uint32_t u : gr.members) {
+                        tslot[u] = (int)s;
+                        s += (g.hist[u] && !g.cst[u]) ? HS : 1;
+                    }
+            for (uint32_t i = 0; i < N; ++i)
+                if (g.needka[i]) {
+                    tkslot[i] = (int)s;
+                    s += KS;
+                }
+            for (auto &lv : levels)
+                for (auto &gr : lv)
+                    for (uint32_t u : gr.members)
+                        if (g.needka[u]) {
+                            tkslot[u] = (int)s;
+                            s += KS;
+                        }
+            for (auto &lv : levels)
+                for (auto &gr : lv)
+                    for (uint32_t u : gr.members)
+                        if (tislot[u] >= 0) tislot[u] = (int)s++;
+            if (s != par_slot) {
+                err = "internal: team slot layout";
+                return false;
+            }
+        }
         // Descriptors, group by group.
         auto slot_of = [&](const Ref &r) {
             if (r.kind == HYK_ARG_U) return tslot[r.u];
@@ -1543,13 +1579,13 @@ struct TeamGen {
     void out(uint32_t u, bool n0, const std::string &v) {
         o << "            const hyk_real v = " << v << ";\n";
         o << "            S[D.c" << ((!n0 && g.hist[u]) ? " + n" : "") << "] = v;\n";
-        if (!n0 && g.needka[u]) o << "            S[D.kc + n - 1] = (hyk_real)n * v;\n";
+        if (!n0 && g.needka[u]) o << "            S[D.kc + n - 1] = HYK_MUL((hyk_real)n, v);\n";
     }
 
     void addsub(const std::string &a, const std::string &b, bool add, uint32_t u, bool n0) {
         std::string v;
         if (!a.empty() && !b.empty())
-            v = "(" + a + (add ? " + " : " - ") + b + ")";
+            v = add ? "HYK_ADD(" + a + ", " + b + ")" : "HYK_SUB(" + a + ", " + b + ")";
         else if (!a.empty())
             v = a;
         else if (!b.empty())
@@ -1625,15 +1661,15 @@ struct TeamGen {
         }
         case HYK_OP_MUL:
             if (isU(A) && isU(B)) {
-                o << "            hyk_real acc = " << at(A, 'a', "0") << " * " << at(B, 'b', "n") << ";\n";
+                o << "            hyk_real acc = HYK_MUL(" << at(A, 'a', "0") << ", " << at(B, 'b', "n") << ");\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 1; j <= n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
                   << at(B, 'b', "n - j") << ", acc);\n";
                 out(u, false, "acc");
             } else if (isU(A) && isK(B)) {
-                out(u, false, cur(A, 'a', false) + " * " + K(B, 'b'));
+                out(u, false, "HYK_MUL(" + cur(A, 'a', false) + ", " + K(B, 'b') + ")");
             } else if (isK(A) && isU(B)) {
-                out(u, false, K(A, 'a') + " * " + cur(B, 'b', false));
+                out(u, false, "HYK_MUL(" + K(A, 'a') + ", " + cur(B, 'b', false) + ")");
             } else if (isU(A) && isT(B)) {
                 o << "            hyk_real acc = " << at(A, 'a', "n - 1") << " * " << lit(1.0) << ";\n";
                 o << "            acc = " << fma_ << "(" << at(A, 'a', "n") << ", t0, acc);\n";
@@ -1652,22 +1688,22 @@ struct TeamGen {
             break;
         case HYK_OP_DIV:
             if (isU(B)) {
-                o << "            hyk_real acc = " << at(B, 'b', "1") << " * S[D.c + n - 1];\n";
+                o << "            hyk_real acc = HYK_MUL(" << at(B, 'b', "1") << ", S[D.c + n - 1]);\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << at(B, 'b', "j")
                   << ", S[D.c + n - j], acc);\n";
                 const std::string a = isU(A) ? cur(A, 'a', false) : lit(0.0);
-                out(u, false, "((" + a + " - acc) * S[D.inv])");
+                out(u, false, "HYK_MUL(HYK_SUB(" + a + ", acc), S[D.inv])");
             } else {
-                out(u, false, "(" + cur(A, 'a', false) + " * S[D.inv])");
+                out(u, false, "HYK_MUL(" + cur(A, 'a', false) + ", S[D.inv])");
             }
             break;
         case HYK_OP_SQUARE:
-            o << "            hyk_real acc = " << at(A, 'a', "0") << " * " << at(A, 'a', "n") << ";\n";
+            o << "            hyk_real acc = HYK_MUL(" << at(A, 'a', "0") << ", " << at(A, 'a', "n") << ");\n";
             o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 1; 2 * j < n; ++j) acc = " << fma_ << "(" << at(A, 'a', "j") << ", "
               << at(A, 'a', "n - j") << ", acc);\n";
-            o << "            acc = acc + acc;\n";
+            o << "            acc = HYK_ADD(acc, acc);\n";
             o << "            if ((n & 1) == 0) acc = " << fma_ << "(" << at(A, 'a', "n / 2") << ", "
               << at(A, 'a', "n / 2") << ", acc);\n";
             out(u, false, "acc");
@@ -1675,63 +1711,63 @@ struct TeamGen {
         case HYK_OP_SQRT:
             o << "            hyk_real acc = " << lit(0.0) << ";\n";
             o << "            if (n == 2) {\n";
-            o << "                acc = S[D.c + 1] * S[D.c + 1];\n";
+            o << "                acc = HYK_MUL(S[D.c + 1], S[D.c + 1]);\n";
             o << "            } else if (n > 2) {\n";
-            o << "                acc = S[D.c + 1] * S[D.c + n - 1];\n";
+            o << "                acc = HYK_MUL(S[D.c + 1], S[D.c + n - 1]);\n";
             o << "#pragma unroll " << ju << "\n";
             o << "                for (int j = 2; 2 * j < n; ++j) acc = " << fma_ << "(S[D.c + j], S[D.c + n - j], acc);\n";
-            o << "                acc = acc + acc;\n";
+            o << "                acc = HYK_ADD(acc, acc);\n";
             o << "                if ((n & 1) == 0) acc = " << fma_ << "(S[D.c + n / 2], S[D.c + n / 2], acc);\n";
             o << "            }\n";
-            out(u, false, "(n == 1 ? (" + cur(A, 'a', false) + " * S[D.inv]) : ((" + cur(A, 'a', false) +
-                              " - acc) * S[D.inv]))");
+            out(u, false, "(n == 1 ? HYK_MUL(" + cur(A, 'a', false) + ", S[D.inv]) : HYK_MUL(HYK_SUB(" +
+                              cur(A, 'a', false) + ", acc), S[D.inv]))");
             break;
         case HYK_OP_POW: {
             size_t ai = 0;
             for (; ai < alphas.size(); ++ai)
                 if (std::memcmp(&alphas[ai], &op.b.num, sizeof(double)) == 0) break;
             const std::string pc = "hyk_pc" + std::to_string(ai) + "[n * (HYK_ORDER + 1)";
-            o << "            hyk_real acc = (" << pc << "] * " << at(A, 'a', "n") << ") * S[D.c];\n";
+            o << "            hyk_real acc = HYK_MUL(HYK_MUL(" << pc << "], " << at(A, 'a', "n") << "), S[D.c]);\n";
             o << "#pragma unroll " << ju << "\n";
-            o << "            for (int j = 1; j < n; ++j) acc = " << fma_ << "(" << pc << " + j] * "
-              << at(A, 'a', "n - j") << ", S[D.c + j], acc);\n";
-            out(u, false, "((acc * hyk_invn[n]) * S[D.inv])");
+            o << "            for (int j = 1; j < n; ++j) acc = " << fma_ << "(HYK_MUL(" << pc << " + j], "
+              << at(A, 'a', "n - j") << "), S[D.c + j], acc);\n";
+            out(u, false, "HYK_MUL(HYK_MUL(acc, hyk_invn[n]), S[D.inv])");
             break;
         }
         case HYK_OP_EXP:
             if (isT(A)) {  // d(t)/dt = 1: the single term j = 1
                 o << "            const hyk_real acc = " << lit(1.0) << " * S[D.c + n - 1];\n";
-                out(u, false, "(acc * hyk_invn[n])");
+                out(u, false, "HYK_MUL(acc, hyk_invn[n])");
                 break;
             }
-            o << "            hyk_real acc = " << wrap(A, "S[D.ka]") << " * S[D.c + n - 1];\n";
+            o << "            hyk_real acc = HYK_MUL(" << wrap(A, "S[D.ka]") << ", S[D.c + n - 1]);\n";
             o << "#pragma unroll " << ju << "\n";
             o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
               << ", S[D.c + n - j], acc);\n";
-            out(u, false, "(acc * hyk_invn[n])");
+            out(u, false, "HYK_MUL(acc, hyk_invn[n])");
             break;
         case HYK_OP_LOG:
             o << "            hyk_real acc = " << lit(0.0) << ";\n";
             o << "            if (n >= 2) {\n";
-            o << "                acc = S[D.kc] * " << at(A, 'a', "n - 1") << ";\n";
+            o << "                acc = HYK_MUL(S[D.kc], " << at(A, 'a', "n - 1") << ");\n";
             o << "#pragma unroll " << ju << "\n";
             o << "                for (int j = 2; j < n; ++j) acc = " << fma_ << "(S[D.kc + j - 1], " << at(A, 'a', "n - j")
               << ", acc);\n";
             o << "            }\n";
-            out(u, false, "(n == 1 ? (" + cur(A, 'a', false) + " * S[D.inv]) : ((" + cur(A, 'a', false) +
-                              " - (acc * hyk_invn[n])) * S[D.inv]))");
+            out(u, false, "(n == 1 ? HYK_MUL(" + cur(A, 'a', false) + ", S[D.inv]) : HYK_MUL(HYK_SUB(" +
+                              cur(A, 'a', false) + ", HYK_MUL(acc, hyk_invn[n])), S[D.inv]))");
             break;
         case HYK_OP_SIN:
         case HYK_OP_COS:
             if (isT(A)) {
                 o << "            const hyk_real acc = " << lit(1.0) << " * S[D.prt + n - 1];\n";
             } else {
-                o << "            hyk_real acc = " << wrap(A, "S[D.ka]") << " * S[D.prt + n - 1];\n";
+                o << "            hyk_real acc = HYK_MUL(" << wrap(A, "S[D.ka]") << ", S[D.prt + n - 1]);\n";
                 o << "#pragma unroll " << ju << "\n";
                 o << "            for (int j = 2; j <= n; ++j) acc = " << fma_ << "(" << wrap(A, "S[D.ka + j - 1]")
                   << ", S[D.prt + n - j], acc);\n";
             }
-            out(u, false, op.op == HYK_OP_SIN ? "(acc * hyk_invn[n])" : "(-(acc * hyk_invn[n]))");
+            out(u, false, op.op == HYK_OP_SIN ? "HYK_MUL(acc, hyk_invn[n])" : "(-HYK_MUL(acc, hyk_invn[n]))");
             break;
         }
         o << "        }\n";
@@ -1759,14 +1795,14 @@ struct TeamGen {
         else if (isT(R) && !n0)
             v = "(n == 1 ? (" + lit(1.0) + " * hyk_invn[2]) : " + lit(0.0) + ")";
         else
-            v = "(" + f + " * hyk_invn[" + nn + "])";
+            v = "HYK_MUL(" + f + ", hyk_invn[" + nn + "])";
         o << "            const hyk_real v = " << v << ";\n";
         o << "            S[D.c + " << nn << "] = v;\n";
         if (g.needka[i]) {
             if (n0)
                 o << "            if (1 < HYK_ORDER) S[D.kc] = " << lit(1.0) << " * v;\n";
             else
-                o << "            if (n + 1 < HYK_ORDER) S[D.kc + n] = (hyk_real)(n + 1) * v;\n";
+                o << "            if (n + 1 < HYK_ORDER) S[D.kc + n] = HYK_MUL((hyk_real)(n + 1), v);\n";
         }
         o << "        }\n";
     }
@@ -1805,6 +1841,7 @@ struct TeamGen {
             o << "};\n";
         }
         o << "static __device__ __noinline__ void hyk_tjets(hyk_real *__restrict__ S, const hyk_real t0, const int r) {\n";
+        o << "    HYK_FMAOPS_CONSTS\n";
         o << "    __syncwarp();\n";
         o << "    {\n        // ---- order 0\n";
         emit_order(true);
