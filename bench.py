@@ -42,8 +42,8 @@ T_END = 200.0
 TOL = 1e-15
 
 # DRAM traffic of one persistent Kepler launch per lane, from ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum = 2.65 MB for 2^14 orbits).
-KEPLER_DRAM_BYTES_PER_LANE = 2.65e6 / 16384
+# (dram__bytes_read.sum + dram__bytes_write.sum = 18.55 MB + 1.65 MB for 2^17 orbits).
+KEPLER_DRAM_BYTES_PER_LANE = (18.546e6 + 1.652e6) / 131072
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -1015,10 +1015,11 @@ def main():
                 "unit": "TFLOP/s",
                 "frac": achieved / peak,
                 # DRAM bytes per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum of one
-                # 2^14-orbit launch (2.65 MB, one load and one store of each lane's state and
-                # bookkeeping), scaled by the lanes of this launch (the traffic is per lane)
+                # 2^17-orbit launch (20.2 MB, one load and one store of each lane's state and
+                # bookkeeping; the cold-row buffer stays in L2), scaled by the lanes of this
+                # launch (the traffic is per lane)
                 "traffic": KEPLER_DRAM_BYTES_PER_LANE * n,
-                "traffic_source": "ncu capture of a 2^14-orbit launch, scaled by lanes",
+                "traffic_source": "ncu capture of a 2^17-orbit launch, scaled by lanes",
                 "kernel": "hyk_prop_kernel (persistent)",
                 "flops_per_traj_step": flops_step,
                 "peak_source": "measured in-process FP64 FMA probe (hyk_fp64_peak), of measured",
