@@ -12,7 +12,9 @@ value: trajectory-steps/s (sum over lanes of accepted non-zero steps / time)
 of the persistent batched kernel.  e2e: the same metric through the public
 API with the state copied from pinned host memory before, and the state and
 step counts copied back after, every step.  paths.plain: the one-launch-per-
-step form on the same workload.  roofline: algorithmic FP64 flops of the
+step form over the unfinished lanes (listed before each launch);
+paths.plain_inplace: one launch per step over every lane (the naive drop-in
+form).  roofline: algorithmic FP64 flops of the
 propagation kernel / its CUDA-event duration, against the FP64 FMA peak
 measured in the same process.  cpu_baseline: the compiled CPU stepper that
 stands in for the reference's compiled batch stepper (generated recurrences in
@@ -970,6 +972,19 @@ def main():
         ps = int(tp.propagate_res_tensors["n_steps"].sum().item())
         paths["plain"] = ps / (a.elapsed_time(b) / 1e3)
         paths["persistent_over_plain"] = value / paths["plain"]
+        # the naive drop-in form: one launch per step over every lane (the
+        # reference's batch step called in a loop), finished lanes included
+        tp.prop_mode = "plain_inplace"
+        tp.set_time(0.0)
+        tp.state[:] = st
+        barrier()
+        a.record(stream)
+        tp.propagate_until(T_END)
+        b.record(stream)
+        barrier()
+        ps = int(tp.propagate_res_tensors["n_steps"].sum().item())
+        paths["plain_inplace"] = ps / (a.elapsed_time(b) / 1e3)
+        paths["persistent_over_plain_inplace"] = value / paths["plain_inplace"]
         del tp
 
     cpu = None

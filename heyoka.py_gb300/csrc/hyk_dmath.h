@@ -17,9 +17,13 @@
  *  log:  x = 2^e m with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
  *        s = (m - 1) / (m + 1), by the odd series to s^23 (|s| <= 0.1716);
  *        e ln2 added with a two-part ln2.
- *  sin/cos: x = k pi/2 + r with a three-part pi/2 (accurate for |x| < 2^30),
- *        Taylor series to r^17 (sine) and r^18 (cosine) on |r| <= pi/4,
- *        quadrant selection from k mod 4.
+ *  sin/cos: x = k pi/2 + r with a three-part pi/2 for |x| < 2^30; for
+ *        larger |x| the reduction of Payne and Hanek ("Radian reduction for
+ *        trigonometric functions", SIGNUM Newsletter 18(1), 1983): the
+ *        fraction of x 2/pi from the bits of 2/pi that matter at x's
+ *        exponent, in 128-bit integer arithmetic, exact for every double;
+ *        then the Taylor series to r^17 (sine) and r^18 (cosine) on
+ *        |r| <= pi/4, quadrant selection from k mod 4.
  *  pow with a constant exponent: integer and half-integer exponents by
  *        products, one square root and one division; other exponents as
  *        exp(alpha log x).
@@ -151,6 +155,103 @@ HYK_DM_FN double hyk_dm_log(double x) {
     return HYK_DM_FMA(ed, 0.6931471805599453, HYK_DM_FMA(ed, 2.3190468138462996e-17, lm));
 }
 
+/* The binary digits of 2/pi, 64 per word, most significant first, after one
+ * word of zeros (the digits of weight 2^0 and above): word j >= 1 holds the
+ * digits of weight 2^-(64(j-1)+1) .. 2^-64j.  The 19 words after the zero
+ * word are floor(2/pi 2^1216) (computed with mpmath at 1536 bits), enough
+ * for the largest double exponent. */
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+static __device__ const unsigned long long hyk_dm_2opi[20] = {
+#else
+static const unsigned long long hyk_dm_2opi[20] = {
+#endif
+    0x0000000000000000ULL, 0xa2f9836e4e441529ULL, 0xfc2757d1f534ddc0ULL, 0xdb6295993c439041ULL,
+    0xfe5163abdebbc561ULL, 0xb7246e3a424dd2e0ULL, 0x06492eea09d1921cULL, 0xfe1deb1cb129a73eULL,
+    0xe88235f52ebb4484ULL, 0xe99c7026b45f7e41ULL, 0x3991d639835339f4ULL, 0x9c845f8bbdf9283bULL,
+    0x1ff897ffde05980fULL, 0xef2f118b5a0a6d1fULL, 0x6d367ecf27cb09b7ULL, 0x4f463f669e5fea2dULL,
+    0x7527bac7ebe5f17bULL, 0x3d0739f78a5292eaULL, 0x6bfb5fb11f8d5d08ULL, 0x56033046fc7b6babULL,
+};
+
+/* High 64 bits of the 128-bit product of two 64-bit integers, and the
+ * leading zeros of a non-zero 64-bit integer. */
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+HYK_DM_FN unsigned long long hyk_dm_mulhi(unsigned long long a, unsigned long long b) { return __umul64hi(a, b); }
+HYK_DM_FN int hyk_dm_clz(unsigned long long a) { return __clzll((long long)a); }
+#else
+HYK_DM_FN unsigned long long hyk_dm_mulhi(unsigned long long a, unsigned long long b) {
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+}
+HYK_DM_FN int hyk_dm_clz(unsigned long long a) { return __builtin_clzll(a); }
+#endif
+
+/* 2^e as a double, -1022 <= e <= 1023. */
+HYK_DM_FN double hyk_dm_pow2(int e) { return HYK_DM_FROM((unsigned long long)(1023 + e) << 52); }
+
+/* Reduction of a finite |x| >= 2^30: r = x - k pi/2 with |r| <= pi/4 and
+ * q = k mod 4.  With x = m 2^E (m the 53-bit integer significand) and
+ * 2/pi = sum_i b_i 2^-i, the terms of x 2/pi with i < E - 1 are multiples of
+ * 4, so x 2/pi = 4 frac(m W) (mod 4) where W = 0.b_(E-1) b_E ... is read
+ * from the table (192 digits: the error of the fraction is below 2^-128).
+ * The nearest quarter of 4 frac(m W) gives q, the signed remainder y times
+ * pi/2 (as two doubles) gives r. */
+HYK_DM_FN double hyk_dm_reduce_big(double x, unsigned *qp) {
+    const unsigned long long u = HYK_DM_BITS(x);
+    const int E = (int)((u >> 52) & 0x7ffULL) - 1075;
+    const unsigned long long m = (u & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+    const int P0 = E + 62; /* table digit (from the start of word 0) of b_(E-1) */
+    const int k = P0 >> 6, sh = P0 & 63;
+    const unsigned long long t0 = hyk_dm_2opi[k], t1 = hyk_dm_2opi[k + 1], t2 = hyk_dm_2opi[k + 2],
+                             t3 = hyk_dm_2opi[k + 3];
+    const unsigned long long w0 = sh ? (t0 << sh) | (t1 >> (64 - sh)) : t0;
+    const unsigned long long w1 = sh ? (t1 << sh) | (t2 >> (64 - sh)) : t1;
+    const unsigned long long w2 = sh ? (t2 << sh) | (t3 >> (64 - sh)) : t2;
+    /* frac(m W) = 0.f1 f2 (the integer part of m W is dropped) */
+    const unsigned long long l0 = m * w0, h1 = hyk_dm_mulhi(m, w1), l1 = m * w1, h2 = hyk_dm_mulhi(m, w2);
+    const unsigned long long f2 = l1 + h2;
+    const unsigned long long f1 = l0 + h1 + (f2 < l1 ? 1ULL : 0ULL);
+    /* 4 frac(m W) = q0 + g, g = 0.g1 g2 in [0, 1) */
+    unsigned q = (unsigned)(f1 >> 62);
+    unsigned long long g1 = (f1 << 2) | (f2 >> 62), g2 = f2 << 2;
+    bool neg = false;
+    if (g1 >> 63) { /* g >= 1/2: the nearest integer is q0 + 1 and y = g - 1 */
+        q += 1;
+        neg = true;
+        g2 = ~g2 + 1ULL;
+        g1 = ~g1 + (g2 == 0 ? 1ULL : 0ULL);
+    }
+    double r = 0.0;
+    if (g1 | g2) {
+        /* |y| = 0.g1 g2 normalised: its top 64 digits n1, then n2 */
+        const int lz = g1 ? hyk_dm_clz(g1) : 64 + hyk_dm_clz(g2);
+        unsigned long long n1, n2;
+        if (lz >= 64) {
+            n1 = g2 << (lz - 64);
+            n2 = 0;
+        } else if (lz > 0) {
+            n1 = (g1 << lz) | (g2 >> (64 - lz));
+            n2 = g2 << lz;
+        } else {
+            n1 = g1;
+            n2 = g2;
+        }
+        /* |y| = (n1 + n2 2^-64) 2^(-64 - lz) = yh + yl */
+        const double sc = hyk_dm_pow2(-64 - lz);
+        const double yh = (double)(n1 >> 11) * (2048.0 * sc);
+        const double yl = ((double)(n1 & 0x7ffULL) + (double)(n2 >> 11) * 1.1102230246251565e-16) * sc;
+        /* r = |y| pi/2 with pi/2 = 1.5707963267948966 + 6.123233995736766e-17 */
+        const double p = yh * 1.5707963267948966;
+        const double pe = HYK_DM_FMA(yh, 1.5707963267948966, -p);
+        r = p + (pe + HYK_DM_FMA(yh, 6.123233995736766e-17, yl * 1.5707963267948966));
+        if (neg) r = -r;
+    }
+    if (x < 0.0) {
+        r = -r;
+        q = 0u - q;
+    }
+    *qp = q & 3u;
+    return r;
+}
+
 /* sin and cos of x together. */
 HYK_DM_FN void hyk_dm_sincos(double x, double *sp, double *cp) {
     const unsigned long long u = HYK_DM_BITS(x);
@@ -159,12 +260,18 @@ HYK_DM_FN void hyk_dm_sincos(double x, double *sp, double *cp) {
         *cp = HYK_DM_NAN;
         return;
     }
-    const double t = HYK_DM_FMA(x, 0.6366197723675814, HYK_DM_RND);
-    const double kd = t - HYK_DM_RND;
-    const unsigned q = (unsigned)(HYK_DM_BITS(t) & 3ULL);
-    double r = HYK_DM_FMA(-kd, 1.5707963267948966, x);
-    r = HYK_DM_FMA(-kd, 6.123233995736766e-17, r);
-    r = HYK_DM_FMA(-kd, -1.4973849048591698e-33, r);
+    unsigned q;
+    double r;
+    if ((u & 0x7fffffffffffffffULL) < 0x41d0000000000000ULL) { /* |x| < 2^30 */
+        const double t = HYK_DM_FMA(x, 0.6366197723675814, HYK_DM_RND);
+        const double kd = t - HYK_DM_RND;
+        q = (unsigned)(HYK_DM_BITS(t) & 3ULL);
+        r = HYK_DM_FMA(-kd, 1.5707963267948966, x);
+        r = HYK_DM_FMA(-kd, 6.123233995736766e-17, r);
+        r = HYK_DM_FMA(-kd, -1.4973849048591698e-33, r);
+    } else {
+        r = hyk_dm_reduce_big(x, &q);
+    }
     const double z = r * r;
     double ps = 2.8114572543455206e-15;  // 1/17!
     ps = HYK_DM_FMA(ps, z, -7.647163731819816e-13);
@@ -324,6 +431,15 @@ HYK_DM_FN void hyk_dmf_sincos(float x, float *sp, float *cp) {
     if ((u & 0x7f800000u) == 0x7f800000u) {
         *sp = HYK_DM_FFROM(0x7fc00000u);
         *cp = HYK_DM_FFROM(0x7fc00000u);
+        return;
+    }
+    if ((u & 0x7fffffffu) >= 0x47800000u) {
+        /* |x| >= 2^16: the float reduction's k pi/2 is no longer exact; the
+         * double functions (exact reduction), rounded to float */
+        double sd, cd;
+        hyk_dm_sincos((double)x, &sd, &cd);
+        *sp = (float)sd;
+        *cp = (float)cd;
         return;
     }
     const float t = HYK_DM_FMAF(x, 0.636619747f, HYK_DMF_RND);

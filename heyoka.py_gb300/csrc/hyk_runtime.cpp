@@ -10,6 +10,7 @@
 #include <cuda.h>
 #include <dlfcn.h>
 #include <nvrtc.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -27,6 +28,25 @@
 
 #include "hyk.h"
 #include "hyk_internal.hpp"
+
+namespace {
+// NVTX range over a host-side phase (compile, launch sequence, graph build),
+// visible in Nsight Systems / Nsight Compute timelines; costs nothing
+// without a tool attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name, bool on = true) : on_(on) {
+        if (on_) nvtxRangePushA(name);
+    }
+    ~NvtxRange() {
+        if (on_) nvtxRangePop();
+    }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+
+  private:
+    bool on_;
+};
+}  // namespace
 
 // Generic kernels compiled by nvcc into this library (hyk_generic.cu).
 extern "C" int hyk_generic_dense_eval(const double *tc, uint32_t n_eq, uint32_t order, uint64_t n_lanes, uint64_t ld,
@@ -48,7 +68,7 @@ thread_local std::string g_err;
 // driver entry point goes through this table.
 #define HYK_STR2(x) #x
 #define HYK_STR(x) HYK_STR2(x)
-#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy) X(cuModuleGetGlobal) X(cuMemcpyHtoD) X(cuMemcpy2DAsync)
+#define HYK_DRIVER_FNS(X) X(cuInit) X(cuDeviceGet) X(cuDevicePrimaryCtxRetain) X(cuDeviceGetAttribute) X(cuCtxSetCurrent) X(cuModuleLoadData) X(cuModuleGetFunction) X(cuFuncSetAttribute) X(cuFuncGetAttribute) X(cuOccupancyMaxActiveBlocksPerMultiprocessor) X(cuModuleUnload) X(cuLaunchKernel) X(cuMemsetD32Async) X(cuMemcpyDtoHAsync) X(cuStreamSynchronize) X(cuGetErrorString) X(cuMemAlloc) X(cuMemFree) X(cuGraphCreate) X(cuGraphAddKernelNode) X(cuGraphInstantiate) X(cuGraphLaunch) X(cuGraphExecDestroy) X(cuGraphDestroy) X(cuModuleGetGlobal) X(cuMemcpyHtoD) X(cuMemcpy2DAsync) X(cuMemcpyDtoH) X(cuMemsetD8)
 
 struct DriverApi {
 #define HYK_DECL(f) decltype(&::f) f = nullptr;
@@ -208,6 +228,7 @@ std::string cache_dir() {
 }
 
 int compile_nvrtc(const std::string &src, const std::string &name, std::string &cubin, std::string &log) {
+    NvtxRange nv("hyk: NVRTC compile");
     nvrtcProgram prog;
     nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), name.c_str(), 0, nullptr, nullptr);
     if (r != NVRTC_SUCCESS) return fail(HYK_ERR_NVRTC, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
@@ -275,6 +296,7 @@ const char *hyk_last_error(void) { return g_err.c_str(); }
 const char *hyk_version(void) { return "hyk 0.1 (sm_103a, FP64 and FP32 Taylor, NVRTC)"; }
 
 int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t *cfg, int device, hyk_module **out) {
+    NvtxRange nv("hyk: module create");
     if (!out) return fail(HYK_ERR_INVALID, "null output pointer");
     *out = nullptr;
     std::unique_ptr<hyk_module> m(new hyk_module());
@@ -456,7 +478,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         return fail(HYK_ERR_INVALID, err);
     }
     if (g.n_slot != nslot || g.n_cold != m->ncold) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
-    m->src = g.src;
+    m->src = (m->cfg.flags & HYK_CFG_DEBUG) ? "#define HYK_DEBUG 1\n" + g.src : g.src;
     m->flops = g.flops;
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -595,6 +617,19 @@ int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info) {
 
 const char *hyk_module_source(const hyk_module *m) { return m ? m->src.c_str() : ""; }
 
+int hyk_module_debug(hyk_module *m, uint64_t out[8], int clear) {
+    if (!m || !out) return fail(HYK_ERR_INVALID, "null argument");
+    if (!(m->cfg.flags & HYK_CFG_DEBUG)) return fail(HYK_ERR_INVALID, "the module was not created with HYK_CFG_DEBUG");
+    HYK_CU(drv().cuCtxSetCurrent(m->dv->ctx));
+    CUdeviceptr rec = 0;
+    size_t bytes = 0;
+    HYK_CU(drv().cuModuleGetGlobal(&rec, &bytes, m->mod, "hyk_dbg"));
+    if (bytes != 8 * sizeof(uint64_t)) return fail(HYK_ERR_INVALID, "internal: hyk_dbg size");
+    HYK_CU(drv().cuMemcpyDtoH(out, rec, bytes));
+    if (clear) HYK_CU(drv().cuMemsetD8(rec, 0, bytes));
+    return 0;
+}
+
 static int check_lanes(const hyk_module *m, const hyk_lanes_t *l) {
     if (!m || !l) return fail(HYK_ERR_INVALID, "null argument");
     if (l->n_lanes == 0) return 0;
@@ -682,6 +717,7 @@ struct PlainRound {
 };
 
 static int build_graph(hyk_module *m, const PlainRound &round, KParams &k, LaunchGraph &lg) {
+    NvtxRange nv("hyk: build step graph");
     k.jets = reinterpret_cast<double *>(m->jets);
     HYK_CU(drv().cuGraphCreate(&lg.g, 0));
     void *args[] = {&k};
@@ -725,6 +761,7 @@ static int fill_events(const hyk_module *m, KParams &k, const hyk_prop_t *p) {
 
 int hyk_step(hyk_module *m, const hyk_lanes_t *lanes, const double *max_delta_t, int backward, int64_t *outcome,
              double *h, double *tc, const struct hyk_prop *ev, void *stream) {
+    NvtxRange nv("hyk: step");
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (!outcome || !h) return fail(HYK_ERR_INVALID, "null outcome or h pointer");
@@ -818,6 +855,8 @@ size_t hyk_propagate_workspace_size(const hyk_module *m, uint64_t n_lanes, int m
 // (hyk_propagate_noalloc, whose callers must not allocate).
 static int propagate_impl(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, int mode, void *workspace,
                           size_t workspace_bytes, uint32_t check_every, uint64_t *iters, void *stream, bool use_graphs) {
+    // (no NVTX call on the no-allocation path: a tool's NVTX handler may allocate)
+    NvtxRange nv(mode == HYK_MODE_PERSISTENT ? "hyk: propagate (persistent)" : "hyk: propagate (plain)", use_graphs);
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (iters) *iters = 0;
@@ -933,6 +972,7 @@ int hyk_propagate_noalloc(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
 }
 
 int hyk_serve(hyk_module *m, const hyk_lanes_t *lanes, const hyk_prop_t *p, const hyk_serve_t *sv, void *stream) {
+    NvtxRange nv("hyk: serve launch");
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (!m->f_serve) return fail(HYK_ERR_UNSUPPORTED, "serving with a device work queue needs a lane-form module");
@@ -987,6 +1027,7 @@ int hyk_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_
 int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,
                 const int64_t *n_steps, double *lambda, double *pbar, void *workspace, size_t workspace_bytes,
                 void *stream) {
+    NvtxRange nv("hyk: adjoint");
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
     if (!m->f_adj) return fail(HYK_ERR_INVALID, "the module was not created with HYK_CFG_ADJOINT");
@@ -1087,6 +1128,7 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (log && log_len) std::snprintf(log, log_len, "%s", g.src.c_str());
         return 0;
     }
+    if (cfg && (cfg->flags & HYK_CFG_DEBUG)) g.src = "#define HYK_DEBUG 1\n" + g.src;
     if (verbose) setenv("HYK_PTXAS_VERBOSE", "1", 1);
     std::string cubin, lg;
     const int rc = compile_nvrtc(g.src, "hyk_check.cu", cubin, lg);

@@ -41,6 +41,10 @@ HYK_CFG_HIGH_ACCURACY = 4
 HYK_CFG_GLOBAL_JETS = 8
 HYK_CFG_FLOAT32 = 16
 HYK_CFG_NO_COLD_ROWS = 32
+HYK_CFG_DEBUG = 64
+HYK_DBG_LANE_RANGE = 1
+HYK_DBG_NONFINITE_JET = 2
+HYK_DBG_CAPACITY = 4
 
 LANE_DONE, LANE_STOPPED, LANE_CAPACITY, LANE_EVENT = 1, 2, 4, 8
 OC_EV_OVERFLOW = -4294967310
@@ -154,6 +158,7 @@ SIGNATURES = {
     "hyk_module_destroy": (c_int, [c_vp]),
     "hyk_module_get_info": (c_int, [c_vp, P(hyk_module_info_t)]),
     "hyk_module_source": (ctypes.c_char_p, [c_vp]),
+    "hyk_module_debug": (c_int, [c_vp, c_vp, c_int]),
     "hyk_step": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_int, c_vp, c_vp, c_vp, P(hyk_prop_t), c_vp]),
     "hyk_prop_init": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_vp]),
     "hyk_propagate_workspace_size": (ctypes.c_size_t, [c_vp, c_u64, c_int]),

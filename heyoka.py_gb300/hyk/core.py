@@ -19,7 +19,7 @@ class Module:
 
     def __init__(self, dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False,
                  team_size: int = 0, persist_ctas: int = 0, high_accuracy: bool = False, global_jets: bool = False,
-                 float32: bool = False, cold_rows: bool = True):
+                 float32: bool = False, cold_rows: bool = True, debug: bool = False):
         L = _lib.load()
         self.dec, self.order, self.device = dec, int(order), int(device)
         self._cdec, self._keep = dec.as_c()
@@ -27,6 +27,8 @@ class Module:
         flags |= _lib.HYK_CFG_GLOBAL_JETS if global_jets else 0
         flags |= _lib.HYK_CFG_FLOAT32 if float32 else 0
         flags |= 0 if cold_rows else _lib.HYK_CFG_NO_COLD_ROWS
+        flags |= _lib.HYK_CFG_DEBUG if debug else 0
+        self.debug = bool(debug)
         self.float32 = bool(float32)
         cfg = _lib.hyk_config_t(int(block_lanes), int(persist_ctas), flags, int(team_size))
         h = ctypes.c_void_p()
@@ -58,6 +60,28 @@ class Module:
         except Exception:  # noqa: BLE001 - interpreter shutdown: nothing left to free
             pass
 
+    def debug_record(self, clear: bool = False):
+        """The debug record of a module built with ``debug=True`` (the
+        device synchronised first): the codes seen, the number of findings
+        and the first one."""
+        import numpy as np
+
+        torch.cuda.synchronize(self.device)
+        out = np.zeros(8, dtype=np.uint64)
+        _lib.check(_lib.load().hyk_module_debug(self.handle, out.ctypes.data, int(bool(clear))), "hyk_module_debug")
+        names = {_lib.HYK_DBG_LANE_RANGE: "lane_range", _lib.HYK_DBG_NONFINITE_JET: "nonfinite_jet",
+                 _lib.HYK_DBG_CAPACITY: "capacity"}
+        codes = int(out[0])
+        rec = {"codes": [n for c, n in names.items() if codes & c], "count": int(out[1]), "first": None}
+        if out[1]:
+            c = int(out[2])
+            d = [int(x) for x in out[3:7]]
+            keys = {_lib.HYK_DBG_LANE_RANGE: ("index", "n_lanes", "position", None),
+                    _lib.HYK_DBG_NONFINITE_JET: ("lane", "variable", "order", "iteration"),
+                    _lib.HYK_DBG_CAPACITY: ("lane", "iteration", None, None)}.get(c, ("a", "b", "c", "d"))
+            rec["first"] = dict({"code": names.get(c, str(c))}, **{k: v for k, v in zip(keys, d) if k})
+        return rec
+
     @property
     def source(self) -> str:
         return _lib.load().hyk_module_source(self.handle).decode()
@@ -83,14 +107,14 @@ class Module:
 
 def get_module(dec: Decomposition, order: int, device: int, block_lanes: int = 0, pin_arith: bool = False,
                team_size: int = 0, persist_ctas: int = 0, high_accuracy: bool = False,
-               global_jets: bool = False, float32: bool = False, cold_rows: bool = True) -> Module:
+               global_jets: bool = False, float32: bool = False, cold_rows: bool = True, debug: bool = False) -> Module:
     key = (dec.digest(), int(order), int(device), int(block_lanes), bool(pin_arith), int(team_size), int(persist_ctas),
-           bool(high_accuracy), bool(global_jets), bool(float32), bool(cold_rows))
+           bool(high_accuracy), bool(global_jets), bool(float32), bool(cold_rows), bool(debug))
     with _cache_lock:
         m = _modules.get(key)
         if m is None:
             m = Module(dec, order, device, block_lanes, pin_arith, team_size, persist_ctas, high_accuracy, global_jets,
-                       float32, cold_rows)
+                       float32, cold_rows, debug)
             _modules[key] = m
         return m
 

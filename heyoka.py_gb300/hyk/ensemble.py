@@ -16,6 +16,15 @@ last step of lanes that finished early) are applied per iteration.
 ``algorithm`` and ``max_workers`` are accepted for compatibility and do not
 change the computation; ``chunksize`` is accepted with ``algorithm="process"``
 only, as in the reference.
+
+``devices=[d0, d1, ...]`` (no counterpart in the reference, whose workers are
+host threads or processes: heyoka/_ensemble_impl.py:46-138) spreads the
+iterations over several GPUs: contiguous ranges of iterations, one per entry,
+each propagated as one device batch by a replica of the template on its GPU
+(its own module there), the GPUs driven from one host thread each, and the
+per-iteration results concatenated in iteration order.  Trajectories are
+independent, so nothing is exchanged between GPUs.  A GPU named more than once
+runs its ranges one after the other.
 """
 
 from __future__ import annotations
@@ -113,8 +122,53 @@ def _validate(tp, arg, n_iter, kwargs):
     return arg
 
 
+def _ensemble_devices(tp, ta, arg, n_iter, gen, devices, kwargs):
+    """The multi-GPU ensemble: iteration ranges per device (shard.partition),
+    one host thread per distinct device, results in iteration order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from . import shard
+    from .integrator import _dev_index
+    from .scalar import taylor_adaptive
+
+    devs = [_dev_index(d) for d in devices]
+    if not devs:
+        raise ValueError("the devices argument must name at least one GPU")
+    _validate(tp, arg, n_iter, dict(kwargs))  # the single-device path's errors, before any work
+    if n_iter == 0:
+        return []
+    scalar = isinstance(ta, taylor_adaptive)
+    base = ta._b if scalar else ta
+    if not isinstance(base, taylor_adaptive_batch):
+        raise TypeError("the GPU ensemble propagation needs a hyk.taylor_adaptive or hyk.taylor_adaptive_batch "
+                        "template integrator")
+    templates = {}
+    for d in dict.fromkeys(devs):
+        r = base if d == base._dev else base._replica(d)
+        templates[d] = taylor_adaptive._wrap(r) if (scalar and r is not base) else (ta if r is base else r)
+    ranges: dict = {}
+    for (lo, hi), d in zip(shard.partition(n_iter, len(devs)), devs):
+        if hi > lo:
+            ranges.setdefault(d, []).append((lo, hi))
+
+    def run(d):
+        out = []
+        for lo, hi in ranges[d]:
+            part = _ensemble(tp, templates[d], arg, hi - lo, lambda c, i, lo=lo: gen(c, lo + i), **dict(kwargs))
+            out.append((lo, part))
+        return out
+
+    with ThreadPoolExecutor(max_workers=len(ranges)) as ex:
+        done = list(ex.map(run, list(ranges)))
+    return [x for _, part in sorted((p for r in done for p in r), key=lambda p: p[0]) for x in part]
+
+
 def _ensemble(tp, ta, arg, n_iter, gen, **kwargs):
     from .scalar import continuous_output, taylor_adaptive
+
+    devices = kwargs.pop("devices", None)
+    if devices is not None:
+        return _ensemble_devices(tp, ta, arg, n_iter, gen, devices, kwargs)
 
     scalar = isinstance(ta, taylor_adaptive)  # a scalar template: one lane per iteration
     if scalar:

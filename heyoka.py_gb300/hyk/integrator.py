@@ -17,18 +17,22 @@ follow from living on a GPU:
 * Step callbacks (``callback=``: one callable, an object with ``pre_hook``, or
   a list) run on the host after each batch step; the persistent kernel then
   advances every lane by one step per launch, so a propagation with a
-  callback runs at one launch and one host round trip per step.  Events run on the
-  device; their callbacks run on the host when the step or propagation
-  returns (``hyk/events.py``).
+  callback runs at one launch and one host round trip per step.  Events are
+  detected on the device; with ``batch_semantics="reference"`` (the default)
+  their callbacks run on the host after each batch step, as in the reference,
+  and with ``"lane"`` when the propagation returns (``hyk/events.py``).
 * ``propagate_*`` run every lane to its own final time in one persistent
-  kernel launch (``prop_mode="persistent"``, the default) or with one kernel
-  launch per step (``prop_mode="plain"``).  Per-lane results follow the
+  kernel launch (``prop_mode="persistent"``, the default), with one kernel
+  launch per step over the lanes not yet finished (``prop_mode="plain"``), or
+  with one launch per step over every lane (``prop_mode="plain_inplace"``:
+  the reference's batch step called in a loop).  Per-lane results follow the
   reference's batch rules; the whole-batch rules that couple lanes are applied
   afterwards: a step limit reached by any lane gives ``step_limit`` to every
   lane, and lanes that finished before the batch's last iteration report
   ``last_h == 0`` and the Taylor coefficients of their final state (the zero
-  steps the reference takes on them).  A non-finite state stops only its own
-  lane (the reference stops the whole batch at that iteration).
+  steps the reference takes on them).  A state that becomes non-finite stops
+  the whole batch at that iteration (``batch_semantics="reference"``) or only
+  its own lane (``"lane"``).
 """
 
 from __future__ import annotations
@@ -44,6 +48,8 @@ import torch
 from . import _lib
 from .core import get_module, lanes_struct, stream_handle
 from .decompose import order_from_tol, taylor_decompose
+
+_PROP_MODES = ("persistent", "plain", "plain_inplace")
 
 EPS = float(np.finfo(np.float64).eps)
 
@@ -246,6 +252,7 @@ class taylor_adaptive_batch:
         autotune=False,
         batch_semantics="reference",
         cold_rows=True,
+        debug=False,
         **kwargs,
     ):
         llvm = {"opt_level": 3, "force_avx512": False, "slp_vectorize": False, "fast_math": False,
@@ -273,8 +280,8 @@ class taylor_adaptive_batch:
                 raise TypeError("the nt_events argument must be a list of nt_event_batch objects")
         self._t_events = _copy.deepcopy(t_events)
         self._nt_events = _copy.deepcopy(nt_events)
-        if prop_mode not in ("persistent", "plain"):
-            raise ValueError("prop_mode must be 'persistent' or 'plain'")
+        if prop_mode not in _PROP_MODES:
+            raise ValueError("prop_mode must be 'persistent', 'plain' or 'plain_inplace'")
         if schedule not in ("lpt", "fifo"):
             raise ValueError("schedule must be 'lpt' or 'fifo'")
         from .var import var_ode_sys
@@ -360,7 +367,8 @@ class taylor_adaptive_batch:
             self._autotune = r
         self._mod_opts = dict(block_lanes=int(block_lanes), pin_arith=bool(pin_arith), team_size=int(team_size),
                               persist_ctas=int(persist_ctas), high_accuracy=self._high_accuracy,
-                              global_jets=bool(global_jets), float32=f32, cold_rows=bool(cold_rows))
+                              global_jets=bool(global_jets), float32=f32, cold_rows=bool(cold_rows),
+                              debug=bool(debug))
         self._mod = get_module(self._dec, self._order, self._dev, **self._mod_opts)
         # propagate_grid's own measured choice, when the autotuner found a
         # different one (its modules share the bookkeeping layout)
@@ -558,8 +566,8 @@ class taylor_adaptive_batch:
 
     @prop_mode.setter
     def prop_mode(self, v):
-        if v not in ("persistent", "plain"):
-            raise ValueError("prop_mode must be 'persistent' or 'plain'")
+        if v not in _PROP_MODES:
+            raise ValueError("prop_mode must be 'persistent', 'plain' or 'plain_inplace'")
         self._prop_mode = v
 
     @property
@@ -1049,8 +1057,10 @@ class taylor_adaptive_batch:
             if ev is not None:
                 ev[0].record(torch.cuda.current_stream(self._dev))
             ws, ws_bytes = mod.ws, mod.ws_bytes
-            if mode == _lib.HYK_MODE_PLAIN:
+            if mode == _lib.HYK_MODE_PLAIN and self._prop_mode == "plain":
                 # counters plus the list of unfinished lanes the plain form steps
+                # (with the counters alone, "plain_inplace", every launch covers
+                # every lane)
                 ws_bytes = int(L.hyk_propagate_workspace_size(mod.handle, B, mode))
                 ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self._tdev)
             while True:
@@ -1314,6 +1324,26 @@ class taylor_adaptive_batch:
                 new.__dict__[k] = _copy.deepcopy(v, memo)
             else:
                 new.__dict__[k] = v
+        return new
+
+    def debug_record(self, clear=False):
+        """With ``debug=True`` (a debug build of the kernels: lane indices
+        checked, non-finite Taylor coefficients recorded, nothing trapped):
+        ``{"codes": [...], "count": n, "first": {...}}`` of the findings since
+        the last clear, the first with its lane, variable, order and
+        iteration."""
+        if not self._mod_opts.get("debug"):
+            raise ValueError("debug_record() needs an integrator constructed with debug=True")
+        return self._mod.debug_record(clear)
+
+    def _replica(self, device):
+        """A copy of the integrator on another GPU, with that GPU's module (the
+        multi-GPU ensemble's per-device template)."""
+        d = self.__getstate__()
+        d.pop("_scalar", None)
+        d["_dev"] = _dev_index(device)
+        new = object.__new__(type(self))
+        new.__setstate__(d)
         return new
 
     def __getstate__(self):

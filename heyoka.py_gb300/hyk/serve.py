@@ -43,7 +43,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .core import get_module, lanes_struct
+from .core import Module, lanes_struct
 from .decompose import order_from_tol, taylor_decompose
 
 _DONE = _lib.LANE_DONE | _lib.LANE_STOPPED
@@ -118,7 +118,10 @@ class LanePool:
         self.dec = taylor_decompose(sys)
         self.order = order_from_tol(tol)
         self.dev = torch.device(device)
-        self.mod = get_module(self.dec, self.order, self.dev.index)
+        # a module of the pool's own (not the integrators' shared one): its
+        # launches run on the pool's streams, and a module's launches must be
+        # ordered (its cold-row buffer holds per-launch data)
+        self.mod = Module(self.dec, self.order, self.dev.index)
         info = self.mod.info_dict()
         self.resident = max(1, info["n_sm"] * info["ctas_per_sm"] * (info["block_lanes"] // info["team_size"]))
         self.C = int(capacity)
@@ -442,7 +445,10 @@ class ResidentPool:
         self.dec = taylor_decompose(sys)
         self.order = order_from_tol(tol)
         self.dev = torch.device(device)
-        self.mod = get_module(self.dec, self.order, self.dev.index)
+        # a module of the pool's own (not the integrators' shared one): its
+        # launches run on the pool's streams, and a module's launches must be
+        # ordered (its cold-row buffer holds per-launch data)
+        self.mod = Module(self.dec, self.order, self.dev.index)
         info = self.mod.info_dict()
         if info["team_size"] != 1:
             raise _lib.HykError("the resident serving pool needs a lane-form module")

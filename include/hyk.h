@@ -136,6 +136,11 @@ typedef struct hyk_config {
                                     keep orders 1..p in a module-owned global buffer when that lets more
                                     lanes share an SM (the module's calls must then be ordered on one
                                     stream, as with HYK_CFG_GLOBAL_JETS) */
+#define HYK_CFG_DEBUG 64u        /* debug build of the module's kernels (slower): lane indices taken from a
+                                    lane list or a serving ring are checked against n_lanes, and a Taylor
+                                    coefficient of a state variable that is not finite is recorded with
+                                    its lane, variable, order and iteration; nothing traps, every finding
+                                    goes to the module's debug record (hyk_module_debug) */
 
 typedef struct hyk_module_info {
     uint32_t n_eq, n_pars, order, n_u;
@@ -162,6 +167,21 @@ int hyk_module_create(const hyk_decomp_t *d, uint32_t order, const hyk_config_t 
                       hyk_module **out);
 int hyk_module_destroy(hyk_module *m);
 int hyk_module_get_info(const hyk_module *m, hyk_module_info_t *info);
+/* Debug record of a module created with HYK_CFG_DEBUG (HYK_ERR_INVALID for
+ * any other module).  out[0]: the OR of every HYK_DBG_* code seen since the
+ * last clear; out[1]: how many findings; out[2]: the code of the first
+ * finding and out[3..6] its details:
+ *   HYK_DBG_LANE_RANGE: the lane index, n_lanes, the list position, 0;
+ *   HYK_DBG_NONFINITE_JET: lane, state variable, order, iteration;
+ *   HYK_DBG_CAPACITY: lane, iteration, 0, 0.
+ * Reads device memory synchronously: the caller synchronises the streams
+ * the module's launches ran on first.  `clear` non-zero zeroes the record
+ * afterwards. */
+#define HYK_DBG_LANE_RANGE 1u    /* a lane list or ring entry >= n_lanes (skipped) */
+#define HYK_DBG_NONFINITE_JET 2u /* a state variable's Taylor coefficient was not finite */
+#define HYK_DBG_CAPACITY 4u      /* a lane stopped on tc/ck/event capacity */
+int hyk_module_debug(hyk_module *m, uint64_t out[8], int clear);
+
 /* The generated CUDA source of the module (valid until hyk_module_destroy). */
 const char *hyk_module_source(const hyk_module *m);
 

@@ -110,3 +110,19 @@ def test_codegen_rejects_bad_input(libhyk):
     d = hyk_decomp_t(1, 1, 0, 0, ctypes.cast(ops, ctypes.POINTER(hyk_uop_t)), ctypes.cast(rhs, ctypes.POINTER(hyk_arg_t)))
     rc = libhyk.hyk_codegen_check(ctypes.byref(d), 10, None, 0, None, 0, None, None)
     assert rc == -1 and b"invalid" in libhyk.hyk_last_error()
+
+
+@pytest.mark.parametrize("team", [0, 4])
+def test_debug_build_compiles_for_sm103a(libhyk, team):
+    """HYK_CFG_DEBUG: the generated source carries the debug hooks (lane
+    index checks, the non-finite coefficient record) and compiles with NVRTC
+    for sm_103a, in the lane and the team form."""
+    from hyk import _lib, workloads as W
+    from hyk.decompose import taylor_decompose
+
+    d, keep = taylor_decompose(W.kepler_sys()).as_c()
+    cfg = _lib.hyk_config_t(128 if team == 0 else 32, 0, _lib.HYK_CFG_DEBUG, team)
+    buf = ctypes.create_string_buffer(1 << 16)
+    rc = libhyk.hyk_codegen_check(ctypes.byref(d), 19, ctypes.byref(cfg), 0, buf, len(buf), None, None)
+    assert rc == 0, libhyk.hyk_last_error().decode()
+    assert libhyk.hyk_module_debug(None, None, 0) == _lib.HYK_ERR_INVALID

@@ -167,3 +167,32 @@ def test_ensemble_with_events_matches_serial():
         for lane in range(3):
             ts = [t for b, t, _ in ti.nt_events[0].callback.hits if b == lane]
             assert ts == sorted(ts)
+
+
+@pytest.mark.parametrize("devices", [[0], [0, 0], [0, 0, 0]])
+@pytest.mark.parametrize("tp", ["until", "grid"])
+def test_devices_equal_single_device(setup, devices, tp):
+    """ensemble_propagate_* with devices= (iteration ranges per GPU, one host
+    thread per GPU, results in iteration order): on one GPU named several
+    times, bit-identical to the single-device ensemble."""
+    ta, ics = setup
+
+    def gen(t, idx):
+        t.set_time(0.0)
+        t.state[:] = ics[idx]
+        return t
+
+    if tp == "until":
+        a = hyk.ensemble_propagate_until_batch(ta, 15.0, 10, gen)
+        b = hyk.ensemble_propagate_until_batch(ta, 15.0, 10, gen, devices=devices)
+    else:
+        grid = np.linspace(0.0, 15.0, 7)
+        a = hyk.ensemble_propagate_grid_batch(ta, grid, 10, gen)
+        b = hyk.ensemble_propagate_grid_batch(ta, grid, 10, gen, devices=devices)
+        for x, y in zip(a, b):
+            assert np.array_equal(x[2], y[2])
+    assert len(b) == 10
+    for i, (x, y) in enumerate(zip(a, b)):
+        assert np.array_equal(np.asarray(x[0].state), np.asarray(y[0].state)), i
+        assert np.all(y[0].time == 15.0)
+        assert x[0].propagate_res == y[0].propagate_res

@@ -67,6 +67,11 @@ def test_dmath_bitwise_gpu_vs_cpu(libhyk, oracle):
         (9, rng.uniform(-1e3, 1e3, 4096), None),
         (10, np.exp(rng.uniform(-10, 10, 4096)), rng.choice([-1.5, -0.5, 2.0, 3.0, -2.0, 0.3, 1.7], 4096)),
         (11, np.exp(rng.uniform(-30, 5, 4096)), np.exp(rng.uniform(-30, 5, 4096))),
+        # large arguments: the exact (Payne-Hanek) reduction of sin and cos
+        (2, np.ldexp(rng.uniform(-2.0, 2.0, 4096), rng.integers(29, 1024, 4096)), None),
+        (3, np.ldexp(rng.uniform(-2.0, 2.0, 4096), rng.integers(29, 1024, 4096)), None),
+        (8, np.ldexp(rng.uniform(-2.0, 2.0, 4096), rng.integers(15, 128, 4096)).astype(np.float32).astype(np.float64),
+         None),
     ]
     pd = ctypes.POINTER(ctypes.c_double)
     for fn, x, a in cases:
@@ -146,7 +151,7 @@ CASES = {
 }
 
 
-@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("mode", ["persistent", "plain", "plain_inplace"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_propagate_until_bitwise(oracle, name, mode):
     sys_, st, pars, tol, tf = CASES[name]()

@@ -310,3 +310,50 @@ def test_single_precision_functions_accuracy(oracle):
     assert ulps(o, x**a) <= 3
     m, q, o = ev(11, np.exp(rng.uniform(-30, 5, 2000)), np.exp(rng.uniform(-30, 5, 2000)))
     assert ulps(o, np.minimum((1 / m) ** (1 / 9), (1 / q) ** (1 / 8))) <= 4  # the step-size factor
+
+
+def test_sincos_large_arguments_exact_reduction(oracle):
+    """sin and cos beyond |x| = 2^30 (the reduction of Payne and Hanek in
+    hyk_dmath.h): within 2 ulp of 2000-bit references over the whole double
+    range, including arguments next to multiples of pi/2 (the double closest
+    to one, 6381956970095103 2^797, among them), in double and in single
+    precision."""
+    import ctypes
+
+    mpmath = pytest.importorskip("mpmath")
+    L = oracle.lib()
+    pd = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(11)
+    xs = list(np.ldexp(rng.uniform(1.0, 2.0, 600), rng.integers(30, 1024, 600)))
+    xs += [2.0**30, -(2.0**30), np.nextafter(2.0**30, 0.0), 1e22, 1e300, -1.7e308, np.ldexp(6381956970095103.0, 797)]
+    mpmath.mp.prec = 2000
+    for e in rng.integers(30, 1000, 100):  # doubles next to k pi/2
+        k = mpmath.floor(mpmath.ldexp(mpmath.mpf(rng.uniform(1.0, 2.0)), int(e)) / (mpmath.pi / 2))
+        xs.append(float(k * mpmath.pi / 2))
+    x = np.array(xs)
+    x = np.concatenate([x, -x])
+    out = {}
+    for fn in (2, 3):
+        o = np.zeros_like(x)
+        L.hyko_dm_eval(fn, x.ctypes.data_as(pd), np.zeros_like(x).ctypes.data_as(pd), o.ctypes.data_as(pd),
+                       ctypes.c_uint64(len(x)))
+        out[fn] = o
+    worst = 0.0
+    for i, xi in enumerate(x):
+        xm = mpmath.mpf(float(xi))
+        for fn, f in ((2, mpmath.sin), (3, mpmath.cos)):
+            ref = f(xm)
+            got = out[fn][i]
+            sp = np.spacing(abs(float(ref))) if ref != 0 else np.spacing(0.0)
+            err = float(abs(mpmath.mpf(float(got)) - ref)) / sp
+            worst = max(worst, err)
+            assert err <= 2.0, (fn, float(xi), got, float(ref), err)
+    # single precision: the float functions go through the exact reduction from |x| = 2^16
+    xf = np.ldexp(rng.uniform(1.0, 2.0, 400), rng.integers(16, 128, 400)).astype(np.float32).astype(np.float64)
+    for fn, f in ((8, mpmath.sin), (9, mpmath.cos)):
+        o = np.zeros_like(xf)
+        L.hyko_dm_eval(fn, xf.ctypes.data_as(pd), np.zeros_like(xf).ctypes.data_as(pd), o.ctypes.data_as(pd),
+                       ctypes.c_uint64(len(xf)))
+        for xi, got in zip(xf, o):
+            ref = float(f(mpmath.mpf(float(xi))))
+            assert abs(got - ref) <= 1.01 * np.spacing(np.float32(abs(ref))), (fn, xi, got, ref)
