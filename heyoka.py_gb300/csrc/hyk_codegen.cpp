@@ -291,9 +291,15 @@ struct Gen {
     std::vector<char> hread;
     uint32_t ncold = 0;
 
-    Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false, bool cold_rows = false)
+    // split: one __noinline__ function per order.  Forced for large systems
+    // (ptxas time), for the adjoint module and for coefficients in global
+    // memory: there a single function of all orders spills (the compiler
+    // keeps values of many operations live across the order's long FMA
+    // chains), and the per-order functions do not.
+    Gen(const Dec &dd, uint32_t order, bool pin_arith, bool adjoint = false, bool cold_rows = false,
+        bool force_split = false)
         : d(dd), p(order), N(dd.n_eq), NU(dd.n_u()), pin(pin_arith), adj(adjoint),
-          split((uint64_t)dd.n_ops * order > 3000), evx(!dd.ev.empty()) {
+          split((uint64_t)dd.n_ops * order > 3000 || adjoint || force_split), evx(!dd.ev.empty()) {
         coldrows = cold_rows && !adjoint && !evx;
         base.resize(NU);
         negf.assign(NU, 0);
@@ -850,14 +856,15 @@ struct Gen {
         std::string coldg = coldrows ? "    hyk_real *__restrict__ hyk_cold_g = hyk_cold_ptr();\n" : "";
         if (fmaops()) coldg += "    HYK_FMAOPS_CONSTS\n";
         if (!split) {
-            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n" << coldg;
+            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0, "
+                 "const unsigned hyk_wm = 0xffffffffu) {\n" << coldg;
             for (uint32_t i = 0; i < N; ++i) o << "    const hyk_real " << vname(i, 0) << " = HYK_SX(" << i << ", 0);\n";
         }
         const uint32_t last = evx ? p : p - 1;  // order p: the event functions' cone only
         for (uint32_t n = 0; n <= last; ++n) {
             if (split) {
                 o << "static __device__ __noinline__ void hyk_jets_o" << n
-                  << "(hyk_real *__restrict__ S, const hyk_real t0) {\n" << coldg;
+                  << "(hyk_real *__restrict__ S, const hyk_real t0, const unsigned hyk_wm) {\n" << coldg;
                 for (uint32_t i = 0; i < N; ++i) {
                     o << "    const hyk_real " << vname(i, n) << " = " << sx(i, n) << ";\n";
                     // The same product the previous order formed (k_i_0 is never read).
@@ -898,14 +905,17 @@ struct Gen {
             }
             // Values of earlier orders are re-read from shared memory: the
             // warp barrier keeps the compiler from carrying them in registers.
-            // It joins the threads that run the recurrences together (the
-            // serving kernel's idle threads wait elsewhere).
+            // It also reconverges the warp's threads at every order (they run
+            // different lanes and may have diverged since the last step):
+            // hyk_wm names the whole warp, except in the serving kernel, whose
+            // idle threads wait elsewhere (hyk_wm 0: the active threads).
             o << "    HYK_WARP_SYNC();\n";
             if (split) o << "}\n";
         }
         if (split) {
-            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0) {\n";
-            for (uint32_t n = 0; n <= last; ++n) o << "    hyk_jets_o" << n << "(S, t0);\n";
+            o << "static __device__ __noinline__ void hyk_jets(hyk_real *__restrict__ S, const hyk_real t0, "
+                 "const unsigned hyk_wm = 0xffffffffu) {\n";
+            for (uint32_t n = 0; n <= last; ++n) o << "    hyk_jets_o" << n << "(S, t0, hyk_wm);\n";
         }
         o << "}\n";
     }
@@ -1877,8 +1887,9 @@ const char *kEvents =
 
 }  // namespace
 
-uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin, bool cold_rows, uint32_t *n_cold) {
-    Gen g(d, order, pin, adjoint, cold_rows);
+uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint, bool pin, bool cold_rows, uint32_t *n_cold,
+                     bool split) {
+    Gen g(d, order, pin, adjoint, cold_rows, split);
     if (n_cold) *n_cold = g.ncold;
     return g.nslot;
 }
@@ -1889,7 +1900,8 @@ struct PrecisionScope {
 };
 
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
-              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc, bool f32, uint64_t cold_stride) {
+              std::string &err, bool adjoint, uint64_t gmem_stride, bool high_acc, bool f32, uint64_t cold_stride,
+              bool split) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -1899,7 +1911,7 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
         return false;
     }
     PrecisionScope prec(f32);
-    Gen g(d, order, pin_arith, adjoint, cold_stride != 0 && gmem_stride == 0);
+    Gen g(d, order, pin_arith, adjoint, cold_stride != 0 && gmem_stride == 0, split);
     const double p = (double)order;
     const double rhofac = rhofac_of(order);
     std::ostringstream h;

@@ -33,8 +33,11 @@ struct GenOut {
 // block size does not change it).
 // cold_rows: the layout with cold state rows (their orders 1..p in a global
 // buffer, only order 0 in shared memory); *n_cold receives their number.
+// split: the recurrences as one function per order (the global-memory lane
+// form; implied for the adjoint and for large systems), which keeps the
+// reciprocals of order-0 denominators in slots of their own.
 uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pin = false, bool cold_rows = false,
-                     uint32_t *n_cold = nullptr);
+                     uint32_t *n_cold = nullptr, bool split = false);
 
 // adjoint: also emit the reverse sweep hyk_jets_bw() and the adjoint kernel
 // (and keep every history up to order p-1 for it).
@@ -44,7 +47,7 @@ uint32_t count_slots(const Dec &d, uint32_t order, bool adjoint = false, bool pi
 // stride (the number of threads of the fixed grid).
 bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t kparams_size, GenOut &out,
               std::string &err, bool adjoint = false, uint64_t gmem_stride = 0, bool high_acc = false,
-              bool f32 = false, uint64_t cold_stride = 0);
+              bool f32 = false, uint64_t cold_stride = 0, bool split = false);
 
 // Team form (several threads per trajectory): slot count and the share of
 // busy threads over the rounds of one order for teams of 1, 2, 4, ..., 32.

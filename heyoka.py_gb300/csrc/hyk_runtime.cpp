@@ -384,6 +384,10 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         // with global-memory regions four warps per CTA
         if (m->gmem && blk == 0) blk = 128;
     } else if (m->gmem) {
+        // The recurrences as one function per order (no spills), with their
+        // own slots for the order-0 reciprocals.
+        nslot = hyk::count_slots(m->d, order, adjoint, pin, false, nullptr, true);
+        lane_bytes = (size_t)nslot * real_bytes;
         // Two CTAs of 128 threads per SM by default: at most 255 registers a
         // thread, so both fit the register file, and eight warps hide the
         // latency of the global-memory coefficients better than four.
@@ -474,7 +478,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32, m->gmem))
             return fail(HYK_ERR_INVALID, err);
     } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
-                              high_acc, f32, m->ncold ? m->cold_threads : 0)) {
+                              high_acc, f32, m->ncold ? m->cold_threads : 0, m->gmem)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (g.n_slot != nslot || g.n_cold != m->ncold) return fail(HYK_ERR_INVALID, "internal: slot count mismatch");
@@ -1099,7 +1103,10 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         return 0;
     }
     const uint32_t slots = hyk::count_slots(d, order, adjoint, pin);
-    const uint64_t gstride = (uint64_t)slots * (f32 ? 4 : 8) * 32 > 227u * 1024 ? 152ull * blk : 0;
+    // The global-memory layout when 32 lanes do not fit shared memory or on
+    // request (HYK_CFG_GLOBAL_JETS), with the slot stride of two CTAs per SM.
+    const bool want_g = (uint64_t)slots * (f32 ? 4 : 8) * 32 > 227u * 1024 || (cfg && (cfg->flags & HYK_CFG_GLOBAL_JETS));
+    const uint64_t gstride = want_g ? 2ull * 152ull * blk : 0;
     // The cold-state-row layout (as the runtime may pick it), with the rows
     // sized for one CTA per SM of a 152-SM GPU.
     uint32_t ncold = 0;
@@ -1113,7 +1120,8 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : (tg ? 128 : 32), sizeof(KParams),
                                 g, err, high_acc, f32, tg))
             return fail(HYK_ERR_UNSUPPORTED, err);
-    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32, cstride)) {
+    } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32, cstride,
+                              gstride != 0)) {
         return fail(HYK_ERR_INVALID, err);
     }
     if (n_slot) *n_slot = g.n_slot;

@@ -1148,6 +1148,11 @@ class taylor_adaptive_batch:
                 p["status"] = torch.where(clear, p["status"] & keep.to(self._tdev), p["status"])
                 d = desc()
         self._finish_prop(p, group, last_tc)
+        # Each lane's steps per unit of time over this propagation: the next
+        # longest-first queue's estimate of its work (orbits whose step size
+        # varies along the orbit are poorly predicted by one step size).
+        span = ((self._thi.double() - t0h.double()) + (self._tlo.double() - t0l.double())).abs()
+        self._step_rate = torch.where(span > 0, p["n_steps"].double() / span, torch.zeros_like(span))
         res = {"grid_out": grid_out}
         if c_output:
             nrec = p["n_iter"]
@@ -1161,8 +1166,11 @@ class taylor_adaptive_batch:
 
     def _lpt_order(self, tf_hi, tf_lo):
         """Longest-first queue order for the persistent kernel: lanes sorted by
-        the estimated number of steps |t_final - t| / h, h the size of a step
-        from the current state (one extra step evaluation, not applied)."""
+        the estimated number of steps, the lane's measured steps per unit of
+        time over its previous propagation times |t_final - t|, or, for a lane
+        without one, |t_final - t| / h, h the size of a step from the current
+        state (one extra step evaluation, not applied).  The order changes
+        only the schedule, never a lane's arithmetic."""
         L = _lib.load()
         B = self._B
         st, th, tl = self._state.clone(), self._thi.clone(), self._tlo.clone()
@@ -1178,6 +1186,10 @@ class taylor_adaptive_batch:
         if tf_lo is not None:
             rem = (rem + tf_lo.double().abs())
         est = torch.nan_to_num(rem / h.double().abs(), nan=0.0, posinf=1e300)
+        rate = self.__dict__.get("_step_rate")
+        if rate is not None and rate.numel() == B and rate.device == est.device:
+            # lanes with a previous propagation: its measured step rate
+            est = torch.where(rate > 0, rate * rem, est)
         return torch.argsort(est, descending=True).contiguous()
 
     def _finish_prop(self, p, group, last_tc):
