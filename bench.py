@@ -14,9 +14,10 @@ API with the state copied from pinned host memory before, and the state and
 step counts copied back after, every step.  paths.plain: the one-launch-per-
 step form over the unfinished lanes (listed before each launch);
 paths.plain_inplace: one launch per step over every lane (the naive drop-in
-form).  roofline: algorithmic FP64 flops of the
-propagation kernel / its CUDA-event duration, against the FP64 FMA peak
-measured in the same process.  cpu_baseline: the compiled CPU stepper that
+form).  roofline: algorithmic FP64 flops of the propagation kernel (the
+measurement contract's count, contract_flops; the code generator's smaller
+count beside it as flops_per_traj_step_generated / frac_generated) / its
+CUDA-event duration, against the FP64 FMA peak measured in the same process.  cpu_baseline: the compiled CPU stepper that
 stands in for the reference's compiled batch stepper (generated recurrences in
 the reference's arithmetic, g++ -O3, vector batches of lanes, OpenMP over all
 host cores; oracle/cpu_batch.py) on a bounded sample of the same orbits.
@@ -66,8 +67,9 @@ def parse():
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--slice", type=int, default=1024, help="serve: the most steps per lane in one slice")
     ap.add_argument("--quantum-ms", type=float, default=2.0, help="serve: target duration of a slice")
-    ap.add_argument("--serve-mode", default="resident", choices=["resident", "slice"],
-                    help="serve: resident kernels fed from a device ring, or time slices relaunched by the host")
+    ap.add_argument("--serve-mode", default="slice", choices=["resident", "slice"],
+                    help="serve: time slices relaunched by the host (default), or resident kernels fed from a "
+                         "device ring")
     ap.add_argument("--members", type=int, default=65536, help="oss, cr3bp-adjoint: trajectories")
     ap.add_argument("--autotune", action="store_true",
                     help="oss: pick the kernel configuration by measurement (hyk.autotune, cached per system)")
@@ -97,20 +99,35 @@ def _ensemble_ics(seed):
     return _ICS[seed]
 
 
-def flops_per_step(sys_, order):
-    """Algorithmic FP64 flops of one trajectory-step (the code generator's count; no GPU needed)."""
-    import ctypes
+def contract_flops(sys_, order):
+    """Algorithmic FP64 flops of one trajectory-step under the measurement
+    contract of the hot-path plan: F = sum over the decomposition's operations
+    of sum_{n=0}^{p} cost(n) + N p (state coefficients) + 2 N p (Horner) +
+    2 N + 30 (step size), with per-order costs add/sub/neg and products or
+    quotients by a number or parameter 1, mul 2n+1, square n+2, div 2n+2,
+    sqrt n+3, pow 4n+3, exp 2n+1, log 2n+3, a sin/cos pair 4n+2 (a lone sin or
+    cos counted as the pair) plus p once for its j a_j."""
+    from hyk import decompose as D
 
-    from hyk import _lib
-    from hyk.decompose import taylor_decompose
-
-    L = _lib.load()
-    d, keep = taylor_decompose(sys_).as_c()
-    buf = ctypes.create_string_buffer(1 << 24)
-    fl = ctypes.c_double()
-    _lib.check(L.hyk_codegen_check(ctypes.byref(d), int(order), None, 2, buf, len(buf), None, ctypes.byref(fl)))
-    del keep
-    return fl.value
+    dec = D.taylor_decompose(sys_)
+    p, N = int(order), dec.n_eq
+    cost = {D.OP_MUL: lambda n: 2 * n + 1, D.OP_SQUARE: lambda n: n + 2, D.OP_DIV: lambda n: 2 * n + 2,
+            D.OP_SQRT: lambda n: n + 3, D.OP_POW: lambda n: 4 * n + 3, D.OP_EXP: lambda n: 2 * n + 1,
+            D.OP_LOG: lambda n: 2 * n + 3}
+    F = 0
+    trig = set()
+    for op, aux, a, b in dec.ops:
+        consts = (D.ARG_NUM, D.ARG_PAR)
+        if op in (D.OP_ADD, D.OP_SUB, D.OP_NEG) or (op in (D.OP_MUL, D.OP_DIV) and (a[0] in consts or b[0] in consts)):
+            F += p + 1
+        elif op in (D.OP_SIN, D.OP_COS):
+            if a in trig:  # the other half of a pair already counted
+                continue
+            trig.add(a)
+            F += sum(4 * n + 2 for n in range(p + 1)) + p
+        else:
+            F += sum(cost[op](n) for n in range(p + 1))
+    return F + N * p + 2 * N * p + 2 * N + 30
 
 
 _CPU = {}
@@ -149,7 +166,7 @@ def cpu_baseline(n_orbits, seed, t_end, steps=1):
     sample = np.ascontiguousarray(st[:, np.sort(idx)])
     sys_ = W.kepler_sys()
     setup = cpu_stepper_setup(sys_, 19, sample[:, :512], t_end)
-    fl = flops_per_step(sys_, 19)
+    fl = contract_flops(sys_, 19)
     best = None
     tot_steps = 0
     threads = 0
@@ -573,7 +590,8 @@ def run_oss(args):
     r = cpu_batch.ensemble_until(W.oss_sys(), np.ascontiguousarray(st[:, pick]), None, 0.0, t_end[pick], order=ta.order,
                                  batch=csetup["batch"])
     cwall = time.perf_counter() - c0
-    fl = info["flops_per_step"] * steps / t_k
+    F = contract_flops(W.oss_sys(), ta.order)
+    fl = F * steps / t_k
     peak = hyk.fp64_peak(0, 300.0)
     h2d = st.nbytes + grid.nbytes
     line = {
@@ -595,14 +613,17 @@ def run_oss(args):
         "e2e": {"value": steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(out_np.nbytes)},
         "roofline": {"bound": "fp64", "achieved": fl / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-                     "frac": fl / peak, "traffic": None,
-                     "note": "flops_per_step x trajectory-steps / propagation-kernel time; peak = in-process FP64 FMA probe"},
+                     "frac": fl / peak, "traffic": None, "flops_per_traj_step": F,
+                     "flops_per_traj_step_generated": info["flops_per_step"],
+                     "frac_generated": info["flops_per_step"] * steps / t_k / peak,
+                     "note": "contract flops per step x trajectory-steps / propagation-kernel time; peak = in-process "
+                             "FP64 FMA probe, of measured (MEASURED_PEAKS.json has no FP64 entry)"},
         "cpu_baseline": {"value": float(r["n_steps"].sum()) / cwall, "unit": UNIT, "cores": r["threads"], "kind": "port",
                          "sample": "4096 of the 65536 members (evenly spaced), propagate_until each member's end time, "
                                    "compiled CPU stepper (reference arithmetic, batches of {} lanes, oracle/cpu_batch.py)"
                                    .format(csetup["batch"]),
-                         "gflops": float(r["n_steps"].sum()) / cwall * info["flops_per_step"] / 1e9,
-                         "frac_of_host_peak": float(r["n_steps"].sum()) / cwall * info["flops_per_step"] / csetup["peak"]},
+                         "gflops": float(r["n_steps"].sum()) / cwall * F / 1e9,
+                         "frac_of_host_peak": float(r["n_steps"].sum()) / cwall * F / csetup["peak"]},
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -684,7 +705,8 @@ def run_kepler_f32(args):
     err = float(np.max(np.abs(np.asarray(ta.state)[:, pick].astype(np.float64) - np.asarray(tdd.state))))
     del tdd
     peak = hyk.fp32_peak(0, 300.0)
-    fl = info["flops_per_step"] * n_steps / t_k
+    F = contract_flops(W.kepler_sys(), ta.order)
+    fl = F * n_steps / t_k
     cpu = None
     if not args.no_cpu:
         idx = np.random.default_rng(123).choice(n, args.cpu_sample, replace=False)
@@ -711,7 +733,8 @@ def run_kepler_f32(args):
         "gpu_launches": 3 * K,
         "roofline": {"bound": "fp32", "achieved": fl / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": fl / peak, "traffic": None, "kernel": "hyk_prop_kernel (persistent, float)",
-                     "flops_per_traj_step": info["flops_per_step"],
+                     "flops_per_traj_step": F, "flops_per_traj_step_generated": info["flops_per_step"],
+                     "frac_generated": info["flops_per_step"] * n_steps / t_k / peak,
                      "peak_source": "measured in-process FP32 FMA probe (hyk_fp32_peak), of measured"},
         "cpu_baseline": cpu, "clocks": clocks,
         "checks": {"all_time_limit": ok, "final_time_exact": final_t_ok,
@@ -869,7 +892,10 @@ def main():
     st = W.kepler_ics(n, seed=1 + rank)
     ta = hyk.taylor_adaptive_batch(W.kepler_sys(), st, tol=TOL, device="cuda:{}".format(dev), team_size=args.team_size)
     info = ta.module_info
-    flops_step = info["flops_per_step"]
+    # algorithmic flops per trajectory-step: the measurement contract's count
+    # (contract_flops), and the code generator's own, more conservative count
+    flops_step = contract_flops(W.kepler_sys(), 19)
+    flops_gen = info["flops_per_step"]
     peak = hyk.fp64_peak(dev, 300.0)
 
     # warm-up on a copy (same kernel, same data)
@@ -1037,7 +1063,10 @@ def main():
                 "traffic_source": "ncu capture of a 2^17-orbit launch, scaled by lanes",
                 "kernel": "hyk_prop_kernel (persistent)",
                 "flops_per_traj_step": flops_step,
-                "peak_source": "measured in-process FP64 FMA probe (hyk_fp64_peak), of measured",
+                "flops_per_traj_step_generated": flops_gen,
+                "frac_generated": flops_gen * n_steps / (sum(kern_ms) / 1e3) / peak,
+                "peak_source": "measured in-process FP64 FMA probe (hyk_fp64_peak), of measured; "
+                               "MEASURED_PEAKS.json has no FP64 entry",
             },
             "cpu_baseline": cpu,
             "clocks": clocks,

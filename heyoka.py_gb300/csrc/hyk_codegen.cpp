@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <sstream>
 
+#include "hyk_fuse.h"
 #include "hyk_internal.hpp"
 
 // hyk_ev_btab (the Bernstein conversion table printed into event kernels)
@@ -291,6 +292,25 @@ struct Gen {
     std::vector<char> hread;
     uint32_t ncold = 0;
 
+    // Sums of squares fused into one recurrence (hyk_fuse.h; GPU arithmetic
+    // only): fz.fuse[k] marks the root ADD, fz.dead the squares and sums it
+    // absorbs (skipped like aliases).
+    HykFusePlan fz;
+    bool fused(uint32_t u) const { return u >= N && !fz.fuse.empty() && fz.fuse[u - N]; }
+    Ref uref(int32_t v) const {
+        hyk_arg_t a{};
+        a.kind = HYK_ARG_U;
+        a.idx = v;
+        return res(a);
+    }
+    // The fused root's addend (kind HYK_ARG_NONE when it has none) and leaves.
+    Ref fz_a(uint32_t u) const { return fz.addend[u - N] >= 0 ? uref(fz.addend[u - N]) : Ref{}; }
+    std::vector<Ref> fz_x(uint32_t u) const {
+        std::vector<Ref> v;
+        for (int32_t x : fz.leaves[u - N]) v.push_back(uref(x));
+        return v;
+    }
+
     // split: one __noinline__ function per order.  Forced for large systems
     // (ptxas time), for the adjoint module and for coefficients in global
     // memory: there a single function of all orders spills (the compiler
@@ -321,6 +341,11 @@ struct Gen {
                 };
                 cst[u] = kconst(op.a) && kconst(op.b);
             }
+        }
+        if (!pin) {
+            fz = hyk_fuse_plan(N, d.n_ops, d.ops.data(), d.rhs.data(), (uint32_t)d.ev.size(), d.ev.data());
+            for (uint32_t k = 0; k < d.n_ops; ++k)
+                if (fz.dead[k]) alias[N + k] = 1;  // computed nowhere
         }
         analyse();
     }
@@ -356,6 +381,10 @@ struct Gen {
             auto K = [&](const Ref &r) {
                 if (r.kind == HYK_ARG_U && !cst[r.u]) needka[r.u] = 1;
             };
+            if (fused(u)) {
+                for (const Ref &x : fz_x(u)) H(x);
+                continue;
+            }
             switch (op.op) {
             case HYK_OP_MUL:
                 if (varying(B)) H(A);
@@ -489,7 +518,8 @@ struct Gen {
             for (uint32_t k = 0; k < d.n_ops; ++k) {
                 const uint32_t u = N + k;
                 const int o = d.ops[k].op;
-                if (alias[u] || o == HYK_OP_ADD || o == HYK_OP_SUB || o == HYK_OP_NEG || p < 2) continue;
+                if (alias[u] || p < 2 || ((o == HYK_OP_ADD || o == HYK_OP_SUB || o == HYK_OP_NEG) && !fused(u)))
+                    continue;
                 aslot[u] = (int)s;
                 s += p - 1;
             }
@@ -642,6 +672,28 @@ struct Gen {
         const Ref A = res(op.a), B = res(op.b);
         const std::string acc = "a" + std::to_string(u) + "_" + std::to_string(n);
         const std::string z = lit(0.0);
+        if (fused(u)) {
+            // a + sum_i x_i^2 in one chain (hyk_fuse.h)
+            const Ref FA = fz_a(u);
+            const std::vector<Ref> FX = fz_x(u);
+            const bool ha = FA.kind == HYK_ARG_U;
+            Acc s{acc};
+            for (const Ref &x : FX)
+                for (uint32_t j = 0; 2 * j < n; ++j) term(s, cf(x, j, n), cf(x, n - j, n));
+            std::string r = ha ? cf(FA, n, n) : "";
+            if (!s.first) {
+                r = ha ? fma(lit(2.0), acc, r) : add(acc, acc);
+                flops += ha ? 2 : 1;
+            }
+            if (n % 2 == 0)
+                for (const Ref &x : FX) {
+                    const std::string xm = cf(x, n / 2, n);
+                    flops += r.empty() ? 1 : 2;
+                    r = r.empty() ? mul(xm, xm) : fma(xm, xm, r);
+                }
+            def(u, n, r);
+            return;
+        }
         switch (op.op) {
         case HYK_OP_ADD:
         case HYK_OP_SUB: {
@@ -1035,6 +1087,22 @@ struct Gen {
         if (unary_fn && m >= 1 && !varying(A)) return;
         const std::string G = ub(u), H = hfac(u), inv = "i" + std::to_string(u);
         std::vector<std::pair<std::string, std::string>> t;
+        if (fused(u)) {
+            // c_n = a_n + sum_i sum_j x_i,j x_i,n-j: abar_m += cbar_m,
+            // xbar_i,m += 2 sum_{n>=m} cbar_n x_i,n-m
+            const Ref FA = fz_a(u);
+            o << "    const double " << H << " = " << G << ";\n";
+            keep(u, m);
+            if (FA.kind == HYK_ARG_U) contrib(FA, m, H);
+            for (const Ref &x : fz_x(u)) {
+                t.clear();
+                if (wants(x, m))
+                    for (uint32_t n = m; n < p; ++n) t.push_back({hval(u, n, m), val(x, n - m)});
+                const std::string sx = gsum(t);
+                if (!sx.empty()) contrib(x, m, sx, "2.0");
+            }
+            return;
+        }
         switch (op.op) {
         case HYK_OP_ADD:
             if (nz(A, m)) contrib(A, m, G);
@@ -1292,7 +1360,7 @@ struct TeamGen {
     uint32_t nslot = 0, par_slot = 0;
     int max_level = 0;
     struct Desc {
-        int a = 0, b = 0, c = 0, ka = 0, kc = 0, inv = 0, prt = 0;
+        int a = 0, b = 0, c = 0, ka = 0, kc = 0, inv = 0, prt = 0, x3 = 0;
         double num = 0;
     };
     std::vector<Desc> descs;
@@ -1345,6 +1413,14 @@ struct TeamGen {
         nslot = s;
     }
 
+    // The operands as the recurrence reads them: a fused a + x^2 (hyk_fuse.h)
+    // reads a and x (in the descriptor's a and b).
+    std::pair<Ref, Ref> opnds(uint32_t u) const {
+        if (g.fused(u)) return {g.fz_a(u), g.fz_x(u)[0]};
+        const auto &op = d.ops[u - N];
+        return {g.res(op.a), g.res(op.b)};
+    }
+
     // A time-constant operation (Gen::cst) reads like a parameter: its value in
     // its slot at order 0, zero above.
     bool isK(const Ref &r) const {
@@ -1362,6 +1438,7 @@ struct TeamGen {
             return false;
         };
         if (g.cst[u]) return true;  // order 0 only
+        if (g.fused(u)) return true;  // two time-varying u-variables (hyk_fuse.h)
         switch (op.op) {
         case HYK_OP_ADD:
         case HYK_OP_SUB:
@@ -1407,11 +1484,13 @@ struct TeamGen {
             const uint32_t u = N + k;
             if (g.alias[u]) continue;
             if (!supported(u, err)) return false;
-            const auto &op = d.ops[k];
-            const Ref A = g.res(op.a), B = g.res(op.b);
+            const auto AB = opnds(u);
+            const Ref A = AB.first, B = AB.second;
             int lv = 0;  // after every u-variable argument (time-constant ones included: order 0 reads them)
             if (A.kind == HYK_ARG_U) lv = std::max(lv, level[A.u]);
             if (B.kind == HYK_ARG_U) lv = std::max(lv, level[B.u]);
+            if (g.fused(u))
+                for (const Ref &x : g.fz_x(u)) lv = std::max(lv, level[x.u]);
             level[u] = lv + 1;
             max_level = std::max(max_level, lv + 1);
         }
@@ -1421,9 +1500,14 @@ struct TeamGen {
             const uint32_t u = N + k;
             if (g.alias[u]) continue;
             const auto &op = d.ops[k];
-            const Ref A = g.res(op.a), B = g.res(op.b);
+            const auto AB = opnds(u);
+            const Ref A = AB.first, B = AB.second;
             std::string key = "op" + std::to_string(op.op) + "_" + rkey(A) + "_" + rkey(B) + "_c" +
                               (g.cst[u] ? "K" : (g.hist[u] ? "h" : "c")) + (g.needka[u] ? "k" : "");
+            if (g.fused(u)) {  // a sum of squares: its leaves' kinds (the first is B)
+                key += "_F";
+                for (const Ref &x : g.fz_x(u)) key += rkey(x);
+            }
             if (op.op == HYK_OP_POW) {
                 char buf[40];
                 std::snprintf(buf, sizeof buf, "_a%a", op.b.num);
@@ -1500,7 +1584,8 @@ struct TeamGen {
                 gr.off = (uint32_t)descs.size();
                 for (uint32_t u : gr.members) {
                     const auto &op = d.ops[u - N];
-                    const Ref A = g.res(op.a), B = g.res(op.b);
+                    const auto AB = opnds(u);
+                    const Ref A = AB.first, B = AB.second;
                     Desc D;
                     D.a = slot_of(A);
                     D.b = slot_of(B);
@@ -1511,6 +1596,12 @@ struct TeamGen {
                     if (op.op == HYK_OP_SIN || op.op == HYK_OP_COS) D.prt = tslot[op.aux];
                     if (A.kind == HYK_ARG_NUM) D.num = A.num;
                     if (B.kind == HYK_ARG_NUM && op.op != HYK_OP_POW) D.num = B.num;
+                    if (g.fused(u)) {
+                        // a sum of squares: the leaves' slots in b, inv, prt, x3
+                        const std::vector<Ref> X = g.fz_x(u);
+                        int *f[HYK_FUSE_MAX] = {&D.b, &D.inv, &D.prt, &D.x3};
+                        for (size_t i = 0; i < X.size(); ++i) *f[i] = tslot[X[i].u];
+                    }
                     descs.push_back(D);
                 }
                 if (d.ops[gr.members[0] - N].op == HYK_OP_POW) {
@@ -1548,6 +1639,10 @@ struct TeamGen {
                 const auto &op = d.ops[gr.members[0] - N];
                 const Ref A = g.res(op.a), B = g.res(op.b);
                 bool conv = false;
+                if (g.fused(gr.members[0])) {
+                    add(gr, 0.5 * p);
+                    continue;
+                }
                 switch (op.op) {
                 case HYK_OP_MUL: conv = isU(A) && isU(B); break;
                 case HYK_OP_DIV: conv = isU(B); break;
@@ -1609,12 +1704,49 @@ struct TeamGen {
         const uint32_t u = gr.members[0];
         if (!n0 && g.cst[u]) return;  // time-constant: order 0 only
         const auto &op = d.ops[u - N];
-        const Ref A = g.res(op.a), B = g.res(op.b);
+        const auto AB = opnds(u);
+        const Ref A = AB.first, B = AB.second;
         const std::string fma_ = "HYK_FMA";
         o << "        // " << gr.key << "\n";
         o << "#pragma unroll 1\n";
         o << "        for (int q = r; q < " << gr.members.size() << "; q += HYK_TEAM) {\n";
         o << "            const hyk_tdesc &D = hyk_td[" << gr.off << " + q];\n";
+        if (g.fused(u)) {
+            // a + sum_i x_i^2 in one chain (hyk_fuse.h), the lane form's arithmetic;
+            // the leaves' slots are in D.b, D.inv, D.prt, D.x3
+            const std::vector<Ref> X = g.fz_x(u);
+            const char *lf[HYK_FUSE_MAX] = {"D.b", "D.inv", "D.prt", "D.x3"};
+            auto lx = [&](size_t i, const std::string &J) { return "S[" + std::string(lf[i]) + " + " + J + "]"; };
+            const bool ha = A.kind == HYK_ARG_U;
+            if (n0) {
+                std::string r = ha ? cur(A, 'a', true) : "";
+                for (size_t i = 0; i < X.size(); ++i)
+                    r = r.empty() ? "HYK_MUL(" + lx(i, "0") + ", " + lx(i, "0") + ")"
+                                  : fma_ + "(" + lx(i, "0") + ", " + lx(i, "0") + ", " + r + ")";
+                out(u, true, r);
+            } else {
+                for (size_t i = 0; i < X.size(); ++i) {
+                    if (i == 0)
+                        o << "            hyk_real acc = HYK_MUL(" << lx(0, "0") << ", " << lx(0, "n") << ");\n";
+                    else
+                        o << "            acc = " << fma_ << "(" << lx(i, "0") << ", " << lx(i, "n") << ", acc);\n";
+                    o << "#pragma unroll " << ju << "\n";
+                    o << "            for (int j = 1; 2 * j < n; ++j) acc = " << fma_ << "(" << lx(i, "j") << ", "
+                      << lx(i, "n - j") << ", acc);\n";
+                }
+                if (ha)
+                    o << "            acc = " << fma_ << "(" << lit(2.0) << ", acc, " << cur(A, 'a', false) << ");\n";
+                else
+                    o << "            acc = HYK_ADD(acc, acc);\n";
+                o << "            if ((n & 1) == 0) {\n";
+                for (size_t i = 0; i < X.size(); ++i)
+                    o << "                acc = " << fma_ << "(" << lx(i, "n / 2") << ", " << lx(i, "n / 2") << ", acc);\n";
+                o << "            }\n";
+                out(u, false, "acc");
+            }
+            o << "        }\n";
+            return;
+        }
         if (n0) {
             const std::string a = cur(A, 'a', true), b = cur(B, 'b', true);
             switch (op.op) {
@@ -1827,11 +1959,12 @@ struct TeamGen {
     }
 
     void emit() {
-        o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, pad;\n    hyk_real num;\n};\n";
+        // (a fused sum of squares keeps its leaves' slots in b, inv, prt, x3)
+        o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, x3;\n    hyk_real num;\n};\n";
         o << "static __device__ const hyk_tdesc hyk_td[" << std::max<size_t>(descs.size(), 1) << "] = {\n";
         for (const auto &D : descs)
             o << "    {" << D.a << ", " << D.b << ", " << D.c << ", " << D.ka << ", " << D.kc << ", " << D.inv << ", "
-              << D.prt << ", 0, " << lit(D.num) << "},\n";
+              << D.prt << ", " << D.x3 << ", " << lit(D.num) << "},\n";
         if (descs.empty()) o << "    {0, 0, 0, 0, 0, 0, 0, 0, " << lit(0.0) << "},\n";
         o << "};\n";
         o << "static __constant__ hyk_real hyk_invn[" << (p + 2) << "] = {" << lit(0.0);

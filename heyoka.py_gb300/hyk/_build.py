@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["hyk_generic.cu", "hyk_noalloc.cu", "hyk_runtime.cpp", "hyk_codegen.cpp"]
-DEPS = SOURCES + ["kernel_template.inc", "kernel_common.inc", "kernel_team.inc", "hyk_internal.hpp", "hyk_dmath.h",
+DEPS = SOURCES + ["kernel_template.inc", "kernel_common.inc", "kernel_team.inc", "hyk_internal.hpp", "hyk_dmath.h", "hyk_fuse.h",
                   "hyk_events.h"]
 
 

@@ -748,11 +748,17 @@ class Server:
     """Continuous-batching server over a set of ODE systems.
 
     ``systems``: name -> (sys, tol).  ``hbm_budget``: bytes of lane state per
-    system pool (admission by footprint).  ``slice_iters``: the most steps
-    per lane in one slice; ``quantum_ms``: the target duration of a slice."""
+    system pool (admission by footprint).  ``mode``: "slice" (the default:
+    time slices of the persistent kernel over every admitted lane, relaunched
+    by the host, LanePool) or "resident" (one resident kernel per system on
+    an equal share of the SMs, fed from a device ring, ResidentPool: the
+    lower latency while the GPU is lightly loaded, but its threads serve the
+    ring in order, so under load short requests wait behind long ones).
+    ``slice_iters``: the most steps per lane in one slice; ``quantum_ms``:
+    the target duration of a slice."""
 
     def __init__(self, systems, hbm_budget=2 << 30, slice_iters=1024, device="cuda:0", max_lanes=1 << 21,
-                 quantum_ms=2.0, mode="resident"):
+                 quantum_ms=2.0, mode="slice"):
         if mode not in ("resident", "slice"):
             raise ValueError("mode must be 'resident' or 'slice'")
         self.pools = {}

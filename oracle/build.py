@@ -19,12 +19,9 @@ LIB = os.path.join(OUT_DIR, "libhyk_oracle.so")
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "hyk_oracle.cpp")
     hdr = os.path.join(ROOT, "include", "hyk.h")
-    dm = os.path.join(ROOT, "heyoka.py_gb300", "csrc", "hyk_dmath.h")
-    if (
-        not force
-        and os.path.exists(LIB)
-        and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr), os.path.getmtime(dm))
-    ):
+    csrc = os.path.join(ROOT, "heyoka.py_gb300", "csrc")
+    deps = [src, hdr] + [os.path.join(csrc, f) for f in ("hyk_dmath.h", "hyk_events.h", "hyk_fuse.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     cmd = [

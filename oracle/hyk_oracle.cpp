@@ -61,6 +61,7 @@
 #include "hyk.h"
 #include "hyk_dmath.h"   // the deterministic elementary functions of the CUDA kernels
 #include "hyk_events.h"  // the event root finder of the CUDA kernels
+#include "hyk_fuse.h"    // the kernels' fusion of sums with a square (gpu arithmetic)
 
 #include <algorithm>
 #include <cmath>
@@ -307,6 +308,9 @@ template <typename T> struct Batch {
     // parameter or such an operation) have only an order-0 value, their
     // higher orders are known zeros (the kernels' code generator does the same).
     std::vector<char> cst;
+    // gpu arithmetic: a + x^2 computed as one chain where the kernels' code
+    // generator does so (hyk_fuse.h); the absorbed square is not computed.
+    HykFusePlan fz;
 
     // md: bit 0 = gpu arithmetic, bit 1 = high accuracy.
     Batch(const Dec &dd, uint32_t order, uint32_t b, int md)
@@ -355,6 +359,8 @@ template <typename T> struct Batch {
                 };
                 cst[d.n_eq + k] = kc(o.a) && kc(o.b);
             }
+        if (mode == 1)
+            fz = hyk_fuse_plan(d.n_eq, d.n_ops, d.ops.data(), d.rhs.data(), (uint32_t)d.ev.size(), d.ev.data());
         // rho factor exp(-2) * exp(-0.7/(p-1)), written as 1/(e*e) * exp((-7/10)/(p-1)).
         const T e1 = M<T>::exp(T(1));
         rhofac = T(1) / (e1 * e1) * M<T>::exp((T(-7) / T(10)) / T(p - 1));
@@ -438,6 +444,34 @@ template <typename T> struct Batch {
         const int64_t ra = numrow_of[2 * k], rb = numrow_of[2 * k + 1];
         std::vector<T> &acc = s_acc;
         bool first = true;
+        if (!fz.dead.empty() && fz.dead[k]) return;  // absorbed by a fused sum
+        if (!fz.fuse.empty() && fz.fuse[k]) {
+            // c_n = a_n + sum_i (x_i^2)_n (hyk_fuse.h): s = sum_i sum_{j < n/2}
+            // x_i,j x_i,n-j, c = fma(2, s, a_n) (s + s without a), then
+            // fma(x_i,n/2, x_i,n/2, c) for every leaf at even n
+            const bool ha = fz.addend[k] >= 0;
+            const T *a = ha ? jr((uint32_t)fz.addend[k], n) : nullptr;
+            for (int32_t x : fz.leaves[k])
+                for (uint32_t j = 0; 2 * j < n; ++j) term(acc.data(), jr((uint32_t)x, j), jr((uint32_t)x, n - j), first);
+            bool have = true;
+            if (!first) {
+                for (uint32_t l = 0; l < B; ++l) c[l] = ha ? M<T>::fma(T(2), acc[l], a[l]) : acc[l] + acc[l];
+            } else if (ha) {
+                for (uint32_t l = 0; l < B; ++l) c[l] = a[l];
+            } else {
+                have = false;
+            }
+            if (n % 2 == 0)
+                for (int32_t x : fz.leaves[k]) {
+                    const T *xm = jr((uint32_t)x, n / 2);
+                    for (uint32_t l = 0; l < B; ++l) c[l] = have ? M<T>::fma(xm[l], xm[l], c[l]) : xm[l] * xm[l];
+                    have = true;
+                }
+            if (!have)
+                for (uint32_t l = 0; l < B; ++l) c[l] = T(0);
+            set_ka(u, n);
+            return;
+        }
         switch (o.op) {
         case HYK_OP_ADD:
         case HYK_OP_SUB: {
