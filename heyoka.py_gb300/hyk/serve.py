@@ -775,11 +775,30 @@ class Server:
                 except _lib.HykError:
                     pool = None  # a team-form system: time slices
             self.pools[name] = pool or LanePool(name, sys, tol, cap, device, slice_iters, quantum_ms * 1e-3)
+        self._warm = False
+
+    def warm(self):
+        """Serve one zero-duration request per pool through the whole path
+        (admission, a launch, counting, retirement): the first launch of each
+        pool pays one-time costs (seconds for the first slice of a pool on a
+        fresh process: module loading and the first use of its host and device
+        buffers) that would otherwise fall on the first real requests.  Done by
+        the first run() unless called before."""
+        if self._warm:
+            return
+        self._warm = True
+        dummies = []
+        for i, (name, pool) in enumerate(self.pools.items()):
+            st = np.zeros((pool.dec.n_eq, 1))
+            pa = np.zeros((pool.dec.n_pars, 1)) if pool.dec.n_pars else None
+            dummies.append(Request(name, st, 0.0, pars=pa, rid=i))
+        self.run(dummies, realtime=False)
 
     def run(self, requests, realtime=True):
         """Serve `requests` (with arrival times in seconds); returns the results
         in completion order.  With ``realtime`` the arrivals follow the wall
         clock; otherwise each request is available from the start."""
+        self.warm()
         reqs = sorted(requests, key=lambda r: r.arrival)
         for i, r in enumerate(reqs):
             if r.rid < 0:
@@ -787,6 +806,12 @@ class Server:
         top = max((r.rid for r in reqs), default=0) + 1
         for p in self.pools.values():
             p.reserve_requests(top)
+            if isinstance(p, ResidentPool):
+                # the finished-lane counters are per request index: a new run
+                # may reuse the indices of an earlier one (no kernel runs now)
+                torch.cuda.synchronize(p.dev)
+                p.done.zero_()
+                torch.cuda.synchronize(p.dev)
         waiting = {name: [] for name in self.pools}
         results = []
         t_start = _time.perf_counter()
