@@ -878,11 +878,10 @@ static int propagate_impl(hyk_module *m, const hyk_lanes_t *lanes, const hyk_pro
         HYK_CU(drv().cuMemsetD32Async((CUdeviceptr)workspace, 0, 4, s));
         k.persistent = 1;
         k.iters_per_launch = p->slice_iters ? p->slice_iters : ~0ULL;
-        // The resident capacity, or fewer CTAs when the queue holds fewer
-        // lanes: a small propagation leaves the other SMs to concurrent work
-        // (the serving pools' slices of other systems).
-        const uint64_t grid = std::max<uint64_t>(
-            1, std::min<uint64_t>((uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm, lane_blocks(m, k.n_order)));
+        // The resident capacity, whatever the number of lanes: a CTA that
+        // finds the queue empty returns at once, and spreading a small batch
+        // over every SM gives each of its warps an FP64 unit of its own.
+        const uint64_t grid = (uint64_t)m->dv->n_sm * (uint64_t)m->ctas_per_sm;
         rc = launch(m, m->f_prop, grid, m->blk, m->smem, k, stream);
         if (rc) return rc;
         if (iters) *iters = 1;
