@@ -292,11 +292,15 @@ struct Gen {
     std::vector<char> hread;
     uint32_t ncold = 0;
 
-    // Sums of squares fused into one recurrence (hyk_fuse.h; GPU arithmetic
-    // only): fz.fuse[k] marks the root ADD, fz.dead the squares and sums it
-    // absorbs (skipped like aliases).
+    // Sums of squares and sums of scaled terms fused into one recurrence
+    // (hyk_fuse.h; GPU arithmetic only): fz.fuse[k] marks the root, fz.dead
+    // the squares, products, negations and sums it absorbs (skipped like
+    // aliases).
     HykFusePlan fz;
     bool fused(uint32_t u) const { return u >= N && !fz.fuse.empty() && fz.fuse[u - N]; }
+    bool fused_sq(uint32_t u) const { return fused(u) && fz.fuse[u - N] == HYK_FUSE_SQ; }
+    bool fused_sc(uint32_t u) const { return fused(u) && fz.fuse[u - N] == HYK_FUSE_SC; }
+    const std::vector<double> &fz_k(uint32_t u) const { return fz.scales[u - N]; }
     Ref uref(int32_t v) const {
         hyk_arg_t a{};
         a.kind = HYK_ARG_U;
@@ -382,8 +386,9 @@ struct Gen {
                 if (r.kind == HYK_ARG_U && !cst[r.u]) needka[r.u] = 1;
             };
             if (fused(u)) {
-                for (const Ref &x : fz_x(u)) H(x);
-                continue;
+                if (fused_sq(u))
+                    for (const Ref &x : fz_x(u)) H(x);
+                continue;  // a sum of scaled terms reads order n only
             }
             switch (op.op) {
             case HYK_OP_MUL:
@@ -518,7 +523,7 @@ struct Gen {
             for (uint32_t k = 0; k < d.n_ops; ++k) {
                 const uint32_t u = N + k;
                 const int o = d.ops[k].op;
-                if (alias[u] || p < 2 || ((o == HYK_OP_ADD || o == HYK_OP_SUB || o == HYK_OP_NEG) && !fused(u)))
+                if (alias[u] || p < 2 || ((o == HYK_OP_ADD || o == HYK_OP_SUB || o == HYK_OP_NEG) && !fused_sq(u)))
                     continue;
                 aslot[u] = (int)s;
                 s += p - 1;
@@ -672,6 +677,19 @@ struct Gen {
         const Ref A = res(op.a), B = res(op.b);
         const std::string acc = "a" + std::to_string(u) + "_" + std::to_string(n);
         const std::string z = lit(0.0);
+        if (fused_sc(u)) {
+            // a + sum_i k_i t_i in one chain (hyk_fuse.h)
+            const Ref FA = fz_a(u);
+            const std::vector<Ref> FX = fz_x(u);
+            const std::vector<double> &FK = fz_k(u);
+            std::string r = FA.kind == HYK_ARG_U ? cf(FA, n, n) : "";
+            for (size_t i = 0; i < FX.size(); ++i) {
+                flops += r.empty() ? 1 : 2;
+                r = r.empty() ? mul(lit(FK[i]), cf(FX[i], n, n)) : fma(lit(FK[i]), cf(FX[i], n, n), r);
+            }
+            def(u, n, r);
+            return;
+        }
         if (fused(u)) {
             // a + sum_i x_i^2 in one chain (hyk_fuse.h)
             const Ref FA = fz_a(u);
@@ -1087,6 +1105,14 @@ struct Gen {
         if (unary_fn && m >= 1 && !varying(A)) return;
         const std::string G = ub(u), H = hfac(u), inv = "i" + std::to_string(u);
         std::vector<std::pair<std::string, std::string>> t;
+        if (fused_sc(u)) {
+            // c_n = a_n + sum_i k_i t_i,n: abar_m += cbar_m, tbar_i,m += k_i cbar_m
+            const Ref FA = fz_a(u);
+            const std::vector<Ref> FX = fz_x(u);
+            if (FA.kind == HYK_ARG_U) contrib(FA, m, G);
+            for (size_t i = 0; i < FX.size(); ++i) contrib(FX[i], m, G, lit(fz_k(u)[i]));
+            return;
+        }
         if (fused(u)) {
             // c_n = a_n + sum_i sum_j x_i,j x_i,n-j: abar_m += cbar_m,
             // xbar_i,m += 2 sum_{n>=m} cbar_n x_i,n-m
@@ -1372,6 +1398,7 @@ struct TeamGen {
     std::vector<std::vector<Group>> levels;  // [level - 1]
     std::vector<Group> supd;                 // state updates
     std::vector<double> alphas;              // distinct pow exponents
+    std::vector<double> scales;              // the leaves' numbers of the sums of scaled terms
     std::string err;
     std::ostringstream o;
     // Unrolling of the convolution loops over j (the same sequence of fused
@@ -1504,8 +1531,9 @@ struct TeamGen {
             const Ref A = AB.first, B = AB.second;
             std::string key = "op" + std::to_string(op.op) + "_" + rkey(A) + "_" + rkey(B) + "_c" +
                               (g.cst[u] ? "K" : (g.hist[u] ? "h" : "c")) + (g.needka[u] ? "k" : "");
-            if (g.fused(u)) {  // a sum of squares: its leaves' kinds (the first is B)
-                key += "_F";
+            if (g.fused(u)) {  // a fused sum: its leaves' kinds (the first is B)
+                if (g.fused_sc(u)) key = "op" + std::to_string(HYK_OP_ADD) + "_" + rkey(A) + "_" + rkey(B) + "_S";
+                else key += "_F";
                 for (const Ref &x : g.fz_x(u)) key += rkey(x);
             }
             if (op.op == HYK_OP_POW) {
@@ -1597,10 +1625,16 @@ struct TeamGen {
                     if (A.kind == HYK_ARG_NUM) D.num = A.num;
                     if (B.kind == HYK_ARG_NUM && op.op != HYK_OP_POW) D.num = B.num;
                     if (g.fused(u)) {
-                        // a sum of squares: the leaves' slots in b, inv, prt, x3
+                        // a fused sum: the leaves' slots in b, inv, prt, x3; a
+                        // sum of scaled terms the offset of its leaves' numbers
+                        // in hyk_tsc in ka
                         const std::vector<Ref> X = g.fz_x(u);
                         int *f[HYK_FUSE_MAX] = {&D.b, &D.inv, &D.prt, &D.x3};
                         for (size_t i = 0; i < X.size(); ++i) *f[i] = tslot[X[i].u];
+                        if (g.fused_sc(u)) {
+                            D.ka = (int)scales.size();
+                            for (double k : g.fz_k(u)) scales.push_back(k);
+                        }
                     }
                     descs.push_back(D);
                 }
@@ -1640,7 +1674,7 @@ struct TeamGen {
                 const Ref A = g.res(op.a), B = g.res(op.b);
                 bool conv = false;
                 if (g.fused(gr.members[0])) {
-                    add(gr, 0.5 * p);
+                    add(gr, g.fused_sq(gr.members[0]) ? 0.5 * p : 1.0);
                     continue;
                 }
                 switch (op.op) {
@@ -1711,6 +1745,22 @@ struct TeamGen {
         o << "#pragma unroll 1\n";
         o << "        for (int q = r; q < " << gr.members.size() << "; q += HYK_TEAM) {\n";
         o << "            const hyk_tdesc &D = hyk_td[" << gr.off << " + q];\n";
+        if (g.fused_sc(u)) {
+            // a + sum_i k_i t_i in one chain (hyk_fuse.h), the lane form's
+            // arithmetic; the leaves' slots are in D.b, D.inv, D.prt, D.x3,
+            // their numbers in hyk_tsc from D.ka
+            const std::vector<Ref> X = g.fz_x(u);
+            const char *lf[HYK_FUSE_MAX] = {"D.b", "D.inv", "D.prt", "D.x3"};
+            std::string r = A.kind == HYK_ARG_U ? cur(A, 'a', n0) : "";
+            for (size_t i = 0; i < X.size(); ++i) {
+                const std::string x = "S[" + std::string(lf[i]) + ((n0 || !g.hist[X[i].u]) ? "]" : " + n]");
+                const std::string k = "hyk_tsc[D.ka + " + std::to_string(i) + "]";
+                r = r.empty() ? "HYK_MUL(" + k + ", " + x + ")" : fma_ + "(" + k + ", " + x + ", " + r + ")";
+            }
+            out(u, n0, r);
+            o << "        }\n";
+            return;
+        }
         if (g.fused(u)) {
             // a + sum_i x_i^2 in one chain (hyk_fuse.h), the lane form's arithmetic;
             // the leaves' slots are in D.b, D.inv, D.prt, D.x3
@@ -1959,13 +2009,17 @@ struct TeamGen {
     }
 
     void emit() {
-        // (a fused sum of squares keeps its leaves' slots in b, inv, prt, x3)
+        // (a fused sum keeps its leaves' slots in b, inv, prt, x3)
         o << "struct hyk_tdesc {\n    int a, b, c, ka, kc, inv, prt, x3;\n    hyk_real num;\n};\n";
         o << "static __device__ const hyk_tdesc hyk_td[" << std::max<size_t>(descs.size(), 1) << "] = {\n";
         for (const auto &D : descs)
             o << "    {" << D.a << ", " << D.b << ", " << D.c << ", " << D.ka << ", " << D.kc << ", " << D.inv << ", "
               << D.prt << ", " << D.x3 << ", " << lit(D.num) << "},\n";
         if (descs.empty()) o << "    {0, 0, 0, 0, 0, 0, 0, 0, " << lit(0.0) << "},\n";
+        o << "};\n";
+        o << "static __device__ const hyk_real hyk_tsc[" << std::max<size_t>(scales.size(), 1) << "] = {";
+        for (size_t i = 0; i < scales.size(); ++i) o << (i ? ", " : "") << lit(scales[i]);
+        if (scales.empty()) o << lit(0.0);
         o << "};\n";
         o << "static __constant__ hyk_real hyk_invn[" << (p + 2) << "] = {" << lit(0.0);
         for (uint32_t k = 1; k <= p + 1; ++k) o << ", " << lit(recip((double)k));

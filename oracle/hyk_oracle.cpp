@@ -308,8 +308,9 @@ template <typename T> struct Batch {
     // parameter or such an operation) have only an order-0 value, their
     // higher orders are known zeros (the kernels' code generator does the same).
     std::vector<char> cst;
-    // gpu arithmetic: a + x^2 computed as one chain where the kernels' code
-    // generator does so (hyk_fuse.h); the absorbed square is not computed.
+    // gpu arithmetic: sums of squares and sums of scaled terms computed as
+    // one chain where the kernels' code generator does so (hyk_fuse.h); the
+    // absorbed squares, products, negations and sums are not computed.
     HykFusePlan fz;
 
     // md: bit 0 = gpu arithmetic, bit 1 = high accuracy.
@@ -445,6 +446,20 @@ template <typename T> struct Batch {
         std::vector<T> &acc = s_acc;
         bool first = true;
         if (!fz.dead.empty() && fz.dead[k]) return;  // absorbed by a fused sum
+        if (!fz.fuse.empty() && fz.fuse[k] == HYK_FUSE_SC) {
+            // c_n = a_n + sum_i k_i t_i,n (hyk_fuse.h): c = a_n (k_1 t_1,n
+            // without a), then c = fma(k_i, t_i,n, c) leaf by leaf
+            const bool ha = fz.addend[k] >= 0;
+            const T *a = ha ? jr((uint32_t)fz.addend[k], n) : nullptr;
+            for (size_t i = 0; i < fz.leaves[k].size(); ++i) {
+                const T kk = T(fz.scales[k][i]);
+                const T *x = jr((uint32_t)fz.leaves[k][i], n);
+                for (uint32_t l = 0; l < B; ++l)
+                    c[l] = i == 0 ? (ha ? M<T>::fma(kk, x[l], a[l]) : kk * x[l]) : M<T>::fma(kk, x[l], c[l]);
+            }
+            set_ka(u, n);
+            return;
+        }
         if (!fz.fuse.empty() && fz.fuse[k]) {
             // c_n = a_n + sum_i (x_i^2)_n (hyk_fuse.h): s = sum_i sum_{j < n/2}
             // x_i,j x_i,n-j, c = fma(2, s, a_n) (s + s without a), then

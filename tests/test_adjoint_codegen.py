@@ -84,6 +84,21 @@ def test_adjoint_step_every_operation(libhyk):
     _check(_host(libhyk, sys_, 12), [1.1, 0.8], [0.3, 0.5], 0.4, 0.05)
 
 
+def test_adjoint_step_scaled_sums(libhyk):
+    """Sums of scaled terms computed as one chain (a difference, a negation,
+    four terms and a fifth added to them) and the 6-body problem whose
+    accelerations they are."""
+    x, y, z = hyk.make_vars("x", "y", "z")
+    sys_ = [
+        (x, 2.0 * y - 3.0 * z),
+        (y, -(4.0 * x) + z * x),
+        (z, 0.5 * (x * y) + 0.25 * (y * z) - 0.125 * (z * x) + 1.5 * hyk.square(y) + 0.75 * x),
+    ]
+    _check(_host(libhyk, sys_, 12), [0.3, -0.2, 0.5], [], 0.0, 0.1)
+    st, _ = W.oss_ics(1, seed=4)
+    _check(_host(libhyk, W.oss_sys(), 19), st[:, 0], [], 0.0, 50.0)
+
+
 def test_per_order_functions_bitwise_vs_oracle(libhyk, oracle):
     """A system large enough for the one-function-per-order form (5-body
     problem, 160 u-operations at order 19): the host build of the generated
