@@ -1381,6 +1381,19 @@ struct TeamGen {
     Gen g;  // alias folding, histories and j*a_j needs (gpu arithmetic, no adjoint)
     const Dec &d;
     uint32_t p, N, NU;
+    // Cold state rows (when every state variable is read by the recurrences
+    // at the current order only, as in the N-body problem): each state
+    // variable keeps two shared-memory slots, order n in slot n & 1 (order 0
+    // is copied in at the start of the step; the update of order n writes
+    // order n + 1 into the other slot, so that the updates that read a state
+    // variable, x' = v, still find its order n), and all its orders 0..p live
+    // in the team's region of the module's global buffer, order-major
+    // (HYK_CROW(i, n)), where the step size, the state update and the
+    // outputs read them.
+    bool cold = false;
+    bool coldvar(uint32_t u) const { return cold && u < N; }
+    // Whether u's history is in shared memory (slot + n) rather than its current order only.
+    bool th(uint32_t u) const { return g.hist[u] && !(cold && u < N); }
     uint32_t XS, HS, KS;  // strides of state rows, operation histories, j*a_j histories (odd)
     std::vector<int> tslot, tkslot, tislot, level;
     uint32_t nslot = 0, par_slot = 0;
@@ -1406,9 +1419,11 @@ struct TeamGen {
     // best on the 6-body problem against 1, 2 and 8).
     int ju = 4;
 
-    TeamGen(const Dec &dd, uint32_t order)
+    TeamGen(const Dec &dd, uint32_t order, bool cold_rows = false)
         : g(dd, order, false, false), d(dd), p(order), N(dd.n_eq), NU(dd.n_u()) {
-        XS = (p + 1) | 1u;
+        cold = cold_rows;
+        for (uint32_t i = 0; i < N; ++i) cold = cold && !g.hread[i];
+        XS = cold ? 2u : (p + 1) | 1u;
         HS = p | 1u;
         KS = (p >= 2 ? p - 1 : 1) | 1u;
         tslot.assign(NU, -1);
@@ -1498,7 +1513,7 @@ struct TeamGen {
     std::string rkey(const Ref &r) const {
         if (r.kind == HYK_ARG_U && g.cst[r.u]) return std::string("3") + (r.neg ? "n" : "p");
         std::string k = std::to_string(r.kind);
-        if (isU(r)) k += std::string(r.neg ? "n" : "p") + (g.hist[r.u] ? "h" : "c");
+        if (isU(r)) k += std::string(r.neg ? "n" : "p") + (coldvar(r.u) ? "d" : th(r.u) ? "h" : "c");
         return k;
     }
 
@@ -1651,6 +1666,7 @@ struct TeamGen {
                 const Ref R = g.res(d.rhs[i]);
                 Desc D;
                 D.a = slot_of(R);
+                D.b = (int)i;  // (cold rows: the state index)
                 D.c = tslot[i];
                 D.kc = tkslot[i];
                 if (R.kind == HYK_ARG_NUM) D.num = R.num;
@@ -1691,13 +1707,20 @@ struct TeamGen {
 
     // ---- expressions (D = the thread's descriptor, n = the order)
     static std::string wrap(const Ref &r, const std::string &s) { return r.neg ? "(-" + s + ")" : s; }
+    // The current order of u-variable u (not time-constant) whose slot is in
+    // the expression fld: its history's order n, its only slot, or (a cold
+    // state variable) slot n & 1.
+    std::string now(uint32_t u, const std::string &fld, bool n0) const {
+        if (n0 || (!th(u) && !coldvar(u))) return "S[" + fld + "]";
+        return coldvar(u) ? "S[" + fld + " + (n & 1)]" : "S[" + fld + " + n]";
+    }
     // Operand coefficient at the current order n (runtime) or at order 0.
     std::string cur(const Ref &r, char f, bool n0) const {
         const std::string fld = std::string("D.") + f;
         switch (r.kind) {
         case HYK_ARG_U:
             if (g.cst[r.u]) return n0 ? wrap(r, "S[" + fld + "]") : "";
-            return wrap(r, (n0 || !g.hist[r.u]) ? "S[" + fld + "]" : "S[" + fld + " + n]");
+            return wrap(r, now(r.u, fld, n0));
         case HYK_ARG_PAR:
             return n0 ? "S[" + fld + "]" : "";
         case HYK_ARG_NUM:
@@ -1753,7 +1776,7 @@ struct TeamGen {
             const char *lf[HYK_FUSE_MAX] = {"D.b", "D.inv", "D.prt", "D.x3"};
             std::string r = A.kind == HYK_ARG_U ? cur(A, 'a', n0) : "";
             for (size_t i = 0; i < X.size(); ++i) {
-                const std::string x = "S[" + std::string(lf[i]) + ((n0 || !g.hist[X[i].u]) ? "]" : " + n]");
+                const std::string x = now(X[i].u, lf[i], n0);
                 const std::string k = "hyk_tsc[D.ka + " + std::to_string(i) + "]";
                 r = r.empty() ? "HYK_MUL(" + k + ", " + x + ")" : fma_ + "(" + k + ", " + x + ", " + r + ")";
             }
@@ -1989,7 +2012,12 @@ struct TeamGen {
         else
             v = "HYK_MUL(" + f + ", hyk_invn[" + nn + "])";
         o << "            const hyk_real v = " << v << ";\n";
-        o << "            S[D.c + " << nn << "] = v;\n";
+        if (cold) {
+            o << "            S[D.c + " << (n0 ? "1" : "((n + 1) & 1)") << "] = v;\n";
+            o << "            HYK_CROW(D.b, " << nn << ") = v;\n";
+        } else {
+            o << "            S[D.c + " << nn << "] = v;\n";
+        }
         if (g.needka[i]) {
             if (n0)
                 o << "            if (1 < HYK_ORDER) S[D.kc] = " << lit(1.0) << " * v;\n";
@@ -2037,9 +2065,16 @@ struct TeamGen {
             }
             o << "};\n";
         }
-        o << "static __device__ __noinline__ void hyk_tjets(hyk_real *__restrict__ S, const hyk_real t0, const int r) {\n";
+        // (C: the team's cold rows, HYK_CROW(i, n) = C[n * HYK_NEQ + i]; unused without them)
+        o << "#define HYK_CROW(i, n) C[(n) * HYK_NEQ + (i)]\n";
+        o << "static __device__ __noinline__ void hyk_tjets(hyk_real *__restrict__ S, hyk_real *__restrict__ C, "
+             "const hyk_real t0, const int r) {\n";
         o << "    HYK_FMAOPS_CONSTS\n";
         o << "    __syncwarp();\n";
+        if (cold) {
+            o << "    for (int i = r; i < HYK_NEQ; i += HYK_TEAM) S[i * HYK_XS] = HYK_CROW(i, 0);\n";
+            o << "    __syncwarp();\n";
+        }
         o << "    {\n        // ---- order 0\n";
         emit_order(true);
         o << "    }\n";
@@ -2162,11 +2197,13 @@ bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err)
     }
     info.n_slot = tg.nslot | 1u;
     for (uint32_t T = 1; T <= 32; T *= 2) info.util[__builtin_ctz(T)] = tg.util(T);
+    TeamGen tc(d, order, true);
+    info.n_slot_cold = (tc.cold && tc.analyse()) ? (tc.nslot | 1u) : 0;
     return true;
 }
 
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc, bool f32, bool gmem) {
+                   std::string &err, bool high_acc, bool f32, bool gmem, bool cold) {
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
@@ -2176,7 +2213,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
         return false;
     }
     PrecisionScope prec(f32);
-    TeamGen tg(d, order);
+    TeamGen tg(d, order, cold && !gmem);
     if (!tg.analyse()) {
         err = tg.err;
         return false;
@@ -2190,7 +2227,7 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
       << d.n_ops << " u-operations, order " << order << "\n";
     h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
       << "\n#define HYK_TPB " << tpb << "\n#define HYK_TEAM " << team << "\n#define HYK_GMEM " << (gmem ? 1 : 0)
-      << "\n#define HYK_XS " << tg.XS
+      << "\n#define HYK_COLD " << (tg.cold ? 1 : 0) << "\n#define HYK_XS " << tg.XS
       << "\n#define HYK_NT " << nt << "\n#define HYK_NSLOT " << tg.nslot << "\n#define HYK_PAR_SLOT " << tg.par_slot
       << "\n#define HYK_RHOFAC " << lit(rhofac) << "\n#define HYK_INV_P " << lit(recip(p)) << "\n#define HYK_INV_PM1 "
       << lit(recip(p - 1.0)) << "\n";
@@ -2201,11 +2238,13 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
     h << kDmath << "\n";
     h << kCommon << "\n";
     h << "static_assert(sizeof(hyk_kparams) == " << kparams_size << ", \"hyk_kparams layout mismatch\");\n";
+    if (tg.cold) h << "extern \"C\" { __constant__ hyk_real *hyk_cold_base; }\n";
     tg.emit();
     h << tg.o.str() << "\n";
     h << kTeam << "\n";
     out.src = h.str();
     out.n_slot = nt;
+    out.n_cold = tg.cold ? d.n_eq : 0;
     out.par_slot = tg.par_slot;
     out.flops = tg.g.flops + 2.0 * d.n_eq * order + 46.0 + 10.0;
     return true;
@@ -2214,15 +2253,17 @@ bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, si
 // Host translation unit of the same generated recurrences (forward jets and,
 // with the adjoint, the reverse sweep) for CPU checks of the generator: one
 // lane, HYK_BLK = 1, the CUDA intrinsics mapped to their host equivalents.
-bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team, bool f32) {
+bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team, bool f32,
+                   bool cold) {
     PrecisionScope ps(f32);
     if (order < 2) {
         err = "the Taylor order must be at least 2";
         return false;
     }
     if (team) {
-        // The team form's recurrences run by a team of one thread.
-        TeamGen tg(d, order);
+        // The team form's recurrences run by a team of one thread (with cold
+        // state rows: in the array C of the translation unit).
+        TeamGen tg(d, order, cold);
         if (!tg.analyse()) {
             err = tg.err;
             return false;
@@ -2238,14 +2279,19 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
         h << "#define HYK_NEQ " << d.n_eq << "\n#define HYK_NPARS " << d.n_pars << "\n#define HYK_ORDER " << order
           << "\n#define HYK_TEAM 1\n#define HYK_XS " << tg.XS << "\n#define HYK_NSLOT " << tg.nslot
           << "\n#define HYK_PAR_SLOT " << tg.par_slot << "\n";
-        h << "#define HYK_SX(i, n) S[(i) * HYK_XS + (n)]\n#define HYK_PAR(k) S[HYK_PAR_SLOT + (k)]\n";
+        h << "static hyk_real C[HYK_NEQ * (HYK_ORDER + 1)];\n";
+        if (tg.cold)
+            h << "#define HYK_SX(i, n) C[(n) * HYK_NEQ + (i)]\n";
+        else
+            h << "#define HYK_SX(i, n) S[(i) * HYK_XS + (n)]\n";
+        h << "#define HYK_PAR(k) S[HYK_PAR_SLOT + (k)]\n";
         tg.emit();
         h << tg.o.str();
         h << "extern \"C\" int hyk_host_nslot(void) { return HYK_NSLOT; }\n";
         h << "extern \"C\" void hyk_host_step(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real h, hyk_real *x1) {\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
              "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
-             "    hyk_tjets(S, t0, 0);\n"
+             "    hyk_tjets(S, C, t0, 0);\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) {\n"
              "        hyk_real acc = HYK_SX(i, HYK_ORDER);\n"
              "        for (int n = HYK_ORDER - 1; n >= 0; --n) acc = HYK_FMA(acc, h, HYK_SX(i, n));\n"
@@ -2253,7 +2299,7 @@ bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src,
         h << "extern \"C\" void hyk_host_tc(hyk_real *S, const hyk_real *x0, const hyk_real *pars, hyk_real t0, hyk_real *tc) {\n"
              "    for (int i = 0; i < HYK_NEQ; ++i) HYK_SX(i, 0) = x0[i];\n"
              "    for (int k = 0; k < HYK_NPARS; ++k) HYK_PAR(k) = pars[k];\n"
-             "    hyk_tjets(S, t0, 0);\n"
+             "    hyk_tjets(S, C, t0, 0);\n"
              "    for (int i = 0; i < HYK_NEQ; ++i)\n"
              "        for (int n = 0; n <= HYK_ORDER; ++n) tc[i * (HYK_ORDER + 1) + n] = HYK_SX(i, n);\n}\n";
         src = h.str();

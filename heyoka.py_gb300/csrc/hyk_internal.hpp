@@ -52,18 +52,20 @@ bool generate(const Dec &d, uint32_t order, bool pin_arith, uint32_t blk, size_t
 // Team form (several threads per trajectory): slot count and the share of
 // busy threads over the rounds of one order for teams of 1, 2, 4, ..., 32.
 struct TeamInfo {
-    uint32_t n_slot = 0;  // doubles per trajectory (padded)
+    uint32_t n_slot = 0;       // doubles per trajectory (padded)
+    uint32_t n_slot_cold = 0;  // the same with cold state rows (0: the system has none)
     double util[6] = {0, 0, 0, 0, 0, 0};
 };
 // false (with the reason) when an operation has no team-form code.
 bool team_layout(const Dec &d, uint32_t order, TeamInfo &info, std::string &err);
 bool generate_team(const Dec &d, uint32_t order, uint32_t team, uint32_t tpb, size_t kparams_size, GenOut &out,
-                   std::string &err, bool high_acc = false, bool f32 = false, bool gmem = false);
+                   std::string &err, bool high_acc = false, bool f32 = false, bool gmem = false, bool cold = false);
 
 // Host (CPU) translation unit of the same recurrences, for checks of the
-// generator (team: the team form's recurrences, run by a team of one).
+// generator (team: the team form's recurrences, run by a team of one; cold:
+// with cold state rows where the system allows them).
 bool generate_host(const Dec &d, uint32_t order, bool adjoint, std::string &src, std::string &err, bool team = false,
-                   bool f32 = false);
+                   bool f32 = false, bool cold = false);
 
 // The recurrences in the reference's arithmetic over an element type chosen
 // by the includer (a vector of lanes for the compiled CPU stepper).

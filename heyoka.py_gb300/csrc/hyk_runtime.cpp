@@ -383,6 +383,25 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
         // one CTA per warp by default: finest packing of the shared memory;
         // with global-memory regions four warps per CTA
         if (m->gmem && blk == 0) blk = 128;
+        // Cold state rows (every state variable read at its current order
+        // only: the N-body problem): two shared-memory slots per state
+        // variable instead of p + 1, its orders in a global buffer of the
+        // module; taken when that fits more CTAs on an SM (the 6-body
+        // problem at order 19: 1593 slots instead of 2277, eight CTAs of two
+        // trajectories instead of six).
+        if (!m->gmem && ti.n_slot_cold && !(m->cfg.flags & HYK_CFG_NO_COLD_ROWS)) {
+            const size_t tpc = blk / m->team;
+            const size_t hot = tpc * ti.n_slot * real_bytes, cold = tpc * ti.n_slot_cold * real_bytes;
+            const uint32_t ch = hot > (size_t)dv.smem_optin ? 0 : (uint32_t)((size_t)dv.smem_per_sm / (hot + 1024));
+            const uint32_t cc = cold > (size_t)dv.smem_optin ? 0 : (uint32_t)((size_t)dv.smem_per_sm / (cold + 1024));
+            if (std::min<uint32_t>(cc, 32) > std::min<uint32_t>(ch, 32)) {
+                nslot = ti.n_slot_cold;
+                lane_bytes = (size_t)nslot * real_bytes;
+                m->ncold = m->d.n_eq;
+                m->cold_ctas = (int)std::min<uint32_t>(cc, 32);
+                m->cold_threads = (uint64_t)dv.n_sm * (uint64_t)m->cold_ctas * blk;
+            }
+        }
     } else if (m->gmem) {
         // The recurrences as one function per order (no spills), with their
         // own slots for the order-0 reciprocals.
@@ -475,7 +494,7 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     hyk::GenOut g;
     const bool high_acc = (m->cfg.flags & HYK_CFG_HIGH_ACCURACY) != 0;
     if (m->team) {
-        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32, m->gmem))
+        if (!hyk::generate_team(m->d, order, m->team, blk, sizeof(KParams), g, err, high_acc, f32, m->gmem, m->ncold != 0))
             return fail(HYK_ERR_INVALID, err);
     } else if (!hyk::generate(m->d, order, pin, blk, sizeof(KParams), g, err, adjoint, m->gmem ? m->gmem_threads : 0,
                               high_acc, f32, m->ncold ? m->cold_threads : 0, m->gmem)) {
@@ -526,7 +545,11 @@ int hyk_module_create(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (m->ncold) {
         // The cold rows' buffer and its address in the module's constant
         // hyk_cold_base (read by every kernel thread of the module).
-        HYK_CU(drv().cuMemAlloc(&m->jets, (size_t)m->cold_threads * m->ncold * order * real_bytes));
+        // (lane form: orders 1..p of each cold row per thread; team form:
+        // orders 0..p of every state variable per team)
+        const size_t cold_bytes = m->team ? (size_t)(m->cold_threads / m->team) * m->ncold * (order + 1) * real_bytes
+                                          : (size_t)m->cold_threads * m->ncold * order * real_bytes;
+        HYK_CU(drv().cuMemAlloc(&m->jets, cold_bytes));
         CUdeviceptr cb = 0;
         size_t cbytes = 0;
         HYK_CU(drv().cuModuleGetGlobal(&cb, &cbytes, m->mod, "hyk_cold_base"));
@@ -1101,7 +1124,8 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     }
     if (team > 1 && verbose == 3) {  // host translation unit of the team form
         std::string hs;
-        if (!hyk::generate_host(d, order, false, hs, err, true, f32)) return fail(HYK_ERR_UNSUPPORTED, err);
+        const bool cold = !(cfg->flags & HYK_CFG_NO_COLD_ROWS) && !(cfg->flags & HYK_CFG_GLOBAL_JETS);
+        if (!hyk::generate_host(d, order, false, hs, err, true, f32, cold)) return fail(HYK_ERR_UNSUPPORTED, err);
         if (log && log_len) std::snprintf(log, log_len, "%s", hs.c_str());
         return 0;
     }
@@ -1121,7 +1145,7 @@ int hyk_codegen_check(const hyk_decomp_t *dd, uint32_t order, const hyk_config_t
     if (team > 1) {
         const bool tg = (cfg->flags & HYK_CFG_GLOBAL_JETS) != 0;
         if (!hyk::generate_team(d, order, team, cfg->block_lanes ? cfg->block_lanes : (tg ? 128 : 32), sizeof(KParams),
-                                g, err, high_acc, f32, tg))
+                                g, err, high_acc, f32, tg, !(cfg->flags & HYK_CFG_NO_COLD_ROWS)))
             return fail(HYK_ERR_UNSUPPORTED, err);
     } else if (!hyk::generate(d, order, pin, blk, sizeof(KParams), g, err, adjoint, gstride, high_acc, f32, cstride,
                               gstride != 0)) {

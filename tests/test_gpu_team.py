@@ -163,3 +163,40 @@ def test_team_plain_compacted_and_in_place_identical(monkeypatch, gmem):
     inplace = run("plain")
     for r in (comp, inplace):
         assert np.array_equal(r[0], ref[0]) and r[1] == ref[1]
+
+
+@pytest.mark.parametrize("mode", ["persistent", "plain"])
+@pytest.mark.parametrize("team", [2, 4, 16])
+def test_team_cold_rows_bitwise(oracle, team, mode):
+    """6-body problem (every state variable read at its current order only):
+    the team form with cold state rows (two shared slots per state variable,
+    the orders in a global buffer per resident team) against the same form
+    without them and against the oracle, bit for bit.  More trajectories
+    than resident teams, so the step and plain kernels loop over them."""
+    st, _ = W.oss_ics(3000, seed=37)
+    a = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, prop_mode=mode, team_size=team)
+    ia = a.module_info
+    assert ia["team_size"] == team
+    assert ia["n_sm"] * ia["ctas_per_sm"] * ia["block_lanes"] // team < 3000
+    if team > 2:  # (two threads: 16 trajectories a CTA fit shared memory only with cold rows)
+        b = hyk.taylor_adaptive_batch(W.oss_sys(), st, tol=1e-15, prop_mode=mode, team_size=team, cold_rows=False)
+        assert ia["smem_per_lane"] < b.module_info["smem_per_lane"]
+        assert ia["ctas_per_sm"] > b.module_info["ctas_per_sm"]
+    else:
+        b = None
+    o = oracle.Oracle(W.oss_sys(), st[:, :8], order=a.order, mode=1)
+    a.step(write_tc=True)
+    o.step()
+    assert np.array_equal(np.asarray(a.state)[:, :8], o.state) and np.array_equal(a.tc[..., :8], o.tc)
+    if b is not None:
+        b.step(write_tc=True)
+        assert np.array_equal(a.tc, b.tc) and torch.equal(a.state, b.state)
+    grid = np.linspace(0.0, 3000.0, 7).reshape(-1, 1) + a.time.reshape(1, -1)
+    _, ga = a.propagate_grid(grid)
+    r = o.propagate_grid(grid[:, :8])
+    assert np.array_equal(ga[..., :8], r["grid"])
+    assert np.array_equal(np.asarray(a.state)[:, :8], o.state)
+    if b is not None:
+        _, gb = b.propagate_grid(grid)
+        assert np.array_equal(ga, gb) and torch.equal(a.state, b.state)
+        assert torch.equal(a.propagate_res_tensors["n_steps"], b.propagate_res_tensors["n_steps"])

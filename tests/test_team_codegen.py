@@ -23,9 +23,9 @@ from hyk.decompose import taylor_decompose
 pd = ctypes.POINTER(ctypes.c_double)
 
 
-def _team_host(libhyk, sys_, order, team=2):
+def _team_host(libhyk, sys_, order, team=2, flags=0):
     d, keep = taylor_decompose(sys_).as_c()
-    cfg = _lib.hyk_config_t(0, 0, 0, team)
+    cfg = _lib.hyk_config_t(0, 0, flags, team)
     buf = ctypes.create_string_buffer(1 << 24)
     rc = libhyk.hyk_codegen_check(ctypes.byref(d), order, ctypes.byref(cfg), 3, buf, len(buf), None, None)
     assert rc == 0, libhyk.hyk_last_error()
@@ -58,16 +58,27 @@ CASES = {
     "var2": lambda: (_var2().sys, np.concatenate([np.array([[0.2, 0.21], [0.3, 0.31]]), _var2().initial_variational_state(2)]),
                      np.array([[0.4, 0.41]]), 20),
     "consts": lambda: (_consts(), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6]]), 15),
+    # every state variable read at its current order only (cold state rows
+    # in the team form), x' = v among the updates, j x_j of a cold variable
+    "linear": lambda: (_linear(), np.array([[0.3, 0.2, 0.1], [0.5, 0.4, 0.6], [-0.2, 0.1, 0.3], [0.7, -0.5, 0.2]]), None, 14),
 }
 
 
-@pytest.mark.parametrize("form", ["team", "lane"])
+def _linear():
+    x, v, y, w = hyk.make_vars("x", "v", "y", "w")
+    # (sin(x) reads the j x_j of x, not its orders)
+    return [(x, v), (v, -2.0 * x + 0.5 * y - 0.25 * v), (y, w), (w, -y + 0.3 * x + 1.5 * hyk.sin(x))]
+
+
+@pytest.mark.parametrize("form", ["team", "team_hot", "lane"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_team_recurrences_bitwise_vs_oracle(libhyk, oracle, name, form):
     """Both forms' generated recurrences (lane form: the host build of the
-    per-lane code; team form: a team of one) against the oracle."""
+    per-lane code; team form: a team of one, with cold state rows where the
+    system allows them, and without) against the oracle."""
     sys_, st, pars, order = CASES[name]()
-    H = _team_host(libhyk, sys_, order, team=2 if form == "team" else 1)
+    H = _team_host(libhyk, sys_, order, team=1 if form == "lane" else 2,
+                   flags=_lib.HYK_CFG_NO_COLD_ROWS if form == "team_hot" else 0)
     o = oracle.Oracle(sys_, st, pars=pars, order=order, mode=1, time=np.full(st.shape[1], 0.25))
     _, h = o.step()
     S = np.zeros(H.hyk_host_nslot())
@@ -96,3 +107,21 @@ def test_team_form_rejects_unsupported_operand(libhyk):
     assert rc != 0 and b"non-variable argument" in libhyk.hyk_last_error()
     cfg = _lib.hyk_config_t(0, 0, 0, 1)
     assert libhyk.hyk_codegen_check(ctypes.byref(d), 10, ctypes.byref(cfg), 2, None, 0, None, None) == 0
+
+
+def test_cold_state_rows_layout(libhyk):
+    """The team form keeps two shared-memory slots per state variable when
+    every state variable is read at its current order only (6-body problem,
+    the linear system), and p + 1 otherwise (Kepler's positions are squared)."""
+    def slots(sys_, flags):
+        d, keep = taylor_decompose(sys_).as_c()
+        cfg = _lib.hyk_config_t(0, 0, flags, 16)
+        n = ctypes.c_uint32()
+        assert libhyk.hyk_codegen_check(ctypes.byref(d), 19, ctypes.byref(cfg), 2, None, 0, ctypes.byref(n), None) == 0
+        return n.value
+
+    for sys_, n_eq in ((W.oss_sys(), 36), (_linear(), 4)):
+        hot, cold = slots(sys_, _lib.HYK_CFG_NO_COLD_ROWS), slots(sys_, 0)
+        assert hot - cold == n_eq * (21 - 2), (hot, cold)
+    k = W.kepler_sys()
+    assert slots(k, 0) == slots(k, _lib.HYK_CFG_NO_COLD_ROWS)
