@@ -1055,8 +1055,8 @@ int hyk_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_
 }
 
 int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,
-                const int64_t *n_steps, double *lambda, double *pbar, void *workspace, size_t workspace_bytes,
-                void *stream) {
+                const int64_t *n_steps, const uint64_t *lane_order, double *lambda, double *pbar, void *workspace,
+                size_t workspace_bytes, void *stream) {
     NvtxRange nv("hyk: adjoint");
     int rc = check_lanes(m, lanes);
     if (rc) return rc;
@@ -1074,6 +1074,7 @@ int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, con
     k.ck_h = const_cast<double *>(ck_h);
     k.ck_cap = (uint64_t)INT64_MAX;  // the caller's tape holds n_steps[lane] steps for every lane
     k.adj_steps = n_steps;
+    k.lane_order = lane_order;
     k.adj_lambda = lambda;
     k.adj_pbar = pbar;
     k.queue = reinterpret_cast<uint64_t *>(workspace);

@@ -167,7 +167,7 @@ SIGNATURES = {
         [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_vp, ctypes.c_size_t, c_u32, P(c_u64), c_vp],
     ),
     "hyk_propagate_noalloc": (c_int, [c_vp, P(hyk_lanes_t), P(hyk_prop_t), c_int, c_u32, P(c_u64), c_vp]),
-    "hyk_adjoint": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_size_t, c_vp]),
+    "hyk_adjoint": (c_int, [c_vp, P(hyk_lanes_t), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_size_t, c_vp]),
     "hyk_dense_eval": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_dense_eval_f32": (c_int, [c_vp, c_u32, c_u32, c_u64, c_u64, c_vp, c_vp, c_vp]),
     "hyk_fp64_peak": (c_int, [c_int, c_d, P(c_d)]),

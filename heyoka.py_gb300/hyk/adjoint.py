@@ -28,6 +28,9 @@ from .core import get_module, lanes_struct, stream_handle
 from .decompose import order_from_tol, taylor_decompose
 
 EPS = 2.220446049250313e-16
+# The reverse sweep takes its lanes longest tape first (the order changes the
+# schedule only, never a lane's arithmetic).
+LONGEST_FIRST = True
 
 
 def _propagate_taped(mod, x, pars, t0, tf, cap=64):
@@ -103,12 +106,16 @@ class _TaylorFlow(torch.autograd.Function):
         dummy_t = torch.zeros(B, dtype=torch.float64, device=lam.device)
         lanes = lanes_struct(lam, p if ctx.has_pars else None, dummy_t, dummy_t)
         with torch.cuda.device(lam.device):
+            # longest tape first: the last lanes taken are the short ones
+            order = torch.argsort(n_iter, descending=True) if LONGEST_FIRST else None
             _lib.check(
                 L.hyk_adjoint(mod.handle, lanes, ck_x.data_ptr(), ck_t.data_ptr(), ck_h.data_ptr(), n_iter.data_ptr(),
-                              lam.data_ptr(), pbar.data_ptr() if npar else None, mod.ws.data_ptr(), mod.ws_bytes,
+                              order.data_ptr() if order is not None else None, lam.data_ptr(),
+                              pbar.data_ptr() if npar else None, mod.ws.data_ptr(), mod.ws_bytes,
                               stream_handle(lam.device.index)),
                 "hyk_adjoint",
             )
+            del order
         return lam, (pbar[:npar] if ctx.has_pars else None), None, None, None, None
 
 

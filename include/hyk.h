@@ -421,13 +421,17 @@ int hyk_memcpy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_
  * Taylor recurrences in reverse, with the taped step sizes held fixed.
  *   lambda: (n_eq, ld) in: dL/dx(t_final); out: dL/dx(t_0)
  *   pbar:   (n_pars, ld) out: dL/dpars (NULL when n_pars == 0)
+ *   lane_order: NULL (lanes in index order), or a permutation of
+ *           0..n_lanes-1 in device memory, the order in which the threads
+ *           take the lanes (longest tape first keeps the tail short);
+ *           indices >= n_lanes are skipped
  * workspace: hyk_propagate_workspace_size() bytes, 256-byte aligned.
  * Gradient of the reference's propagation, which has no adjoint: no
  * counterpart in the reference (it offers forward variational equations,
  * heyoka/expose_var_ode_sys.cpp:29-59). */
 int hyk_adjoint(hyk_module *m, const hyk_lanes_t *lanes, const double *ck_x, const double *ck_t, const double *ck_h,
-                const int64_t *n_steps, double *lambda, double *pbar, void *workspace, size_t workspace_bytes,
-                void *stream);
+                const int64_t *n_steps, const uint64_t *lane_order, double *lambda, double *pbar, void *workspace,
+                size_t workspace_bytes, void *stream);
 
 /* Dense output: out[i][l] = sum_n tc[i][n][l] * dt[l]^n (Horner), the
  * evaluator behind update_d_output / continuous output

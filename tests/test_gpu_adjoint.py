@@ -135,3 +135,23 @@ def test_cr3bp_gradient_vs_variational_equations_t50_256(libhyk, oracle):
     rel_x = np.max(np.abs(grad[:6] - gx), axis=0) / np.max(np.abs(grad[:6]), axis=0)
     rel_p = np.abs(grad[6] - gp[0]) / np.abs(grad[6])
     assert rel_x.max() < 1e-8 and rel_p.max() < 1e-8, (rel_x.max(), rel_p.max())
+
+
+def test_longest_first_order_same_bits(libhyk):
+    """The reverse sweep's lane order (longest tape first, or index order)
+    changes the schedule only: the gradients are the same bits."""
+    st, mu = W.cr3bp_ics(3000, seed=41)
+    tf = np.exp(np.random.default_rng(5).uniform(0.0, np.log(20.0), 3000))
+    grads = []
+    for lpt in (True, False):
+        adjoint.LONGEST_FIRST = lpt
+        try:
+            x = torch.tensor(st, device="cuda", requires_grad=True)
+            p = torch.tensor(mu, device="cuda", requires_grad=True)
+            xf, _ = adjoint.taylor_flow(W.cr3bp_sys(), x, torch.tensor(tf, device="cuda"), pars=p, tol=1e-15)
+            (xf[:3] ** 2).sum().backward()
+            grads.append((x.grad.cpu().numpy(), p.grad.cpu().numpy()))
+        finally:
+            adjoint.LONGEST_FIRST = True
+    assert np.array_equal(grads[0][0], grads[1][0]) and np.array_equal(grads[0][1], grads[1][1])
+    assert np.all(np.isfinite(grads[0][0]))
