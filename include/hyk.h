@@ -131,11 +131,14 @@ typedef struct hyk_config {
 #define HYK_CFG_GLOBAL_JETS 8u   /* one thread per trajectory with the Taylor coefficients in global memory
                                     (chosen automatically for systems that leave fewer than two warps
                                     per SM in shared memory) */
-#define HYK_CFG_NO_COLD_ROWS 32u /* lane form: keep every state variable's coefficients in shared memory.
-                                    By default the variables that no recurrence reads at a later order
-                                    keep orders 1..p in a module-owned global buffer when that lets more
-                                    lanes share an SM (the module's calls must then be ordered on one
-                                    stream, as with HYK_CFG_GLOBAL_JETS) */
+#define HYK_CFG_NO_COLD_ROWS 32u /* keep every state variable's coefficients in shared memory.
+                                    By default, when that lets more lanes (trajectories) share an SM,
+                                    the lane form keeps orders 1..p of the variables that no recurrence
+                                    reads at a later order in a module-owned global buffer, and the team
+                                    form, when no recurrence reads any state variable at a later order,
+                                    keeps two shared slots per state variable and all orders in that
+                                    buffer (the module's calls must then be ordered on one stream, as
+                                    with HYK_CFG_GLOBAL_JETS) */
 #define HYK_CFG_DEBUG 64u        /* debug build of the module's kernels (slower): lane indices taken from a
                                     lane list or a serving ring are checked against n_lanes, and a Taylor
                                     coefficient of a state variable that is not finite is recorded with
